@@ -1,0 +1,225 @@
+/*
+ * mosaic_gpu.h -- C ABI of the GB300 (sm_103a) tile matching-and-placement
+ * library, a drop-in for mosaic-art-rust's hot path.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (MG_OK = 0); on failure
+ *     mg_last_error() gives a message for the calling thread.  Nothing aborts,
+ *     traps or unwinds across this boundary.
+ *   - Host buffers belong to the caller and are never freed by the library.
+ *     Device buffers belong to the context (mg_ctx) or to a plan (mg_plan).
+ *   - RGB8 images are interleaved, row-major, `stride` bytes between rows.
+ *   - Lab colours are float triples (L, a, b).  Material identity is an int
+ *     index; a grid cell holding -1 has no tile (the reference's
+ *     Option<PathBuf> = None).
+ *   - A context is externally synchronised: one thread at a time.  All work of
+ *     a context runs on its own CUDA stream; calls with host outputs return
+ *     after the results are on the host.
+ *
+ * Each declaration cites the reference interface it replaces
+ * (path:line inside naporin0624/mosaic-art-rust).
+ */
+#ifndef MOSAIC_GPU_H
+#define MOSAIC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MG_OK 0
+#define MG_ERR_ARG 1     /* invalid argument (size, null pointer, empty grid) */
+#define MG_ERR_OOM 2     /* device or pinned-host allocation failed */
+#define MG_ERR_CUDA 3    /* a CUDA runtime call failed */
+#define MG_ERR_TIMEOUT 4 /* a bounded wait inside a kernel ran out */
+#define MG_ERR_BUDGET 5  /* request does not fit the device-memory budget */
+#define MG_ERR_STATE 6   /* call not valid in the object's current state */
+
+#define MG_SIM_FULL 0       /* P x P, symmetric, zero diagonal */
+#define MG_SIM_TRIANGULAR 1 /* strict upper triangle, row order (similarity.rs:38-41) */
+
+typedef struct mg_ctx mg_ctx;
+typedef struct mg_plan mg_plan;
+
+/* ---- library, context, memory --------------------------------------------- */
+int mg_version(void);
+const char* mg_last_error(void);
+/* Number of kernels this library has launched in the process. */
+unsigned long long mg_kernel_launches(void);
+int mg_ctx_create(int device, mg_ctx** out);
+int mg_ctx_destroy(mg_ctx* ctx);
+int mg_ctx_sync(mg_ctx* ctx);
+/* Pinned host memory (for fast host<->device copies); NULL on failure. */
+void* mg_host_alloc(size_t bytes);
+void mg_host_free(void* p);
+
+/* ---- colour statistics ------------------------------------------------------ */
+/* lib.rs:94-119 MosaicGenerator::calculate_average_lab: mean of per-pixel Lab. */
+int mg_average_lab(mg_ctx* ctx, const uint8_t* rgb, int w, int h, int64_t stride, float lab[3]);
+/* lib.rs:121-123 MosaicGenerator::is_aspect_ratio_match (returns 0 or 1). */
+int mg_is_aspect_ratio_match(float img_aspect, float target_aspect, float tolerance);
+/* main.rs:495-496, 537-541 (cell crop + calculate_average_lab) and main.rs:687-708
+ * (calculate_average_rgb) for every cell of a gw x gh grid, cell size
+ * (w/gw) x (h/gh).  lab_out: gw*gh*3 floats; avg_rgb_out (nullable): gw*gh*3. */
+int mg_cells_lab(mg_ctx* ctx, const uint8_t* img, int w, int h, int64_t stride, int gw, int gh,
+                 float* lab_out, uint8_t* avg_rgb_out);
+/* main.rs:193-208, 244-253 (process_tile -> calculate_average_lab for each
+ * material) in one launch.  lab_out: n*3; avg_rgb_out (nullable): n*3. */
+int mg_images_lab(mg_ctx* ctx, const uint8_t* const* imgs, const int* w, const int* h,
+                  const int64_t* stride, int n, float* lab_out, uint8_t* avg_rgb_out);
+/* main.rs:166-261 load_tiles selection (aspect filter in input order, the
+ * unfiltered fallback of main.rs:215-253, truncation to max_materials).
+ * Writes the chosen material indices to `selected`; returns the count (>= 0)
+ * or -MG_ERR_ARG. */
+int mg_select_palette(const int* widths, const int* heights, int n, float target_aspect,
+                      float tolerance, int max_materials, int* selected);
+
+/* ---- similarity database --------------------------------------------------------- */
+/* similarity.rs:69-82 build_similarities (+ similarity.rs:141-146
+ * calculate_lab_distance) on the device.  layout MG_SIM_FULL or
+ * MG_SIM_TRIANGULAR; out: p*p or p*(p-1)/2 floats. */
+int mg_similarity_build(mg_ctx* ctx, const float* lab, int p, int layout, float* out);
+/* similarity.rs:141-146 calculate_lab_distance. */
+float mg_lab_distance(const float a[3], const float b[3]);
+
+/* ---- k nearest (replaces kiddo nearest_n, main.rs:145-151, 348-352) ---------- */
+/* For each of nq query Lab colours, the k nearest of p palette colours by
+ * squared Euclidean distance, ascending, ties to the lowest index.
+ * idx_out, dist_out: nq*k. */
+int mg_nearest_n(mg_ctx* ctx, const float* palette_lab, int p, const float* query_lab, int nq, int k,
+                 uint32_t* idx_out, float* dist_out);
+
+/* ---- adjacency ------------------------------------------------------------------ */
+/* adjacency.rs:63-88 calculate_penalty for n (candidate, x, y) triples
+ * (cxy: n*3 ints) against one grid; out: n floats (weighted). */
+int mg_penalty_batch(mg_ctx* ctx, const float* palette_lab, int p, const int32_t* grid, int gw, int gh,
+                     float weight, const int32_t* cxy, int n, float* out);
+/* adjacency.rs:91-130 calculate_total_cost (unweighted). */
+int mg_total_cost(mg_ctx* ctx, const float* palette_lab, int p, const int32_t* grid, int gw, int gh,
+                  float* out);
+/* adjacency.rs:133-214 calculate_swap_delta for n position pairs
+ * (pairs: n*4 ints x1, y1, x2, y2); out: n floats. */
+int mg_swap_delta_batch(mg_ctx* ctx, const float* palette_lab, int p, const int32_t* grid, int gw, int gh,
+                        const int32_t* pairs, int n, float* out);
+
+/* ---- greedy placement (main.rs:335-475 over the grid, main.rs:529-545) ------------ */
+typedef struct mg_place_config {
+  int max_usage_per_image;        /* main.rs:53-55, UsageTracker cap */
+  float adjacency_penalty_weight; /* main.rs:57-59; <= 0 disables the penalty */
+} mg_place_config;
+/* Row-major greedy placement from per-cell Lab colours.  grid_out: gw*gh
+ * palette indices (-1 only when p == 0).  n_resets (nullable): how many
+ * cells fell back to the global usage reset of main.rs:428. */
+int mg_place_greedy(mg_ctx* ctx, const float* palette_lab, int p, const float* cell_lab, int gw, int gh,
+                    const mg_place_config* cfg, int32_t* grid_out, int* n_resets);
+
+/* ---- annealing (optimizer.rs) ------------------------------------------------------ */
+typedef struct mg_sa_config {      /* optimizer.rs:7-27 OptimizationConfig + chains */
+  int64_t max_iterations;          /* default 1000 */
+  float initial_temperature;       /* default 100.0 */
+  float temperature_decay;         /* default 0.99995 */
+  int chains;                      /* independent chains, >= 1 */
+  uint64_t seed;                   /* Philox key */
+  uint32_t stream;                 /* Philox stream id (e.g. request id) */
+  int greedy_only;                 /* 1 = optimizer.rs:132-198 optimize_greedy */
+} mg_sa_config;
+typedef struct mg_sa_result {      /* optimizer.rs:203-221 OptimizationResult */
+  float initial_cost, final_cost, best_cost;
+  int64_t improved_count, accepted_count, iterations;
+  int best_chain;
+} mg_sa_result;
+void mg_sa_config_default(mg_sa_config* cfg);
+/* optimizer.rs:41-129 MosaicOptimizer::optimize, run as cfg->chains chains
+ * from the same start grid.  On return `grid` holds the final grid of the
+ * chain with the lowest final cost (ties: lowest chain).  per_chain
+ * (nullable): chains results; chain_grids (nullable): chains*gw*gh. */
+int mg_optimize(mg_ctx* ctx, const float* palette_lab, int p, int32_t* grid, int gw, int gh,
+                const mg_sa_config* cfg, mg_sa_result* best, mg_sa_result* per_chain, int32_t* chain_grids);
+/* optimizer.rs:205-220 OptimizationResult::improvement_percentage. */
+float mg_improvement_percentage(const mg_sa_result* r);
+
+/* ---- colour adjustment (color_adjustment.rs) ---------------------------------------- */
+typedef struct mg_color_adjustment { /* color_adjustment.rs:6-15 */
+  float brightness, contrast, hue_shift, saturation;
+} mg_color_adjustment;
+/* color_adjustment.rs:30-37 ColorAdjustment::new (clamps). */
+mg_color_adjustment mg_color_adjustment_new(float brightness, float contrast, float hue_shift,
+                                            float saturation);
+/* color_adjustment.rs:99-154 calculate_optimal_adjustment for n (tile, target)
+ * mean-RGB pairs (each n*3 bytes); out: n adjustments. */
+int mg_optimal_adjustment_batch(mg_ctx* ctx, const uint8_t* tile_rgb, const uint8_t* target_rgb, int n,
+                                float strength, mg_color_adjustment* out);
+/* color_adjustment.rs:40-51 apply_to_image (adjust_pixel of every pixel). */
+int mg_apply_adjustment(mg_ctx* ctx, const mg_color_adjustment* adj, const uint8_t* rgb, int w, int h,
+                        int64_t stride, uint8_t* out);
+/* main.rs:548-592 / 627-664: composite p thumbnails (p x th x tw x 3) into the
+ * (gw*tw) x (gh*th) output by grid (palette indices), colour-adjusting each
+ * cell when strength > 0 (cell_avg_rgb: gw*gh*3 target means). */
+int mg_composite(mg_ctx* ctx, const int32_t* grid, int gw, int gh, const uint8_t* thumbs, int p, int tw, int th,
+                 const uint8_t* cell_avg_rgb, float strength, uint8_t* out);
+
+/* ---- the whole generate_mosaic job (main.rs:105-164 new + main.rs:477-685) ------------ */
+typedef struct mg_request {
+  const uint8_t* target;          /* target RGB8 image */
+  int target_w, target_h;
+  int64_t target_stride;          /* 0 -> 3*target_w */
+  int n_materials;
+  const uint8_t* const* materials; /* n_materials RGB8 images (decoded tiles) */
+  const int* material_w;
+  const int* material_h;
+  const int64_t* material_stride;  /* nullable -> 3*w */
+  const uint8_t* thumbnails;       /* nullable: n_materials x tile_h x tile_w x 3, the resized tiles
+                                      (main.rs:549); NULL -> area-average resize on the device */
+  int tile_w, tile_h;              /* output tile size; 0 -> cell size (main.rs:495-496) */
+  int grid_w, grid_h;              /* main.rs:37-43 */
+  int max_materials;               /* main.rs:45-47 */
+  float aspect_tolerance;          /* main.rs:49-51 */
+  int max_usage_per_image;         /* main.rs:53-55 */
+  float adjacency_penalty_weight;  /* main.rs:57-59 */
+  float color_adjustment_strength; /* main.rs:77-79, clamped to [0,1] (main.rs:162) */
+  int enable_optimization;         /* main.rs:61-63 */
+  int64_t optimization_iterations; /* main.rs:65-67 */
+  float initial_temperature;       /* optimizer.rs:21 */
+  float temperature_decay;         /* optimizer.rs:22 */
+  int chains;                      /* annealing chains (>= 1) */
+  uint64_t seed;
+  uint32_t stream;
+  int build_similarity;            /* 1: build the P x P similarity DB (main.rs:120-143) */
+} mg_request;
+
+typedef struct mg_result {
+  int32_t* grid;          /* nullable, grid_w*grid_h: ORIGINAL material index or -1 */
+  uint8_t* image;         /* nullable, out_h x out_w x 3 */
+  int out_w, out_h;       /* set by the call */
+  int palette_size;       /* tiles kept by load_tiles */
+  int n_resets;           /* cells that used the global usage reset */
+  int best_chain;         /* -1 when the optimiser did not run */
+  float initial_cost, final_cost, best_cost;
+  int64_t accepted_count, improved_count;
+} mg_result;
+
+void mg_request_default(mg_request* req);
+/* One complete job from host buffers to host buffers. */
+int mg_generate(mg_ctx* ctx, const mg_request* req, mg_result* res);
+
+/* Device-resident form of the same job: mg_plan_create uploads the inputs
+ * (palette selection, target, selected materials, thumbnails) into device
+ * memory; mg_plan_run runs the whole device pipeline on them (no host copies);
+ * mg_plan_read copies results to the host. */
+int mg_plan_create(mg_ctx* ctx, const mg_request* req, mg_plan** out);
+int mg_plan_run(mg_plan* plan);
+int mg_plan_read(mg_plan* plan, mg_result* res);
+int mg_plan_destroy(mg_plan* plan);
+/* Device time of each stage of the last mg_plan_run, in ms (CUDA events):
+ * [0] material Lab, [1] similarity, [2] cell Lab, [3] nearest, [4] greedy,
+ * [5] anneal, [6] composite, [7] total.  Returns the count written. */
+int mg_plan_stage_ms(mg_plan* plan, float* ms, int cap);
+/* Number of kernels one mg_plan_run launches. */
+int mg_plan_launches(mg_plan* plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

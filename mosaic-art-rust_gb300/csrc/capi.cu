@@ -1,0 +1,996 @@
+// capi.cu -- the C ABI of mosaic_gpu.h: contexts, host<->device staging, the
+// per-stage entry points and the whole-job plan.
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "mg_internal.h"
+
+namespace mg {
+
+unsigned long long g_launches = 0;
+
+namespace {
+thread_local std::string g_error;
+}
+
+void set_error(const std::string& msg) { g_error = msg; }
+int fail(int code, const std::string& msg) {
+  set_error(msg);
+  return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? MG_ERR_OOM : MG_ERR_CUDA;
+}
+
+int DevBuf::ensure(size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (bytes <= cap) return MG_OK;
+  release();
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    cap = 0;
+    cudaGetLastError();
+    return fail(MG_ERR_OOM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+  }
+  cap = bytes;
+  return MG_OK;
+}
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+}
+
+}  // namespace mg
+
+using namespace mg;
+
+struct mg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DevBuf in0, in1, in2, out0, out1, out2, sums, regions, err;
+  mg_plan* gen_plan = nullptr;
+};
+
+struct mg_plan {
+  mg_ctx* ctx = nullptr;
+  // geometry and configuration
+  int W = 0, H = 0, gw = 0, gh = 0, cw = 0, ch = 0, tw = 0, th = 0, N = 0, P = 0, K = 0, k = 0;
+  int64_t iters = 0;
+  float weight = 0, strength = 0, t0 = 100.0f, decay = 0.99995f;
+  int max_usage = 0, enable_opt = 0, build_sim = 0, device_thumbs = 0, run_sa = 0;
+  uint64_t seed = 0;
+  uint32_t stream_id = 0;
+  std::vector<int> selected;
+  std::vector<Region> h_regions;
+  // device buffers
+  DevBuf target, mats, regions, thumb_regions, thumbs, pal_lab, thumb_rgb, sim, cell_lab, cell_rgb, cand_idx,
+      cand_dist, grid_greedy, resets, init_cost, greedy_job, chain_grids, chain_res, anneal_job, final_grid,
+      finals_ptr, best_chain, adj, out, sums, err;
+  cudaEvent_t ev[8] = {};
+  bool events = false;
+  int launches = 0;
+  bool ran = false;
+};
+
+namespace {
+
+int check_ctx(mg_ctx* ctx) {
+  if (!ctx) return fail(MG_ERR_ARG, "null context");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  return MG_OK;
+}
+
+std::vector<float4> to_f4(const float* lab3, int n) {
+  std::vector<float4> v((size_t)std::max(n, 1));
+  for (int i = 0; i < n; ++i) v[i] = make_float4(lab3[3 * i], lab3[3 * i + 1], lab3[3 * i + 2], 0.0f);
+  return v;
+}
+
+int upload(mg_ctx* ctx, DevBuf& b, const void* src, size_t bytes) {
+  MG_CHECK(b.ensure(bytes));
+  if (bytes) MG_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  return MG_OK;
+}
+
+int finish(mg_ctx* ctx) {
+  MG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (ctx->err.p) {
+    uint32_t e = 0;
+    MG_CUDA(cudaMemcpy(&e, ctx->err.p, 4, cudaMemcpyDeviceToHost));
+    if (e) {
+      MG_CUDA(cudaMemset(ctx->err.p, 0, 4));
+      return fail(MG_ERR_TIMEOUT, "a bounded wait inside a kernel ran out");
+    }
+  }
+  return MG_OK;
+}
+
+int ensure_err(mg_ctx* ctx) {
+  if (!ctx->err.p) {
+    MG_CHECK(ctx->err.ensure(16));
+    MG_CUDA(cudaMemsetAsync(ctx->err.p, 0, 16, ctx->stream));
+  }
+  return MG_OK;
+}
+
+bool valid_image(const void* p, int w, int h, int64_t stride) {
+  return p && w > 0 && h > 0 && stride >= 3ll * w;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mg_version(void) { return 10000; }
+const char* mg_last_error(void) { return g_error.c_str(); }
+unsigned long long mg_kernel_launches(void) { return g_launches; }
+
+int mg_ctx_create(int device, mg_ctx** out) {
+  if (!out) return fail(MG_ERR_ARG, "null out");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return fail(MG_ERR_CUDA, "no CUDA device available");
+  }
+  if (device < 0 || device >= n) return fail(MG_ERR_ARG, "device index out of range");
+  MG_CUDA(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  MG_CUDA(cudaGetDeviceProperties(&prop, device));
+  if (prop.major < 10) return fail(MG_ERR_CUDA, "this library is built for sm_103a (Blackwell Ultra)");
+  mg_ctx* c = new mg_ctx();
+  c->device = device;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  upload_lab_consts(c->stream);
+  int s = ensure_err(c);
+  if (s == MG_OK) s = finish(c);
+  if (s != MG_OK) {
+    mg_ctx_destroy(c);
+    return s;
+  }
+  *out = c;
+  return MG_OK;
+}
+
+int mg_ctx_destroy(mg_ctx* ctx) {
+  if (!ctx) return MG_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->gen_plan) mg_plan_destroy(ctx->gen_plan);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (DevBuf* b : {&ctx->in0, &ctx->in1, &ctx->in2, &ctx->out0, &ctx->out1, &ctx->out2, &ctx->sums, &ctx->regions,
+                    &ctx->err})
+    b->release();
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return MG_OK;
+}
+
+int mg_ctx_sync(mg_ctx* ctx) {
+  MG_CHECK(check_ctx(ctx));
+  return finish(ctx);
+}
+
+void* mg_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, bytes ? bytes : 16, cudaHostAllocPortable | cudaHostAllocMapped) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaHostAlloc failed");
+    return nullptr;
+  }
+  return p;
+}
+void mg_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+// ---- colour statistics ----------------------------------------------------------
+int mg_average_lab(mg_ctx* ctx, const uint8_t* rgb, int w, int h, int64_t stride, float lab[3]) {
+  MG_CHECK(check_ctx(ctx));
+  if (!lab || !valid_image(rgb, w, h, stride)) return fail(MG_ERR_ARG, "invalid image");
+  const size_t row = 3ull * w;
+  MG_CHECK(ctx->in0.ensure(row * h));
+  MG_CUDA(cudaMemcpy2DAsync(ctx->in0.p, row, rgb, stride, row, h, cudaMemcpyHostToDevice, ctx->stream));
+  Region r{0, w, h, (int64_t)row};
+  MG_CHECK(upload(ctx, ctx->regions, &r, sizeof(r)));
+  MG_CHECK(ctx->sums.ensure(sizeof(RegionSums)));
+  MG_CHECK(ctx->out0.ensure(sizeof(float4)));
+  MG_CHECK(launch_region_stats(ctx->in0.as<uint8_t>(), nullptr, ctx->regions.as<Region>(), 1, (int64_t)w * h,
+                               ctx->out0.as<float4>(), nullptr, ctx->sums.as<RegionSums>(), 1, ctx->stream));
+  float4 v;
+  MG_CUDA(cudaMemcpyAsync(&v, ctx->out0.p, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream));
+  MG_CHECK(finish(ctx));
+  lab[0] = v.x;
+  lab[1] = v.y;
+  lab[2] = v.z;
+  return MG_OK;
+}
+
+int mg_is_aspect_ratio_match(float img_aspect, float target_aspect, float tolerance) {
+  return std::fabs(img_aspect - target_aspect) <= tolerance ? 1 : 0;
+}
+
+int mg_cells_lab(mg_ctx* ctx, const uint8_t* img, int w, int h, int64_t stride, int gw, int gh, float* lab_out,
+                 uint8_t* avg_rgb_out) {
+  MG_CHECK(check_ctx(ctx));
+  if (!valid_image(img, w, h, stride) || !lab_out) return fail(MG_ERR_ARG, "invalid image");
+  if (gw <= 0 || gh <= 0 || w / gw <= 0 || h / gh <= 0) return fail(MG_ERR_ARG, "grid larger than the image");
+  const int n = gw * gh;
+  const size_t row = 3ull * w;
+  MG_CHECK(ctx->in0.ensure(row * h));
+  MG_CUDA(cudaMemcpy2DAsync(ctx->in0.p, row, img, stride, row, h, cudaMemcpyHostToDevice, ctx->stream));
+  CellGeom g{gw, gh, w / gw, h / gh, (int64_t)row};
+  MG_CHECK(ctx->sums.ensure(sizeof(RegionSums) * n));
+  MG_CHECK(ctx->out0.ensure(sizeof(float4) * n));
+  MG_CHECK(ctx->out1.ensure(sizeof(uchar4) * n));
+  MG_CHECK(launch_region_stats(ctx->in0.as<uint8_t>(), &g, nullptr, n, (int64_t)g.cw * g.ch, ctx->out0.as<float4>(),
+                               ctx->out1.as<uchar4>(), ctx->sums.as<RegionSums>(), 1, ctx->stream));
+  std::vector<float4> lab(n);
+  std::vector<uchar4> rgb(n);
+  MG_CUDA(cudaMemcpyAsync(lab.data(), ctx->out0.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  MG_CUDA(cudaMemcpyAsync(rgb.data(), ctx->out1.p, sizeof(uchar4) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  MG_CHECK(finish(ctx));
+  for (int i = 0; i < n; ++i) {
+    lab_out[3 * i] = lab[i].x;
+    lab_out[3 * i + 1] = lab[i].y;
+    lab_out[3 * i + 2] = lab[i].z;
+    if (avg_rgb_out) {
+      avg_rgb_out[3 * i] = rgb[i].x;
+      avg_rgb_out[3 * i + 1] = rgb[i].y;
+      avg_rgb_out[3 * i + 2] = rgb[i].z;
+    }
+  }
+  return MG_OK;
+}
+
+int mg_images_lab(mg_ctx* ctx, const uint8_t* const* imgs, const int* w, const int* h, const int64_t* stride, int n,
+                  float* lab_out, uint8_t* avg_rgb_out) {
+  MG_CHECK(check_ctx(ctx));
+  if (n < 0 || (n > 0 && (!imgs || !w || !h || !lab_out))) return fail(MG_ERR_ARG, "invalid image list");
+  if (n == 0) return MG_OK;
+  std::vector<Region> regs(n);
+  int64_t off = 0, maxpx = 0;
+  for (int i = 0; i < n; ++i) {
+    const int64_t st = stride ? stride[i] : 3ll * w[i];
+    if (!valid_image(imgs[i], w[i], h[i], st)) return fail(MG_ERR_ARG, "invalid image " + std::to_string(i));
+    regs[i] = Region{off, w[i], h[i], 3ll * w[i]};
+    off += 3ll * w[i] * h[i];
+    off = (off + 15) & ~15ll;
+    maxpx = std::max<int64_t>(maxpx, (int64_t)w[i] * h[i]);
+  }
+  MG_CHECK(ctx->in0.ensure((size_t)off));
+  for (int i = 0; i < n; ++i) {
+    const int64_t st = stride ? stride[i] : 3ll * w[i];
+    MG_CUDA(cudaMemcpy2DAsync(ctx->in0.as<uint8_t>() + regs[i].offset, 3ull * w[i], imgs[i], st, 3ull * w[i], h[i],
+                              cudaMemcpyHostToDevice, ctx->stream));
+  }
+  MG_CHECK(upload(ctx, ctx->regions, regs.data(), sizeof(Region) * n));
+  MG_CHECK(ctx->sums.ensure(sizeof(RegionSums) * n));
+  MG_CHECK(ctx->out0.ensure(sizeof(float4) * n));
+  MG_CHECK(ctx->out1.ensure(sizeof(uchar4) * n));
+  MG_CHECK(launch_region_stats(ctx->in0.as<uint8_t>(), nullptr, ctx->regions.as<Region>(), n, maxpx,
+                               ctx->out0.as<float4>(), ctx->out1.as<uchar4>(), ctx->sums.as<RegionSums>(), 1,
+                               ctx->stream));
+  std::vector<float4> lab(n);
+  std::vector<uchar4> rgb(n);
+  MG_CUDA(cudaMemcpyAsync(lab.data(), ctx->out0.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  MG_CUDA(cudaMemcpyAsync(rgb.data(), ctx->out1.p, sizeof(uchar4) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  MG_CHECK(finish(ctx));
+  for (int i = 0; i < n; ++i) {
+    lab_out[3 * i] = lab[i].x;
+    lab_out[3 * i + 1] = lab[i].y;
+    lab_out[3 * i + 2] = lab[i].z;
+    if (avg_rgb_out) {
+      avg_rgb_out[3 * i] = rgb[i].x;
+      avg_rgb_out[3 * i + 1] = rgb[i].y;
+      avg_rgb_out[3 * i + 2] = rgb[i].z;
+    }
+  }
+  return MG_OK;
+}
+
+int mg_select_palette(const int* widths, const int* heights, int n, float target_aspect, float tolerance,
+                      int max_materials, int* selected) {
+  if (n < 0 || max_materials < 0 || (n > 0 && (!widths || !heights || !selected))) return -MG_ERR_ARG;
+  int cnt = 0;
+  for (int i = 0; i < n; ++i) {
+    if (heights[i] <= 0 || widths[i] <= 0) return -MG_ERR_ARG;
+    const float a = (float)widths[i] / (float)heights[i];
+    if (mg_is_aspect_ratio_match(a, target_aspect, tolerance)) selected[cnt++] = i;
+  }
+  if (cnt == 0) {
+    const int64_t lim = std::min<int64_t>(n, 2ll * max_materials);
+    for (int64_t i = 0; i < lim; ++i) selected[cnt++] = (int)i;
+  }
+  return std::min(cnt, max_materials);
+}
+
+// ---- similarity --------------------------------------------------------------------
+int mg_similarity_build(mg_ctx* ctx, const float* lab, int p, int layout, float* out) {
+  MG_CHECK(check_ctx(ctx));
+  if (p < 0 || (p > 0 && (!lab || !out))) return fail(MG_ERR_ARG, "invalid palette");
+  if (layout != MG_SIM_FULL && layout != MG_SIM_TRIANGULAR) return fail(MG_ERR_ARG, "unknown layout");
+  if (p == 0) return MG_OK;
+  auto pal = to_f4(lab, p);
+  MG_CHECK(upload(ctx, ctx->in1, pal.data(), sizeof(float4) * p));
+  const size_t count = layout == MG_SIM_FULL ? (size_t)p * p : (size_t)p * (p - 1) / 2;
+  MG_CHECK(ctx->out0.ensure(sizeof(float) * count));
+  MG_CHECK(launch_similarity(ctx->in1.as<float4>(), p, layout == MG_SIM_TRIANGULAR, ctx->out0.as<float>(), ctx->stream));
+  if (count) MG_CUDA(cudaMemcpyAsync(out, ctx->out0.p, sizeof(float) * count, cudaMemcpyDeviceToHost, ctx->stream));
+  return finish(ctx);
+}
+
+float mg_lab_distance(const float a[3], const float b[3]) { return lab_distance(a[0], a[1], a[2], b[0], b[1], b[2]); }
+
+// ---- nearest --------------------------------------------------------------------------
+int mg_nearest_n(mg_ctx* ctx, const float* palette_lab, int p, const float* query_lab, int nq, int k,
+                 uint32_t* idx_out, float* dist_out) {
+  MG_CHECK(check_ctx(ctx));
+  if (p < 0 || nq < 0 || k <= 0 || k > 100) return fail(MG_ERR_ARG, "need p >= 0, nq >= 0, 1 <= k <= 100");
+  if (nq == 0) return MG_OK;
+  if (!query_lab || !idx_out || !dist_out || (p > 0 && !palette_lab)) return fail(MG_ERR_ARG, "null buffer");
+  MG_CHECK(ensure_err(ctx));
+  auto pal = to_f4(palette_lab, p);
+  auto q = to_f4(query_lab, nq);
+  MG_CHECK(upload(ctx, ctx->in1, pal.data(), sizeof(float4) * std::max(p, 1)));
+  MG_CHECK(upload(ctx, ctx->in2, q.data(), sizeof(float4) * nq));
+  MG_CHECK(ctx->out0.ensure(sizeof(uint32_t) * (size_t)nq * k));
+  MG_CHECK(ctx->out1.ensure(sizeof(float) * (size_t)nq * k));
+  MG_CHECK(launch_nearest(ctx->in1.as<float4>(), p, ctx->in2.as<float4>(), nq, k, ctx->out0.as<uint32_t>(),
+                          ctx->out1.as<float>(), ctx->err.as<uint32_t>(), ctx->stream));
+  if (p == 0) {
+    MG_CHECK(finish(ctx));
+    for (size_t i = 0; i < (size_t)nq * k; ++i) {
+      idx_out[i] = 0xFFFFFFFFu;
+      dist_out[i] = INFINITY;
+    }
+    return MG_OK;
+  }
+  MG_CUDA(cudaMemcpyAsync(idx_out, ctx->out0.p, sizeof(uint32_t) * (size_t)nq * k, cudaMemcpyDeviceToHost, ctx->stream));
+  MG_CUDA(cudaMemcpyAsync(dist_out, ctx->out1.p, sizeof(float) * (size_t)nq * k, cudaMemcpyDeviceToHost, ctx->stream));
+  return finish(ctx);
+}
+
+// ---- adjacency ----------------------------------------------------------------------------
+static int check_grid(const float* pal, int p, const int32_t* grid, int gw, int gh) {
+  if (gw <= 0 || gh <= 0 || !grid || p < 0 || (p > 0 && !pal)) return fail(MG_ERR_ARG, "invalid grid or palette");
+  for (int i = 0; i < gw * gh; ++i)
+    if (grid[i] < -1 || grid[i] >= p) return fail(MG_ERR_ARG, "grid entry out of palette range");
+  return MG_OK;
+}
+
+int mg_penalty_batch(mg_ctx* ctx, const float* palette_lab, int p, const int32_t* grid, int gw, int gh, float weight,
+                     const int32_t* cxy, int n, float* out) {
+  MG_CHECK(check_ctx(ctx));
+  MG_CHECK(check_grid(palette_lab, p, grid, gw, gh));
+  if (n < 0 || (n > 0 && (!cxy || !out))) return fail(MG_ERR_ARG, "invalid items");
+  if (n == 0) return MG_OK;
+  std::vector<int4> items(n);
+  for (int i = 0; i < n; ++i) {
+    items[i] = make_int4(cxy[3 * i], cxy[3 * i + 1], cxy[3 * i + 2], 0);
+    if (items[i].x < 0 || items[i].x >= p || items[i].y < 0 || items[i].y >= gw || items[i].z < 0 || items[i].z >= gh)
+      return fail(MG_ERR_ARG, "item out of range");
+  }
+  auto pal = to_f4(palette_lab, p);
+  MG_CHECK(upload(ctx, ctx->in0, pal.data(), sizeof(float4) * std::max(p, 1)));
+  MG_CHECK(upload(ctx, ctx->in1, grid, sizeof(int32_t) * gw * gh));
+  MG_CHECK(upload(ctx, ctx->in2, items.data(), sizeof(int4) * n));
+  MG_CHECK(ctx->out0.ensure(sizeof(float) * n));
+  MG_CHECK(launch_penalty(ctx->in0.as<float4>(), ctx->in1.as<int32_t>(), gw, gh, weight, ctx->in2.as<int4>(), n,
+                          ctx->out0.as<float>(), ctx->stream));
+  MG_CUDA(cudaMemcpyAsync(out, ctx->out0.p, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  return finish(ctx);
+}
+
+int mg_total_cost(mg_ctx* ctx, const float* palette_lab, int p, const int32_t* grid, int gw, int gh, float* out) {
+  MG_CHECK(check_ctx(ctx));
+  if (!out) return fail(MG_ERR_ARG, "null out");
+  if (gh == 0 || gw == 0) {  // adjacency.rs:92-95: an empty grid costs 0
+    *out = 0.0f;
+    return MG_OK;
+  }
+  MG_CHECK(check_grid(palette_lab, p, grid, gw, gh));
+  auto pal = to_f4(palette_lab, p);
+  MG_CHECK(upload(ctx, ctx->in0, pal.data(), sizeof(float4) * std::max(p, 1)));
+  MG_CHECK(upload(ctx, ctx->in1, grid, sizeof(int32_t) * gw * gh));
+  MG_CHECK(ctx->out0.ensure(sizeof(float)));
+  MG_CHECK(launch_total_cost(ctx->in0.as<float4>(), ctx->in1.as<int32_t>(), gw, gh, ctx->out0.as<float>(), ctx->stream));
+  MG_CUDA(cudaMemcpyAsync(out, ctx->out0.p, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  return finish(ctx);
+}
+
+int mg_swap_delta_batch(mg_ctx* ctx, const float* palette_lab, int p, const int32_t* grid, int gw, int gh,
+                        const int32_t* pairs, int n, float* out) {
+  MG_CHECK(check_ctx(ctx));
+  MG_CHECK(check_grid(palette_lab, p, grid, gw, gh));
+  if (n < 0 || (n > 0 && (!pairs || !out))) return fail(MG_ERR_ARG, "invalid pairs");
+  if (n == 0) return MG_OK;
+  for (int i = 0; i < n; ++i) {
+    const int* q = pairs + 4 * i;
+    if (q[0] < 0 || q[0] >= gw || q[2] < 0 || q[2] >= gw || q[1] < 0 || q[1] >= gh || q[3] < 0 || q[3] >= gh)
+      return fail(MG_ERR_ARG, "position out of range");
+  }
+  auto pal = to_f4(palette_lab, p);
+  MG_CHECK(upload(ctx, ctx->in0, pal.data(), sizeof(float4) * std::max(p, 1)));
+  MG_CHECK(upload(ctx, ctx->in1, grid, sizeof(int32_t) * gw * gh));
+  MG_CHECK(upload(ctx, ctx->in2, pairs, sizeof(int4) * n));
+  MG_CHECK(ctx->out0.ensure(sizeof(float) * n));
+  MG_CHECK(launch_swap_delta(ctx->in0.as<float4>(), ctx->in1.as<int32_t>(), gw, gh, ctx->in2.as<int4>(), n,
+                             ctx->out0.as<float>(), ctx->stream));
+  MG_CUDA(cudaMemcpyAsync(out, ctx->out0.p, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  return finish(ctx);
+}
+
+// ---- greedy --------------------------------------------------------------------------------
+int mg_place_greedy(mg_ctx* ctx, const float* palette_lab, int p, const float* cell_lab, int gw, int gh,
+                    const mg_place_config* cfg, int32_t* grid_out, int* n_resets) {
+  MG_CHECK(check_ctx(ctx));
+  if (!cfg || !cell_lab || !grid_out || gw <= 0 || gh <= 0 || p < 0 || (p > 0 && !palette_lab))
+    return fail(MG_ERR_ARG, "invalid arguments");
+  if (cfg->max_usage_per_image < 0) return fail(MG_ERR_ARG, "negative max usage");
+  const int n = gw * gh;
+  if (p == 0) {  // main.rs:341-345: no tiles -> nothing placed
+    for (int i = 0; i < n; ++i) grid_out[i] = -1;
+    if (n_resets) *n_resets = 0;
+    return MG_OK;
+  }
+  MG_CHECK(ensure_err(ctx));
+  const int k = std::min(p, 100);
+  auto pal = to_f4(palette_lab, p);
+  auto q = to_f4(cell_lab, n);
+  MG_CHECK(upload(ctx, ctx->in0, pal.data(), sizeof(float4) * p));
+  MG_CHECK(upload(ctx, ctx->in1, q.data(), sizeof(float4) * n));
+  MG_CHECK(ctx->out0.ensure(sizeof(uint32_t) * (size_t)n * k));
+  MG_CHECK(ctx->out1.ensure(sizeof(float) * (size_t)n * k));
+  MG_CHECK(ctx->out2.ensure(sizeof(int32_t) * n + 64));
+  MG_CHECK(launch_nearest(ctx->in0.as<float4>(), p, ctx->in1.as<float4>(), n, k, ctx->out0.as<uint32_t>(),
+                          ctx->out1.as<float>(), ctx->err.as<uint32_t>(), ctx->stream));
+  int32_t* d_grid = ctx->out2.as<int32_t>();
+  int* d_resets = reinterpret_cast<int*>(d_grid + n);
+  GreedyJob job{ctx->out0.as<uint32_t>(), ctx->out1.as<float>(), d_grid, gw, gh, k,
+                (uint32_t)cfg->max_usage_per_image, cfg->adjacency_penalty_weight, d_resets, nullptr};
+  MG_CHECK(upload(ctx, ctx->regions, &job, sizeof(job)));
+  const size_t row_bytes = ((size_t)gw * 4 + 15) & ~(size_t)15;
+  const bool smem_usage = row_bytes + (size_t)p * 4 <= 190 * 1024;
+  if (!smem_usage) MG_CHECK(ctx->sums.ensure(sizeof(uint32_t) * p));
+  MG_CHECK(launch_greedy(ctx->in0.as<float4>(), p, ctx->regions.as<GreedyJob>(), 1,
+                         smem_usage ? nullptr : ctx->sums.as<uint32_t>(),
+                         (int)(row_bytes + (smem_usage ? (size_t)p * 4 : 0)), ctx->stream));
+  MG_CUDA(cudaMemcpyAsync(grid_out, d_grid, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  int resets = 0;
+  MG_CUDA(cudaMemcpyAsync(&resets, d_resets, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MG_CHECK(finish(ctx));
+  if (n_resets) *n_resets = resets;
+  return MG_OK;
+}
+
+// ---- annealing --------------------------------------------------------------------------------
+void mg_sa_config_default(mg_sa_config* cfg) {
+  if (!cfg) return;
+  cfg->max_iterations = 1000;
+  cfg->initial_temperature = 100.0f;
+  cfg->temperature_decay = 0.99995f;
+  cfg->chains = 1;
+  cfg->seed = 0x5eed5eed5eedull;
+  cfg->stream = 0;
+  cfg->greedy_only = 0;
+}
+
+float mg_improvement_percentage(const mg_sa_result* r) {
+  if (!r) return 0.0f;
+  if (r->initial_cost > 0.0f) return ((r->initial_cost - r->final_cost) / r->initial_cost) * 100.0f;
+  return 0.0f;
+}
+
+static void to_result(const ChainResult& c, int64_t iters, int chain, mg_sa_result* r) {
+  r->initial_cost = c.initial_cost;
+  r->final_cost = c.final_cost;
+  r->best_cost = c.best_cost;
+  r->improved_count = c.improved;
+  r->accepted_count = c.accepted;
+  r->iterations = iters;
+  r->best_chain = chain;
+}
+
+int mg_optimize(mg_ctx* ctx, const float* palette_lab, int p, int32_t* grid, int gw, int gh, const mg_sa_config* cfg,
+                mg_sa_result* best, mg_sa_result* per_chain, int32_t* chain_grids) {
+  MG_CHECK(check_ctx(ctx));
+  if (!cfg || !best) return fail(MG_ERR_ARG, "null config or result");
+  if (cfg->chains < 1 || cfg->max_iterations < 0) return fail(MG_ERR_ARG, "need chains >= 1, iterations >= 0");
+  if (gh == 0 || gw == 0) {  // optimizer.rs:42-46: empty grid -> default result
+    std::memset(best, 0, sizeof(*best));
+    best->best_chain = 0;
+    return MG_OK;
+  }
+  MG_CHECK(check_grid(palette_lab, p, grid, gw, gh));
+  const int n = gw * gh, K = cfg->chains;
+  auto pal = to_f4(palette_lab, p);
+  MG_CHECK(upload(ctx, ctx->in0, pal.data(), sizeof(float4) * std::max(p, 1)));
+  MG_CHECK(upload(ctx, ctx->in1, grid, sizeof(int32_t) * n));
+  MG_CHECK(ctx->out0.ensure(sizeof(int32_t) * (size_t)n * K));
+  MG_CHECK(ctx->out1.ensure(sizeof(ChainResult) * K));
+  MG_CHECK(ctx->out2.ensure(sizeof(int32_t) * n + 64));
+  AnnealJob job{};
+  job.grid_in = ctx->in1.as<int32_t>();
+  job.chain_grids = ctx->out0.as<int32_t>();
+  job.results = ctx->out1.as<ChainResult>();
+  job.initial_cost = nullptr;
+  job.gw = gw;
+  job.gh = gh;
+  job.chains = K;
+  job.iters = cfg->max_iterations;
+  job.t0 = cfg->initial_temperature;
+  job.decay = cfg->temperature_decay;
+  job.key0 = (uint32_t)cfg->seed;
+  job.key1 = (uint32_t)(cfg->seed >> 32);
+  job.stream = cfg->stream;
+  job.greedy_only = cfg->greedy_only;
+  struct {
+    AnnealJob job;
+    int32_t* final_ptr;
+  } blob{job, ctx->out2.as<int32_t>()};
+  MG_CHECK(upload(ctx, ctx->regions, &blob, sizeof(blob)));
+  const AnnealJob* d_job = ctx->regions.as<AnnealJob>();
+  int32_t* const* d_final = reinterpret_cast<int32_t* const*>(ctx->regions.as<uint8_t>() + offsetof(decltype(blob), final_ptr));
+  int* d_best = reinterpret_cast<int*>(ctx->out2.as<int32_t>() + n);
+  MG_CHECK(launch_anneal(ctx->in0.as<float4>(), std::max(p, 1), d_job, nullptr, nullptr, K, n, ctx->stream));
+  MG_CHECK(launch_select_best(d_job, 1, d_final, d_best, ctx->stream));
+  std::vector<ChainResult> res(K);
+  int bc = 0;
+  MG_CUDA(cudaMemcpyAsync(res.data(), ctx->out1.p, sizeof(ChainResult) * K, cudaMemcpyDeviceToHost, ctx->stream));
+  MG_CUDA(cudaMemcpyAsync(&bc, d_best, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MG_CUDA(cudaMemcpyAsync(grid, ctx->out2.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  if (chain_grids)
+    MG_CUDA(cudaMemcpyAsync(chain_grids, ctx->out0.p, sizeof(int32_t) * (size_t)n * K, cudaMemcpyDeviceToHost,
+                            ctx->stream));
+  MG_CHECK(finish(ctx));
+  to_result(res[bc], cfg->max_iterations, bc, best);
+  if (per_chain)
+    for (int c = 0; c < K; ++c) to_result(res[c], cfg->max_iterations, c, per_chain + c);
+  return MG_OK;
+}
+
+// ---- colour adjustment -----------------------------------------------------------------------------
+mg_color_adjustment mg_color_adjustment_new(float brightness, float contrast, float hue_shift, float saturation) {
+  Adjust a = adjustment_new(brightness, contrast, hue_shift, saturation);
+  return mg_color_adjustment{a.brightness, a.contrast, a.hue_shift, a.saturation};
+}
+
+int mg_optimal_adjustment_batch(mg_ctx* ctx, const uint8_t* tile_rgb, const uint8_t* target_rgb, int n, float strength,
+                                mg_color_adjustment* out) {
+  MG_CHECK(check_ctx(ctx));
+  if (n < 0 || (n > 0 && (!tile_rgb || !target_rgb || !out))) return fail(MG_ERR_ARG, "invalid arguments");
+  if (n == 0) return MG_OK;
+  MG_CHECK(upload(ctx, ctx->in0, tile_rgb, 3ull * n));
+  MG_CHECK(upload(ctx, ctx->in1, target_rgb, 3ull * n));
+  MG_CHECK(ctx->out0.ensure(sizeof(float4) * n));
+  MG_CHECK(launch_optimal_adjustment(ctx->in0.as<uint8_t>(), ctx->in1.as<uint8_t>(), n, strength,
+                                     ctx->out0.as<float4>(), ctx->stream));
+  static_assert(sizeof(mg_color_adjustment) == sizeof(float4), "layout");
+  MG_CUDA(cudaMemcpyAsync(out, ctx->out0.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  return finish(ctx);
+}
+
+int mg_apply_adjustment(mg_ctx* ctx, const mg_color_adjustment* adj, const uint8_t* rgb, int w, int h, int64_t stride,
+                        uint8_t* out) {
+  MG_CHECK(check_ctx(ctx));
+  if (!adj || !out || !valid_image(rgb, w, h, stride)) return fail(MG_ERR_ARG, "invalid arguments");
+  const size_t row = 3ull * w;
+  MG_CHECK(ctx->in0.ensure(row * h));
+  MG_CUDA(cudaMemcpy2DAsync(ctx->in0.p, row, rgb, stride, row, h, cudaMemcpyHostToDevice, ctx->stream));
+  MG_CHECK(ctx->out0.ensure(row * h));
+  MG_CHECK(launch_adjust_image(make_float4(adj->brightness, adj->contrast, adj->hue_shift, adj->saturation),
+                               ctx->in0.as<uint8_t>(), w, h, (int64_t)row, ctx->out0.as<uint8_t>(), ctx->stream));
+  MG_CUDA(cudaMemcpyAsync(out, ctx->out0.p, row * h, cudaMemcpyDeviceToHost, ctx->stream));
+  return finish(ctx);
+}
+
+int mg_composite(mg_ctx* ctx, const int32_t* grid, int gw, int gh, const uint8_t* thumbs, int p, int tw, int th,
+                 const uint8_t* cell_avg_rgb, float strength, uint8_t* out) {
+  MG_CHECK(check_ctx(ctx));
+  if (!grid || !out || gw <= 0 || gh <= 0 || tw <= 0 || th <= 0 || p < 0 || (p > 0 && !thumbs))
+    return fail(MG_ERR_ARG, "invalid arguments");
+  const bool adjust = strength > 0.0f;
+  if (adjust && !cell_avg_rgb) return fail(MG_ERR_ARG, "cell_avg_rgb required when strength > 0");
+  const int n = gw * gh;
+  for (int i = 0; i < n; ++i)
+    if (grid[i] < -1 || grid[i] >= p) return fail(MG_ERR_ARG, "grid entry out of palette range");
+  const size_t tb = 3ull * tw * th;
+  MG_CHECK(upload(ctx, ctx->in0, thumbs, tb * std::max(p, 1) * (p > 0)));
+  MG_CHECK(upload(ctx, ctx->in1, grid, sizeof(int32_t) * n));
+  MG_CHECK(ctx->out0.ensure(tb * n));
+  if (adjust && p > 0) {
+    // thumbnail means (main.rs:557) and cell means -> per-cell adjustment
+    std::vector<Region> regs(p);
+    for (int i = 0; i < p; ++i) regs[i] = Region{(int64_t)(tb * i), tw, th, 3ll * tw};
+    MG_CHECK(upload(ctx, ctx->regions, regs.data(), sizeof(Region) * p));
+    MG_CHECK(ctx->sums.ensure(sizeof(RegionSums) * p));
+    MG_CHECK(ctx->out1.ensure(sizeof(uchar4) * p + sizeof(uchar4) * n + sizeof(float4) * n + 64));
+    uchar4* thumb_rgb = ctx->out1.as<uchar4>();
+    uchar4* cell_rgb = thumb_rgb + p;
+    float4* adjv = reinterpret_cast<float4*>(ctx->out1.as<uint8_t>() + (((sizeof(uchar4) * (p + n)) + 15) & ~15ull));
+    MG_CHECK(launch_region_stats(ctx->in0.as<uint8_t>(), nullptr, ctx->regions.as<Region>(), p, (int64_t)tw * th,
+                                 nullptr, thumb_rgb, ctx->sums.as<RegionSums>(), 0, ctx->stream));
+    std::vector<uchar4> crgb(n);
+    for (int i = 0; i < n; ++i) crgb[i] = make_uchar4(cell_avg_rgb[3 * i], cell_avg_rgb[3 * i + 1], cell_avg_rgb[3 * i + 2], 0);
+    MG_CUDA(cudaMemcpyAsync(cell_rgb, crgb.data(), sizeof(uchar4) * n, cudaMemcpyHostToDevice, ctx->stream));
+    MG_CHECK(launch_cell_adjust(ctx->in1.as<int32_t>(), n, thumb_rgb, cell_rgb, strength, adjv,
+                                ctx->stream));
+    MG_CHECK(launch_composite(ctx->in1.as<int32_t>(), gw, gh, ctx->in0.as<uint8_t>(), tw, th, adjv, 1,
+                              ctx->out0.as<uint8_t>(), ctx->stream));
+    MG_CUDA(cudaMemcpyAsync(out, ctx->out0.p, tb * n, cudaMemcpyDeviceToHost, ctx->stream));
+    return finish(ctx);
+  }
+  MG_CHECK(launch_composite(ctx->in1.as<int32_t>(), gw, gh, ctx->in0.as<uint8_t>(), tw, th, nullptr, 0,
+                            ctx->out0.as<uint8_t>(), ctx->stream));
+  MG_CUDA(cudaMemcpyAsync(out, ctx->out0.p, tb * n, cudaMemcpyDeviceToHost, ctx->stream));
+  return finish(ctx);
+}
+
+// ---- the whole job -------------------------------------------------------------------------------
+void mg_request_default(mg_request* r) {
+  if (!r) return;
+  std::memset(r, 0, sizeof(*r));
+  r->grid_w = 50;  // main.rs:37-43 defaults
+  r->grid_h = 28;
+  r->max_materials = 500;
+  r->aspect_tolerance = 0.1f;
+  r->max_usage_per_image = 3;
+  r->adjacency_penalty_weight = 0.3f;
+  r->color_adjustment_strength = 0.3f;
+  r->enable_optimization = 1;
+  r->optimization_iterations = 1000;
+  r->initial_temperature = 100.0f;
+  r->temperature_decay = 0.99995f;
+  r->chains = 1;
+  r->seed = 0x5eed5eed5eedull;
+  r->build_similarity = 1;
+}
+
+}  // extern "C"
+
+namespace {
+
+void plan_release(mg_plan* pl) {
+  for (DevBuf* b : {&pl->target, &pl->mats, &pl->regions, &pl->thumb_regions, &pl->thumbs, &pl->pal_lab,
+                    &pl->thumb_rgb, &pl->sim, &pl->cell_lab, &pl->cell_rgb, &pl->cand_idx, &pl->cand_dist,
+                    &pl->grid_greedy, &pl->resets, &pl->init_cost, &pl->greedy_job, &pl->chain_grids, &pl->chain_res,
+                    &pl->anneal_job, &pl->final_grid, &pl->finals_ptr, &pl->best_chain, &pl->adj, &pl->out, &pl->sums,
+                    &pl->err})
+    b->release();
+  if (pl->events)
+    for (auto& e : pl->ev) cudaEventDestroy(e);
+  pl->events = false;
+}
+
+// Validate the request, select the palette and upload the inputs.
+int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r) {
+  if (!r) return fail(MG_ERR_ARG, "null request");
+  if (!valid_image(r->target, r->target_w, r->target_h, r->target_stride ? r->target_stride : 3ll * r->target_w))
+    return fail(MG_ERR_ARG, "invalid target image");
+  if (r->grid_w <= 0 || r->grid_h <= 0) return fail(MG_ERR_ARG, "grid dimensions must be positive");
+  if (r->target_w / r->grid_w <= 0 || r->target_h / r->grid_h <= 0) return fail(MG_ERR_ARG, "grid larger than the target");
+  if (r->n_materials < 0 || (r->n_materials > 0 && (!r->materials || !r->material_w || !r->material_h)))
+    return fail(MG_ERR_ARG, "invalid material list");
+  if (r->max_materials < 0 || r->max_usage_per_image < 0 || r->tile_w < 0 || r->tile_h < 0)
+    return fail(MG_ERR_ARG, "negative size parameter");
+  if (r->enable_optimization && (r->chains < 1 || r->optimization_iterations < 0))
+    return fail(MG_ERR_ARG, "need chains >= 1 and iterations >= 0");
+  pl->ctx = ctx;
+  pl->W = r->target_w;
+  pl->H = r->target_h;
+  pl->gw = r->grid_w;
+  pl->gh = r->grid_h;
+  pl->cw = pl->W / pl->gw;
+  pl->ch = pl->H / pl->gh;
+  pl->tw = r->tile_w ? r->tile_w : pl->cw;
+  pl->th = r->tile_h ? r->tile_h : pl->ch;
+  pl->N = pl->gw * pl->gh;
+  pl->weight = r->adjacency_penalty_weight;
+  pl->strength = rclamp(r->color_adjustment_strength, 0.0f, 1.0f);
+  pl->max_usage = r->max_usage_per_image;
+  pl->enable_opt = r->enable_optimization;
+  pl->iters = r->optimization_iterations;
+  pl->t0 = r->initial_temperature;
+  pl->decay = r->temperature_decay;
+  pl->K = r->enable_optimization ? r->chains : 0;
+  pl->seed = r->seed;
+  pl->stream_id = r->stream;
+  pl->build_sim = r->build_similarity;
+  // palette selection (main.rs:166-261)
+  pl->selected.assign(std::max(r->n_materials, 1), 0);
+  const float target_aspect = (float)r->target_w / (float)r->target_h;
+  int P = mg_select_palette(r->material_w, r->material_h, r->n_materials, target_aspect, r->aspect_tolerance,
+                            r->max_materials, pl->selected.data());
+  if (P < 0) return fail(MG_ERR_ARG, "invalid material sizes");
+  pl->selected.resize(P);
+  pl->P = P;
+  pl->k = std::min(P, 100);
+  if (P >= 65535) return fail(MG_ERR_ARG, "palette too large (max 65534 materials)");
+  pl->run_sa = pl->enable_opt && pl->weight > 0.0f && P > 0;  // main.rs:608
+  if (pl->run_sa && (size_t)pl->N * 2 > 200 * 1024) return fail(MG_ERR_ARG, "grid too large for the annealer");
+  cudaStream_t s = ctx->stream;
+  // target, packed rows
+  const size_t trow = 3ull * pl->W;
+  MG_CHECK(pl->target.ensure(trow * pl->H));
+  MG_CUDA(cudaMemcpy2DAsync(pl->target.p, trow, r->target, r->target_stride ? r->target_stride : trow, trow, pl->H,
+                            cudaMemcpyHostToDevice, s));
+  // selected materials, packed with 16-byte aligned starts
+  pl->h_regions.resize(std::max(P, 1));
+  int64_t off = 0;
+  for (int i = 0; i < P; ++i) {
+    const int m = pl->selected[i];
+    pl->h_regions[i] = Region{off, r->material_w[m], r->material_h[m], 3ll * r->material_w[m]};
+    off += 3ll * r->material_w[m] * r->material_h[m];
+    off = (off + 15) & ~15ll;
+  }
+  MG_CHECK(pl->mats.ensure((size_t)off));
+  for (int i = 0; i < P; ++i) {
+    const int m = pl->selected[i];
+    const int64_t st = r->material_stride ? r->material_stride[m] : 3ll * r->material_w[m];
+    if (!valid_image(r->materials[m], r->material_w[m], r->material_h[m], st))
+      return fail(MG_ERR_ARG, "invalid material " + std::to_string(m));
+    MG_CUDA(cudaMemcpy2DAsync(pl->mats.as<uint8_t>() + pl->h_regions[i].offset, 3ull * r->material_w[m],
+                              r->materials[m], st, 3ull * r->material_w[m], r->material_h[m], cudaMemcpyHostToDevice, s));
+  }
+  MG_CHECK(pl->regions.ensure(sizeof(Region) * std::max(P, 1)));
+  MG_CUDA(cudaMemcpyAsync(pl->regions.p, pl->h_regions.data(), sizeof(Region) * std::max(P, 1), cudaMemcpyHostToDevice, s));
+  // thumbnails (input, or resized on the device in mg_plan_run)
+  const size_t tb = 3ull * pl->tw * pl->th;
+  MG_CHECK(pl->thumbs.ensure(tb * std::max(P, 1)));
+  pl->device_thumbs = r->thumbnails == nullptr;
+  if (!pl->device_thumbs) {
+    int i = 0;
+    while (i < P) {  // merge runs of consecutive selected materials into one copy
+      int j = i + 1;
+      while (j < P && pl->selected[j] == pl->selected[j - 1] + 1) ++j;
+      MG_CUDA(cudaMemcpyAsync(pl->thumbs.as<uint8_t>() + tb * i, r->thumbnails + tb * pl->selected[i], tb * (j - i),
+                              cudaMemcpyHostToDevice, s));
+      i = j;
+    }
+  }
+  std::vector<Region> tregs(std::max(P, 1));
+  for (int i = 0; i < P; ++i) tregs[i] = Region{(int64_t)(tb * i), pl->tw, pl->th, 3ll * pl->tw};
+  MG_CHECK(pl->thumb_regions.ensure(sizeof(Region) * std::max(P, 1)));
+  MG_CUDA(cudaMemcpyAsync(pl->thumb_regions.p, tregs.data(), sizeof(Region) * std::max(P, 1), cudaMemcpyHostToDevice, s));
+  // working buffers
+  const int N = pl->N, K = std::max(pl->K, 1), k = std::max(pl->k, 1);
+  MG_CHECK(pl->pal_lab.ensure(sizeof(float4) * std::max(P, 1)));
+  MG_CHECK(pl->thumb_rgb.ensure(sizeof(uchar4) * std::max(P, 1)));
+  if (pl->build_sim) MG_CHECK(pl->sim.ensure(sizeof(float) * (size_t)std::max(P, 1) * std::max(P, 1)));
+  MG_CHECK(pl->cell_lab.ensure(sizeof(float4) * N));
+  MG_CHECK(pl->cell_rgb.ensure(sizeof(uchar4) * N));
+  MG_CHECK(pl->cand_idx.ensure(sizeof(uint32_t) * (size_t)N * k));
+  MG_CHECK(pl->cand_dist.ensure(sizeof(float) * (size_t)N * k));
+  MG_CHECK(pl->grid_greedy.ensure(sizeof(int32_t) * N));
+  MG_CHECK(pl->resets.ensure(16));
+  MG_CHECK(pl->init_cost.ensure(16));
+  MG_CHECK(pl->chain_grids.ensure(sizeof(int32_t) * (size_t)N * K));
+  MG_CHECK(pl->chain_res.ensure(sizeof(ChainResult) * K));
+  MG_CHECK(pl->final_grid.ensure(sizeof(int32_t) * N));
+  MG_CHECK(pl->best_chain.ensure(16));
+  MG_CHECK(pl->adj.ensure(sizeof(float4) * N));
+  MG_CHECK(pl->out.ensure(tb * N));
+  MG_CHECK(pl->sums.ensure(sizeof(RegionSums) * std::max(N, std::max(P, 1))));
+  MG_CHECK(pl->err.ensure(16));
+  MG_CUDA(cudaMemsetAsync(pl->err.p, 0, 16, s));
+  MG_CUDA(cudaMemsetAsync(pl->resets.p, 0, 16, s));
+  GreedyJob gj{pl->cand_idx.as<uint32_t>(), pl->cand_dist.as<float>(), pl->grid_greedy.as<int32_t>(), pl->gw, pl->gh,
+               pl->k, (uint32_t)pl->max_usage, pl->weight, pl->resets.as<int>(), pl->init_cost.as<float>()};
+  MG_CHECK(pl->greedy_job.ensure(sizeof(GreedyJob)));
+  MG_CUDA(cudaMemcpyAsync(pl->greedy_job.p, &gj, sizeof(gj), cudaMemcpyHostToDevice, s));
+  AnnealJob aj{};
+  aj.grid_in = pl->grid_greedy.as<int32_t>();
+  aj.chain_grids = pl->chain_grids.as<int32_t>();
+  aj.results = pl->chain_res.as<ChainResult>();
+  aj.initial_cost = pl->init_cost.as<float>();
+  aj.gw = pl->gw;
+  aj.gh = pl->gh;
+  aj.chains = K;
+  aj.iters = pl->iters;
+  aj.t0 = pl->t0;
+  aj.decay = pl->decay;
+  aj.key0 = (uint32_t)pl->seed;
+  aj.key1 = (uint32_t)(pl->seed >> 32);
+  aj.stream = pl->stream_id;
+  aj.greedy_only = 0;
+  MG_CHECK(pl->anneal_job.ensure(sizeof(AnnealJob)));
+  MG_CUDA(cudaMemcpyAsync(pl->anneal_job.p, &aj, sizeof(aj), cudaMemcpyHostToDevice, s));
+  int32_t* fp = pl->final_grid.as<int32_t>();
+  MG_CHECK(pl->finals_ptr.ensure(sizeof(int32_t*)));
+  MG_CUDA(cudaMemcpyAsync(pl->finals_ptr.p, &fp, sizeof(fp), cudaMemcpyHostToDevice, s));
+  if (!pl->events) {
+    for (auto& e : pl->ev) MG_CUDA(cudaEventCreate(&e));
+    pl->events = true;
+  }
+  MG_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+  pl->ran = false;
+  return MG_OK;
+}
+
+int plan_run(mg_plan* pl) {
+  mg_ctx* ctx = pl->ctx;
+  cudaStream_t s = ctx->stream;
+  const unsigned long long l0 = g_launches;
+  const int P = pl->P, N = pl->N;
+  MG_CUDA(cudaEventRecord(pl->ev[0], s));
+  // [0] palette ingestion: thumbnails (when not given), material Lab, thumbnail means
+  if (P > 0) {
+    if (pl->device_thumbs)
+      MG_CHECK(launch_thumbnails(pl->mats.as<uint8_t>(), pl->regions.as<Region>(), P, pl->tw, pl->th,
+                                 pl->thumbs.as<uint8_t>(), s));
+    int64_t maxpx = 0;
+    for (int i = 0; i < P; ++i) maxpx = std::max<int64_t>(maxpx, (int64_t)pl->h_regions[i].w * pl->h_regions[i].h);
+    MG_CHECK(launch_region_stats(pl->mats.as<uint8_t>(), nullptr, pl->regions.as<Region>(), P, maxpx,
+                                 pl->pal_lab.as<float4>(), nullptr, pl->sums.as<RegionSums>(), 1, s));
+    if (pl->strength > 0.0f)
+      MG_CHECK(launch_region_stats(pl->thumbs.as<uint8_t>(), nullptr, pl->thumb_regions.as<Region>(), P,
+                                   (int64_t)pl->tw * pl->th, nullptr, pl->thumb_rgb.as<uchar4>(),
+                                   pl->sums.as<RegionSums>(), 0, s));
+  }
+  MG_CUDA(cudaEventRecord(pl->ev[1], s));
+  // [1] similarity database (main.rs:120-143)
+  if (pl->build_sim && P > 0)
+    MG_CHECK(launch_similarity(pl->pal_lab.as<float4>(), P, 0, pl->sim.as<float>(), s));
+  MG_CUDA(cudaEventRecord(pl->ev[2], s));
+  // [2] cell Lab + cell mean RGB
+  CellGeom g{pl->gw, pl->gh, pl->cw, pl->ch, 3ll * pl->W};
+  MG_CHECK(launch_region_stats(pl->target.as<uint8_t>(), &g, nullptr, N, (int64_t)pl->cw * pl->ch,
+                               pl->cell_lab.as<float4>(), pl->cell_rgb.as<uchar4>(), pl->sums.as<RegionSums>(), 1, s));
+  MG_CUDA(cudaEventRecord(pl->ev[3], s));
+  // [3] k nearest per cell
+  if (P > 0)
+    MG_CHECK(launch_nearest(pl->pal_lab.as<float4>(), P, pl->cell_lab.as<float4>(), N, pl->k, pl->cand_idx.as<uint32_t>(),
+                            pl->cand_dist.as<float>(), pl->err.as<uint32_t>(), s));
+  MG_CUDA(cudaEventRecord(pl->ev[4], s));
+  // [4] greedy placement
+  if (P > 0) {
+    const size_t row_bytes = ((size_t)pl->gw * 4 + 15) & ~(size_t)15;
+    const bool smem_usage = row_bytes + (size_t)P * 4 <= 190 * 1024;
+    if (!smem_usage) MG_CHECK(pl->sums.ensure(sizeof(uint32_t) * P));
+    MG_CHECK(launch_greedy(pl->pal_lab.as<float4>(), P, pl->greedy_job.as<GreedyJob>(), 1,
+                           smem_usage ? nullptr : pl->sums.as<uint32_t>(),
+                           (int)(row_bytes + (smem_usage ? (size_t)P * 4 : 0)), s));
+  } else {
+    MG_CUDA(cudaMemsetAsync(pl->grid_greedy.p, 0xFF, sizeof(int32_t) * N, s));
+  }
+  MG_CUDA(cudaEventRecord(pl->ev[5], s));
+  // [5] annealing chains + best-chain selection
+  const int32_t* final_grid = pl->grid_greedy.as<int32_t>();
+  if (pl->run_sa) {
+    MG_CHECK(launch_anneal(pl->pal_lab.as<float4>(), P, pl->anneal_job.as<AnnealJob>(), nullptr, nullptr, pl->K, N, s));
+    MG_CHECK(launch_select_best(pl->anneal_job.as<AnnealJob>(), 1, pl->finals_ptr.as<int32_t*>(),
+                                pl->best_chain.as<int>(), s));
+    final_grid = pl->final_grid.as<int32_t>();
+  }
+  MG_CUDA(cudaEventRecord(pl->ev[6], s));
+  // [6] colour adjustment + composite
+  const bool adjust = pl->strength > 0.0f && P > 0;
+  if (adjust)
+    MG_CHECK(launch_cell_adjust(final_grid, N, pl->thumb_rgb.as<uchar4>(), pl->cell_rgb.as<uchar4>(), pl->strength,
+                                pl->adj.as<float4>(), s));
+  MG_CHECK(launch_composite(final_grid, pl->gw, pl->gh, pl->thumbs.as<uint8_t>(), pl->tw, pl->th, pl->adj.as<float4>(),
+                            adjust ? 1 : 0, pl->out.as<uint8_t>(), s));
+  MG_CUDA(cudaEventRecord(pl->ev[7], s));
+  pl->launches = (int)(g_launches - l0);
+  pl->ran = true;
+  return MG_OK;
+}
+
+int plan_read(mg_plan* pl, mg_result* res) {
+  if (!pl->ran) return fail(MG_ERR_STATE, "plan has not run");
+  mg_ctx* ctx = pl->ctx;
+  cudaStream_t s = ctx->stream;
+  const int N = pl->N;
+  const int32_t* final_grid = pl->run_sa ? pl->final_grid.as<int32_t>() : pl->grid_greedy.as<int32_t>();
+  std::vector<int32_t> grid(N);
+  ChainResult cr{};
+  int bc = -1, resets = 0;
+  if (res->image)
+    MG_CUDA(cudaMemcpyAsync(res->image, pl->out.p, 3ull * pl->tw * pl->th * N, cudaMemcpyDeviceToHost, s));
+  MG_CUDA(cudaMemcpyAsync(grid.data(), final_grid, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, s));
+  MG_CUDA(cudaMemcpyAsync(&resets, pl->resets.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (pl->run_sa) MG_CUDA(cudaMemcpyAsync(&bc, pl->best_chain.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MG_CHECK(finish(ctx));
+  uint32_t kerr = 0;
+  MG_CUDA(cudaMemcpy(&kerr, pl->err.p, 4, cudaMemcpyDeviceToHost));
+  if (kerr) return fail(MG_ERR_TIMEOUT, "a bounded wait inside a kernel ran out");
+  if (pl->run_sa) MG_CUDA(cudaMemcpy(&cr, pl->chain_res.as<ChainResult>() + bc, sizeof(cr), cudaMemcpyDeviceToHost));
+  if (res->grid)
+    for (int i = 0; i < N; ++i) res->grid[i] = grid[i] < 0 ? -1 : pl->selected[grid[i]];
+  res->out_w = pl->gw * pl->tw;
+  res->out_h = pl->gh * pl->th;
+  res->palette_size = pl->P;
+  res->n_resets = resets;
+  res->best_chain = bc;
+  res->initial_cost = cr.initial_cost;
+  res->final_cost = cr.final_cost;
+  res->best_cost = cr.best_cost;
+  res->accepted_count = cr.accepted;
+  res->improved_count = cr.improved;
+  return MG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mg_plan_create(mg_ctx* ctx, const mg_request* req, mg_plan** out) {
+  MG_CHECK(check_ctx(ctx));
+  if (!out) return fail(MG_ERR_ARG, "null out");
+  *out = nullptr;
+  mg_plan* pl = new mg_plan();
+  int s = plan_setup(pl, ctx, req);
+  if (s != MG_OK) {
+    std::string msg = g_error;
+    plan_release(pl);
+    delete pl;
+    set_error(msg);
+    return s;
+  }
+  *out = pl;
+  return MG_OK;
+}
+
+int mg_plan_run(mg_plan* pl) {
+  if (!pl) return fail(MG_ERR_ARG, "null plan");
+  MG_CHECK(check_ctx(pl->ctx));
+  return plan_run(pl);
+}
+
+int mg_plan_read(mg_plan* pl, mg_result* res) {
+  if (!pl || !res) return fail(MG_ERR_ARG, "null plan or result");
+  MG_CHECK(check_ctx(pl->ctx));
+  return plan_read(pl, res);
+}
+
+int mg_plan_destroy(mg_plan* pl) {
+  if (!pl) return MG_OK;
+  if (pl->ctx) {
+    cudaSetDevice(pl->ctx->device);
+    cudaStreamSynchronize(pl->ctx->stream);
+  }
+  plan_release(pl);
+  delete pl;
+  return MG_OK;
+}
+
+int mg_plan_stage_ms(mg_plan* pl, float* ms, int cap) {
+  if (!pl || !ms) return fail(MG_ERR_ARG, "null argument");
+  if (!pl->ran) return fail(MG_ERR_STATE, "plan has not run");
+  MG_CHECK(check_ctx(pl->ctx));
+  MG_CUDA(cudaEventSynchronize(pl->ev[7]));
+  int n = 0;
+  for (int i = 0; i < 7 && n < cap; ++i, ++n) MG_CUDA(cudaEventElapsedTime(&ms[n], pl->ev[i], pl->ev[i + 1]));
+  if (n < cap) {
+    MG_CUDA(cudaEventElapsedTime(&ms[n], pl->ev[0], pl->ev[7]));
+    ++n;
+  }
+  return n;
+}
+
+int mg_plan_launches(mg_plan* pl) { return pl ? pl->launches : 0; }
+
+int mg_generate(mg_ctx* ctx, const mg_request* req, mg_result* res) {
+  MG_CHECK(check_ctx(ctx));
+  if (!res) return fail(MG_ERR_ARG, "null result");
+  if (!ctx->gen_plan) ctx->gen_plan = new mg_plan();
+  MG_CHECK(plan_setup(ctx->gen_plan, ctx, req));
+  MG_CHECK(plan_run(ctx->gen_plan));
+  return plan_read(ctx->gen_plan, res);
+}
+
+}  // extern "C"

@@ -1,0 +1,360 @@
+// k_anneal.cu -- (e) simulated annealing, K independent chains per mosaic,
+// plus the batched adjacency evaluators of the C ABI.
+//
+// Reference: optimizer.rs:41-129 MosaicOptimizer::optimize (and
+// optimizer.rs:132-198 optimize_greedy), adjacency.rs:91-130
+// calculate_total_cost, adjacency.rs:133-214 calculate_swap_delta,
+// adjacency.rs:63-88 calculate_penalty.
+//
+// One CTA (one warp) per chain.  The chain's grid lives in shared memory as
+// 16-bit palette indices, and the palette Lab too when it fits, so a proposal
+// touches no global memory.  Random numbers are counter-based: at iteration t
+// of chain c, Philox4x32-10 with key (seed lo, seed hi) and counter
+// (t, c, stream, 2*(t>>32)) gives x1, y1, x2, y2 (multiply-high range
+// reduction) and counter (t, c, stream, 2*(t>>32)+1) gives the acceptance
+// uniform, so a CPU replay of the same stream makes the same decisions.
+// Lanes compute Philox for 32 iterations at once.  Per proposal, lanes 0-3
+// evaluate the neighbours of pos1 (up, down, left, right), lanes 4-7 those of
+// pos2, lane 8 the mutual pair; the old and new sums are then accumulated in
+// exactly the reference's order (absent terms are +0 and leave a sum as is).
+// The acceptance test uses this library's own exp, identical on host and
+// device.  An iteration that draws pos1 == pos2 or an empty cell is skipped
+// without cooling, as in the reference.
+#include "mg_internal.h"
+
+namespace mg {
+namespace {
+
+constexpr uint16_t kNone16 = 0xFFFFu;
+
+__device__ __forceinline__ float wgt(const float4& a, const float4& b) {
+  return adj_weight_from_sim(lab_distance(a.x, a.y, a.z, b.x, b.y, b.z));
+}
+
+template <bool kLabSmem>
+__global__ void __launch_bounds__(32) anneal_kernel(const float4* __restrict__ pal, int p,
+                                                    const AnnealJob* __restrict__ jobs,
+                                                    const int* __restrict__ chain_job,
+                                                    const int* __restrict__ chain_id) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int lane = threadIdx.x;
+  const int jid = chain_job ? chain_job[blockIdx.x] : 0;
+  const int chain = chain_id ? chain_id[blockIdx.x] : (int)blockIdx.x;
+  const AnnealJob J = jobs[jid];
+  const int gw = J.gw, gh = J.gh, n = gw * gh;
+  float4* s_lab = reinterpret_cast<float4*>(smem);
+  uint16_t* s_grid = reinterpret_cast<uint16_t*>(smem + (kLabSmem ? (size_t)p * sizeof(float4) : 0));
+  if (kLabSmem)
+    for (int i = lane; i < p; i += 32) s_lab[i] = pal[i];
+  for (int i = lane; i < n; i += 32) {
+    const int g = J.grid_in[i];
+    s_grid[i] = g < 0 ? kNone16 : (uint16_t)g;
+  }
+  __syncwarp();
+  auto lab = [&](int i) -> float4 { return kLabSmem ? s_lab[i] : __ldg(pal + i); };
+
+  // Initial cost: calculate_total_cost of the start grid (sequential FP32 sum).
+  float current;
+  if (J.initial_cost) {
+    current = *J.initial_cost;
+  } else {
+    current = 0.0f;
+    for (int c0 = 0; c0 < n; c0 += 32) {
+      const int c = c0 + lane;
+      float tr = 0.0f, td = 0.0f;
+      if (c < n) {
+        const int x = c % gw, y = c / gw;
+        const uint16_t cur = s_grid[c];
+        if (cur != kNone16) {
+          const float4 lc = lab(cur);
+          if (x < gw - 1 && s_grid[c + 1] != kNone16) tr = wgt(lc, lab(s_grid[c + 1]));
+          if (y < gh - 1 && s_grid[c + gw] != kNone16) td = wgt(lc, lab(s_grid[c + gw]));
+        }
+      }
+      const int cnt = min(32, n - c0);
+      for (int s = 0; s < cnt; ++s) {
+        current = __fadd_rn(current, __shfl_sync(0xffffffffu, tr, s));
+        current = __fadd_rn(current, __shfl_sync(0xffffffffu, td, s));
+      }
+    }
+  }
+  const float initial = current;
+  float best = current;
+  long long accepted = 0, improved = 0, cooled = 0;
+  float temp = J.t0;
+  const float decay = J.decay;
+  const bool greedy_only = J.greedy_only != 0;
+  const uint32_t k0 = J.key0, k1 = J.key1, strm = J.stream;
+
+  uint32_t rx1 = 0, ry1 = 0, rx2 = 0, ry2 = 0;
+  float ru = 0.0f;
+  for (long long it = 0; it < J.iters; ++it) {
+    const int src = (int)(it & 31);
+    if (src == 0) {
+      const long long my = it + lane;
+      const uint32_t hi = (uint32_t)((unsigned long long)my >> 32);
+      const u32x4 a = philox((uint32_t)my, (uint32_t)chain, strm, 2u * hi, k0, k1);
+      rx1 = range_u32(a.x, (uint32_t)gw);
+      ry1 = range_u32(a.y, (uint32_t)gh);
+      rx2 = range_u32(a.z, (uint32_t)gw);
+      ry2 = range_u32(a.w, (uint32_t)gh);
+      const u32x4 b = philox((uint32_t)my, (uint32_t)chain, strm, 2u * hi + 1u, k0, k1);
+      ru = unit_f32(b.x);
+    }
+    const int x1 = (int)__shfl_sync(0xffffffffu, rx1, src), y1 = (int)__shfl_sync(0xffffffffu, ry1, src);
+    const int x2 = (int)__shfl_sync(0xffffffffu, rx2, src), y2 = (int)__shfl_sync(0xffffffffu, ry2, src);
+    const float u = __shfl_sync(0xffffffffu, ru, src);
+    const int p1 = y1 * gw + x1, p2 = y2 * gw + x2;
+    if (p1 == p2) continue;
+    const uint16_t g1 = s_grid[p1], g2 = s_grid[p2];
+    if (g1 == kNone16 || g2 == kNone16) continue;
+    float delta = 0.0f;
+    if (g1 != g2) {
+      float o = 0.0f, nw = 0.0f;
+      if (lane < 8) {
+        const bool first = lane < 4;
+        const int bx = first ? x1 : x2, by = first ? y1 : y2;
+        const int other = first ? p2 : p1;
+        const int dir = lane & 3;
+        int nx = bx, ny = by;
+        bool inb;
+        if (dir == 0) { ny = by - 1; inb = by > 0; }
+        else if (dir == 1) { ny = by + 1; inb = by < gh - 1; }
+        else if (dir == 2) { nx = bx - 1; inb = bx > 0; }
+        else { nx = bx + 1; inb = bx < gw - 1; }
+        if (inb) {
+          const int nb = ny * gw + nx;
+          if (nb != other) {
+            const uint16_t a = s_grid[nb];
+            if (a != kNone16) {
+              const float4 la = lab(a);
+              const float w1 = wgt(lab(g1), la), w2 = wgt(lab(g2), la);
+              o = first ? w1 : w2;
+              nw = first ? w2 : w1;
+            }
+          }
+        }
+      } else if (lane == 8) {
+        const int dx = x1 - x2, dy = y1 - y2;
+        if ((dx == 0 && (dy == 1 || dy == -1)) || (dy == 0 && (dx == 1 || dx == -1))) {
+          const float c = wgt(lab(g1), lab(g2));
+          o = c;
+          nw = c;
+        }
+      }
+      float old_cost = 0.0f, new_cost = 0.0f;
+#pragma unroll
+      for (int s = 0; s < 9; ++s) {
+        old_cost = __fadd_rn(old_cost, __shfl_sync(0xffffffffu, o, s));
+        new_cost = __fadd_rn(new_cost, __shfl_sync(0xffffffffu, nw, s));
+      }
+      delta = __fsub_rn(new_cost, old_cost);
+    }
+    bool accept;
+    if (greedy_only) accept = delta < 0.0f;
+    else accept = delta < 0.0f || u < exp_spec(__fdiv_rn(-delta, temp));
+    if (accept) {
+      if (lane == 0) {
+        s_grid[p1] = g2;
+        s_grid[p2] = g1;
+      }
+      current = __fadd_rn(current, delta);
+      ++accepted;
+      if (current < best) {
+        best = current;
+        ++improved;
+      }
+    }
+    __syncwarp();
+    if (!greedy_only) temp = __fmul_rn(temp, decay);
+    ++cooled;
+  }
+  int32_t* out = J.chain_grids + (size_t)chain * n;
+  for (int i = lane; i < n; i += 32) {
+    const uint16_t g = s_grid[i];
+    out[i] = g == kNone16 ? -1 : (int32_t)g;
+  }
+  if (lane == 0) {
+    ChainResult r;
+    r.initial_cost = initial;
+    r.final_cost = current;
+    r.best_cost = greedy_only ? current : best;
+    r.pad = 0.0f;
+    r.accepted = accepted;
+    r.improved = greedy_only ? accepted : improved;
+    r.cooled = cooled;
+    r.pad2 = 0;
+    J.results[chain] = r;
+  }
+}
+
+// Lowest final cost wins (ties: lowest chain); copy its grid.
+__global__ void select_best_kernel(const AnnealJob* __restrict__ jobs, int32_t* const* __restrict__ finals,
+                                   int* __restrict__ best_chain) {
+  __shared__ int s_best;
+  const AnnealJob J = jobs[blockIdx.x];
+  if (threadIdx.x == 0) {
+    int b = 0;
+    for (int c = 1; c < J.chains; ++c)
+      if (J.results[c].final_cost < J.results[b].final_cost) b = c;
+    s_best = b;
+    if (best_chain) best_chain[blockIdx.x] = b;
+  }
+  __syncthreads();
+  const int n = J.gw * J.gh;
+  const int32_t* src = J.chain_grids + (size_t)s_best * n;
+  int32_t* dst = finals[blockIdx.x];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+// ---- batched evaluators (one thread per item, the reference's loops verbatim) ----
+__device__ __forceinline__ float wgt_idx(const float4* pal, int a, int b) { return wgt(__ldg(pal + a), __ldg(pal + b)); }
+
+__device__ int adjacent_positions(int x, int y, int gw, int gh, int* nx, int* ny) {
+  int n = 0;
+  if (y > 0) { nx[n] = x; ny[n] = y - 1; ++n; }
+  if (y < gh - 1) { nx[n] = x; ny[n] = y + 1; ++n; }
+  if (x > 0) { nx[n] = x - 1; ny[n] = y; ++n; }
+  if (x < gw - 1) { nx[n] = x + 1; ny[n] = y; ++n; }
+  return n;
+}
+
+__global__ void swap_delta_kernel(const float4* __restrict__ pal, const int32_t* __restrict__ grid, int gw, int gh,
+                                  const int4* __restrict__ pairs, int n, float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int4 q = pairs[i];
+  const int x1 = q.x, y1 = q.y, x2 = q.z, y2 = q.w;
+  const int a1 = grid[y1 * gw + x1], a2 = grid[y2 * gw + x2];
+  if (a1 < 0 || a2 < 0 || a1 == a2) { out[i] = 0.0f; return; }
+  float old_cost = 0.0f, new_cost = 0.0f;
+  int nx[4], ny[4];
+  bool adj = false;
+  int m = adjacent_positions(x1, y1, gw, gh, nx, ny);
+  for (int t = 0; t < m; ++t) {
+    if (nx[t] == x2 && ny[t] == y2) { adj = true; continue; }
+    const int a = grid[ny[t] * gw + nx[t]];
+    if (a >= 0) {
+      old_cost = __fadd_rn(old_cost, wgt_idx(pal, a1, a));
+      new_cost = __fadd_rn(new_cost, wgt_idx(pal, a2, a));
+    }
+  }
+  m = adjacent_positions(x2, y2, gw, gh, nx, ny);
+  for (int t = 0; t < m; ++t) {
+    if (nx[t] == x1 && ny[t] == y1) continue;
+    const int a = grid[ny[t] * gw + nx[t]];
+    if (a >= 0) {
+      old_cost = __fadd_rn(old_cost, wgt_idx(pal, a2, a));
+      new_cost = __fadd_rn(new_cost, wgt_idx(pal, a1, a));
+    }
+  }
+  if (adj) {
+    const float c = wgt_idx(pal, a1, a2);
+    old_cost = __fadd_rn(old_cost, c);
+    new_cost = __fadd_rn(new_cost, c);
+  }
+  out[i] = __fsub_rn(new_cost, old_cost);
+}
+
+__global__ void penalty_kernel(const float4* __restrict__ pal, const int32_t* __restrict__ grid, int gw, int gh,
+                               float weight, const int4* __restrict__ cxy, int n, float* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int4 q = cxy[i];
+  int nx[4], ny[4];
+  const int m = adjacent_positions(q.y, q.z, gw, gh, nx, ny);
+  float pen = 0.0f;
+  for (int t = 0; t < m; ++t) {
+    const int a = grid[ny[t] * gw + nx[t]];
+    if (a >= 0) pen = __fadd_rn(pen, wgt_idx(pal, q.x, a));
+  }
+  out[i] = __fmul_rn(pen, weight);
+}
+
+__global__ void total_cost_kernel(const float4* __restrict__ pal, const int32_t* __restrict__ grid, int gw, int gh,
+                                  float* __restrict__ out) {
+  const int lane = threadIdx.x;
+  float total = 0.0f;
+  const int n = gw * gh;
+  for (int c0 = 0; c0 < n; c0 += 32) {
+    const int c = c0 + lane;
+    float tr = 0.0f, td = 0.0f;
+    if (c < n) {
+      const int x = c % gw, y = c / gw;
+      const int cur = grid[c];
+      if (cur >= 0) {
+        if (x < gw - 1 && grid[c + 1] >= 0) tr = wgt_idx(pal, cur, grid[c + 1]);
+        if (y < gh - 1 && grid[c + gw] >= 0) td = wgt_idx(pal, cur, grid[c + gw]);
+      }
+    }
+    const int cnt = min(32, n - c0);
+    for (int s = 0; s < cnt; ++s) {
+      total = __fadd_rn(total, __shfl_sync(0xffffffffu, tr, s));
+      total = __fadd_rn(total, __shfl_sync(0xffffffffu, td, s));
+    }
+  }
+  if (lane == 0) *out = total;
+}
+
+}  // namespace
+
+int launch_anneal(const float4* pal, int p, const AnnealJob* jobs_dev, const int* chain_job_dev,
+                  const int* chain_id_dev, int total_chains, int max_cells, cudaStream_t stream) {
+  if (total_chains <= 0) return MG_OK;
+  if (p >= 65535) return fail(MG_ERR_ARG, "annealing supports palettes below 65535 materials");
+  const size_t grid_bytes = ((size_t)max_cells * 2 + 15) & ~(size_t)15;
+  const size_t lab_bytes = (size_t)p * sizeof(float4);
+  const size_t kMaxSmem = 200 * 1024;
+  if (grid_bytes > kMaxSmem) return fail(MG_ERR_ARG, "grid too large for the annealer (max 102400 cells)");
+  static int configured_device = -1;
+  int dev = 0;
+  MG_CUDA(cudaGetDevice(&dev));
+  if (configured_device != dev) {
+    MG_CUDA(cudaFuncSetAttribute(anneal_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    MG_CUDA(cudaFuncSetAttribute(anneal_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    configured_device = dev;
+  }
+  if (grid_bytes + lab_bytes <= kMaxSmem)
+    anneal_kernel<true><<<total_chains, 32, grid_bytes + lab_bytes, stream>>>(pal, p, jobs_dev, chain_job_dev, chain_id_dev);
+  else
+    anneal_kernel<false><<<total_chains, 32, grid_bytes, stream>>>(pal, p, jobs_dev, chain_job_dev, chain_id_dev);
+  g_launches += 1;
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+int launch_select_best(const AnnealJob* jobs_dev, int n_jobs, int32_t* const* final_grids_dev, int* best_chain_dev,
+                       cudaStream_t stream) {
+  if (n_jobs <= 0) return MG_OK;
+  select_best_kernel<<<n_jobs, 256, 0, stream>>>(jobs_dev, final_grids_dev, best_chain_dev);
+  g_launches += 1;
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+int launch_total_cost(const float4* pal, const int32_t* grid, int gw, int gh, float* out, cudaStream_t stream) {
+  total_cost_kernel<<<1, 32, 0, stream>>>(pal, grid, gw, gh, out);
+  g_launches += 1;
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+int launch_swap_delta(const float4* pal, const int32_t* grid, int gw, int gh, const int4* pairs, int n, float* out,
+                      cudaStream_t stream) {
+  if (n <= 0) return MG_OK;
+  swap_delta_kernel<<<(n + 127) / 128, 128, 0, stream>>>(pal, grid, gw, gh, pairs, n, out);
+  g_launches += 1;
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+int launch_penalty(const float4* pal, const int32_t* grid, int gw, int gh, float weight, const int4* cxy, int n,
+                   float* out, cudaStream_t stream) {
+  if (n <= 0) return MG_OK;
+  penalty_kernel<<<(n + 127) / 128, 128, 0, stream>>>(pal, grid, gw, gh, weight, cxy, n, out);
+  g_launches += 1;
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+}  // namespace mg

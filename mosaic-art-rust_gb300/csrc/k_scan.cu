@@ -1,0 +1,237 @@
+// k_scan.cu -- (b) brute-force k-nearest scan over the material palette,
+// replacing the kiddo k-d tree query of main.rs:145-151 / 348-352
+// (nearest_n::<SquaredEuclidean>, k = min(P, 100)).
+//
+// Lab is 3-D, so the scan is SM/L1 work, not a contraction.  Design:
+//  - The palette (float4 per material) is streamed into shared memory in
+//    chunks of kChunk entries by TMA bulk copies (cp.async.bulk, completion on
+//    an mbarrier), double-buffered.  When the palette fits in the two stages it
+//    is loaded once and stays resident for every query the CTA handles.
+//  - One warp per query.  Each lane computes squared distances with no fused
+//    multiply-add (the reference's evaluation order), packs (distance bits,
+//    index) into a 64-bit key -- distances are non-negative, so key order is
+//    (distance, index) order and ties go to the lowest index -- and appends keys
+//    below the current k-th best to a per-warp buffer.  A full buffer is
+//    bitonic-sorted and merged into the sorted top-k list (merge-path ranks).
+#include "mg_internal.h"
+#include "mg_ptx.cuh"
+
+namespace mg {
+namespace {
+
+constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * 32;
+constexpr int kChunk = 2048;   // palette entries per shared-memory stage (32 KB)
+constexpr int kListCap = 128;  // k <= 100
+constexpr int kBufCap = 128;   // candidate buffer; merged when it could overflow
+constexpr unsigned long long kMaxKey = ~0ull;
+
+struct WarpLists {
+  unsigned long long list[kListCap];
+  unsigned long long tmp[kListCap];
+  unsigned long long buf[kBufCap];
+};
+
+constexpr size_t kSmemBytes = 2 * kChunk * sizeof(float4) + 16 + kWarps * sizeof(WarpLists);
+
+__device__ __forceinline__ int lower_bound_u64(const unsigned long long* a, int n, unsigned long long key) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Sort buf[0..m) ascending (m a power of two, <= kBufCap) with a bitonic network.
+__device__ void warp_bitonic_sort(unsigned long long* buf, int m, int lane) {
+  for (int size = 2; size <= m; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = lane; t < (m >> 1); t += 32) {
+        int i = 2 * t - (t & (stride - 1));
+        int j = i + stride;
+        bool asc = (i & size) == 0;
+        unsigned long long a = buf[i], b = buf[j];
+        if ((a > b) == asc) {
+          buf[i] = b;
+          buf[j] = a;
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Merge the nbuf buffered keys into the sorted list (first k kept).
+__device__ void warp_merge(WarpLists& W, int& len, int& nbuf, unsigned long long& thr, int k, int lane) {
+  if (nbuf == 0) return;
+  int m = 1;
+  while (m < nbuf) m <<= 1;
+  for (int i = nbuf + lane; i < m; i += 32) W.buf[i] = kMaxKey;
+  __syncwarp();
+  warp_bitonic_sort(W.buf, m, lane);
+  for (int i = lane; i < len; i += 32) {
+    unsigned long long key = W.list[i];
+    int r = i + lower_bound_u64(W.buf, nbuf, key);
+    if (r < k) W.tmp[r] = key;
+  }
+  for (int j = lane; j < nbuf; j += 32) {
+    unsigned long long key = W.buf[j];
+    int r = j + lower_bound_u64(W.list, len, key);
+    if (r < k) W.tmp[r] = key;
+  }
+  __syncwarp();
+  len = min(k, len + nbuf);
+  for (int i = lane; i < len; i += 32) W.list[i] = W.tmp[i];
+  __syncwarp();
+  nbuf = 0;
+  thr = (len == k) ? W.list[k - 1] : kMaxKey;
+}
+
+__global__ void __launch_bounds__(kThreads) nearest_kernel(const float4* __restrict__ pal, int p,
+                                                           const float4* __restrict__ queries, int nq, int k,
+                                                           int out_stride, uint32_t* __restrict__ out_idx,
+                                                           float* __restrict__ out_dist, uint32_t* __restrict__ err) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  float4* stage0 = reinterpret_cast<float4*>(smem);
+  float4* stages[2] = {stage0, stage0 + kChunk};
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * kChunk * sizeof(float4));
+  WarpLists* lists = reinterpret_cast<WarpLists*>(smem + 2 * kChunk * sizeof(float4) + 16);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nchunks = (p + kChunk - 1) / kChunk;
+  const bool resident = nchunks <= 2;
+  const int ngroups = (nq + kWarps - 1) / kWarps;
+  const int my_groups = blockIdx.x < ngroups ? (ngroups - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const long long total_seq = (long long)my_groups * nchunks;
+
+  auto chunk_len = [&](int c) { return min(kChunk, p - c * kChunk); };
+  auto issue = [&](int s, int c) {
+    const uint32_t bytes = (uint32_t)chunk_len(c) * sizeof(float4);
+    mbar_arrive_expect_tx(&bars[s], bytes);
+    tma_load_1d(stages[s], pal + (size_t)c * kChunk, bytes, &bars[s]);
+  };
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && total_seq > 0) {
+    if (resident) {
+      for (int c = 0; c < nchunks; ++c) issue(c, c);
+    } else {
+      issue(0, 0);
+      if (total_seq > 1) issue(1, 1 % nchunks);
+    }
+  }
+  uint32_t parity[2] = {0, 0};
+  if (resident && total_seq > 0) {
+    for (int c = 0; c < nchunks; ++c) {
+      if (!mbar_wait_bounded(&bars[c], 0)) {
+        atomicOr(err, kErrTimeout);
+        return;
+      }
+    }
+  }
+
+  WarpLists& W = lists[warp];
+  long long seq = 0;
+  for (int g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    const int qi = g * kWarps + warp;
+    const bool active = qi < nq;
+    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active) q = queries[qi];
+    int len = 0, nbuf = 0;
+    unsigned long long thr = kMaxKey;
+    for (int c = 0; c < nchunks; ++c, ++seq) {
+      const int s = resident ? c : (int)(seq & 1);
+      if (!resident) {
+        if (!mbar_wait_bounded(&bars[s], parity[s])) {
+          atomicOr(err, kErrTimeout);
+          return;
+        }
+        parity[s] ^= 1u;
+      }
+      const float4* sp = stages[s];
+      const int n = chunk_len(c);
+      const int gbase = c * kChunk;
+      if (active) {
+        for (int base = 0; base < n; base += 128) {
+          unsigned long long key[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int j = base + u * 32 + lane;
+            key[u] = kMaxKey;
+            if (j < n) {
+              const float4 e = sp[j];
+              const float d = sq_dist(q.x, q.y, q.z, e.x, e.y, e.z);
+              key[u] = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)(gbase + j);
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const bool pass = key[u] < thr;
+            const unsigned mask = __ballot_sync(0xffffffffu, pass);
+            if (mask) {
+              const int pos = nbuf + __popc(mask & ((1u << lane) - 1u));
+              if (pass) W.buf[pos] = key[u];
+              nbuf += __popc(mask);
+              __syncwarp();
+              if (nbuf > kBufCap - 32) warp_merge(W, len, nbuf, thr, k, lane);
+            }
+          }
+        }
+      }
+      if (!resident) {
+        __syncthreads();  // every warp is done with stage s
+        if (threadIdx.x == 0 && seq + 2 < total_seq) issue(s, (int)((seq + 2) % nchunks));
+      }
+    }
+    if (active) {
+      __syncwarp();
+      warp_merge(W, len, nbuf, thr, k, lane);
+      for (int i = lane; i < out_stride; i += 32) {
+        unsigned long long key = i < len ? W.list[i] : kMaxKey;
+        out_idx[(size_t)qi * out_stride + i] = i < len ? (uint32_t)key : 0xFFFFFFFFu;
+        out_dist[(size_t)qi * out_stride + i] = i < len ? __uint_as_float((uint32_t)(key >> 32)) : __int_as_float(0x7f800000);
+      }
+      __syncwarp();
+    }
+  }
+}
+
+}  // namespace
+
+int launch_nearest(const float4* pal, int p, const float4* queries, int nq, int k, uint32_t* idx, float* dist,
+                   uint32_t* err, cudaStream_t stream) {
+  if (nq <= 0) return MG_OK;
+  if (k <= 0 || k > 100) return fail(MG_ERR_ARG, "k must be in 1..100");
+  const int keff = min(k, p);
+  if (p <= 0) {
+    MG_CUDA(cudaMemsetAsync(idx, 0xFF, sizeof(uint32_t) * (size_t)nq * k, stream));
+    return MG_OK;
+  }
+  static int configured_device = -1;
+  int dev = 0;
+  MG_CUDA(cudaGetDevice(&dev));
+  if (configured_device != dev) {
+    MG_CUDA(cudaFuncSetAttribute(nearest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
+    configured_device = dev;
+  }
+  int sms = 0, per_sm = 0;
+  MG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nearest_kernel, kThreads, kSmemBytes));
+  if (per_sm < 1) per_sm = 1;
+  const int ngroups = (nq + kWarps - 1) / kWarps;
+  const int grid = min(ngroups, sms * per_sm);
+  // Rows shorter than k (p < k) are padded by the kernel with index ~0 / +inf.
+  nearest_kernel<<<grid, kThreads, kSmemBytes, stream>>>(pal, p, queries, nq, keff, k, idx, dist, err);
+  g_launches += 1;
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+}  // namespace mg

@@ -1,0 +1,135 @@
+// mg_internal.h -- shared declarations of the CUDA library behind mosaic_gpu.h.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/mosaic_gpu.h"
+#include "mg_math.h"
+
+namespace mg {
+
+// ---- errors -----------------------------------------------------------------
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define MG_CUDA(call)                                        \
+  do {                                                       \
+    cudaError_t _e = (call);                                 \
+    if (_e != cudaSuccess) return ::mg::cuda_fail(_e, #call); \
+  } while (0)
+
+#define MG_CHECK(status)           \
+  do {                             \
+    int _s = (status);             \
+    if (_s != MG_OK) return _s;    \
+  } while (0)
+
+// ---- device buffers ------------------------------------------------------------
+// A grow-only device allocation, reused across calls on one context.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes);
+  void release();
+  template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// Error word written by kernels whose waits are bounded (a wait that runs out
+// sets it and the kernel returns); read back by the host after a launch.
+enum KernelError : uint32_t { kErrNone = 0, kErrTimeout = 1, kErrRange = 2 };
+
+// Region of an RGB8 image: byte offset of its first pixel, size, row stride.
+struct Region {
+  int64_t offset;
+  int32_t w, h;
+  int64_t stride;
+};
+
+// Per-region sums from the Lab reduction: fixed-point L, a, b and u64 R, G, B.
+struct RegionSums {
+  long long lab[3];
+  unsigned long long rgb[3];
+};
+
+// Grid geometry for cell regions of a target image.
+struct CellGeom {
+  int gw, gh, cw, ch;
+  int64_t stride;
+};
+
+// ---- kernels (launchers; all asynchronous on `stream`) -----------------------
+// (a) Lab + mean RGB of regions.  Cells of a target (geom != nullptr) or an
+// explicit region list.  out_lab: float4 (L, a, b, 0); out_rgb: uchar4.
+int launch_region_stats(const uint8_t* base, const CellGeom* geom, const Region* regions, int n_regions,
+                        int64_t max_region_px, float4* out_lab, uchar4* out_rgb, RegionSums* scratch,
+                        int want_lab, cudaStream_t stream);
+void upload_lab_consts(cudaStream_t stream);
+
+// Area-average thumbnails of regions at tw x th.
+int launch_thumbnails(const uint8_t* base, const Region* regions, int n, int tw, int th, uint8_t* out,
+                      cudaStream_t stream);
+
+// (b) k nearest palette entries for every query (ties -> lowest index).
+int launch_nearest(const float4* pal, int p, const float4* queries, int nq, int k, uint32_t* idx,
+                   float* dist, uint32_t* err, cudaStream_t stream);
+
+// (c) similarity matrix, full (P x P) or strict upper triangle.
+int launch_similarity(const float4* pal, int p, int triangular, float* out, cudaStream_t stream);
+
+// (d) greedy placement of one or more mosaics.
+struct GreedyJob {
+  const uint32_t* cand_idx;  // N x k
+  const float* cand_dist;    // N x k
+  int32_t* grid;             // N (palette index)
+  int gw, gh, k;
+  uint32_t max_usage;
+  float weight;
+  int* n_resets;             // 1 int
+  float* total_cost;         // 1 float: calculate_total_cost of the placed grid
+};
+int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_jobs, uint32_t* usage_scratch,
+                  int smem_usage, cudaStream_t stream);
+
+// (e) annealing chains.
+struct ChainResult {
+  float initial_cost, final_cost, best_cost, pad;
+  long long accepted, improved, cooled, pad2;
+};
+struct AnnealJob {
+  const int32_t* grid_in;   // N
+  int32_t* chain_grids;     // chains x N
+  ChainResult* results;     // chains
+  const float* initial_cost;  // 1 float (calculate_total_cost of grid_in); nullptr -> computed
+  int gw, gh, chains;
+  long long iters;
+  float t0, decay;
+  uint32_t key0, key1, stream;
+  int greedy_only;
+};
+int launch_anneal(const float4* pal, int p, const AnnealJob* jobs_dev, const int* chain_job_dev,
+                  const int* chain_id_dev, int total_chains, int max_cells, cudaStream_t stream);
+int launch_select_best(const AnnealJob* jobs_dev, int n_jobs, int32_t* const* final_grids_dev,
+                       int* best_chain_dev, cudaStream_t stream);
+int launch_total_cost(const float4* pal, const int32_t* grid, int gw, int gh, float* out, cudaStream_t stream);
+int launch_swap_delta(const float4* pal, const int32_t* grid, int gw, int gh, const int4* pairs, int n, float* out,
+                      cudaStream_t stream);
+int launch_penalty(const float4* pal, const int32_t* grid, int gw, int gh, float weight, const int4* cxy, int n,
+                   float* out, cudaStream_t stream);
+
+// (f) colour adjustment + composite.
+int launch_cell_adjust(const int32_t* grid, int n_cells, const uchar4* thumb_rgb, const uchar4* cell_rgb,
+                       float strength, float4* adj, cudaStream_t stream);
+int launch_composite(const int32_t* grid, int gw, int gh, const uint8_t* thumbs, int tw, int th, const float4* adj,
+                     int do_adjust, uint8_t* out, cudaStream_t stream);
+int launch_adjust_image(const float4 adj, const uint8_t* in, int w, int h, int64_t stride, uint8_t* out,
+                        cudaStream_t stream);
+int launch_optimal_adjustment(const uint8_t* tile_rgb, const uint8_t* target_rgb, int n, float strength,
+                              float4* out, cudaStream_t stream);
+
+// Number of kernel launches issued by this library since load (for reporting).
+extern unsigned long long g_launches;
+
+}  // namespace mg

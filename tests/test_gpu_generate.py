@@ -1,0 +1,108 @@
+"""Whole generate_mosaic jobs on the GPU (through the C ABI) against the CPU oracle.
+
+Bar: grid and annealed chain bit-exact, output pixels within 1 LSB (observed:
+exact), palette size and fallback count equal.  The full recommended-settings
+workload (3840x2880, 1500 materials, 80x60, 32 chains x 2000 iterations) is
+compared at full size.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _compare(ctx, orc, cfg, threads=8):
+    from mosaic_gpu import job
+
+    inp = job.make_inputs(cfg)
+    res, grid, image = job.generate(ctx, job.RequestHolder(inp))
+    ref = orc.generate(inp, threads=threads)
+    assert res.palette_size == ref["p"]
+    assert res.n_resets == ref["n_resets"]
+    assert np.array_equal(grid, ref["grid"])
+    assert int(np.abs(image.astype(np.int16) - ref["image"].astype(np.int16)).max(initial=0)) <= 1
+    assert res.best_chain == ref["best_chain"]
+    assert np.float32(res.final_cost) == np.float32(ref["final_cost"])
+    assert np.float32(res.initial_cost) == np.float32(ref["initial_cost"])
+    return inp, res, grid, image, ref
+
+
+def _small(name, **kw):
+    from mosaic_gpu import job
+
+    return job.scaled(job.WORKLOADS[name], **kw)
+
+
+@pytest.mark.parametrize("cfg_kw", [
+    dict(name="small", target_w=320, target_h=240, n_materials=120, material_side=32, grid_w=16, grid_h=12),
+    dict(name="recommended", target_w=480, target_h=360, n_materials=150, material_side=64, grid_w=20, grid_h=15,
+         tile_w=12, tile_h=12, iterations=500, chains=6),
+    dict(name="large", target_w=716, target_h=536, n_materials=400, material_side=32, grid_w=35, grid_h=26,
+         tile_w=8, tile_h=8, iterations=3000, chains=8, blobs=16),
+])
+def test_generate_scaled_workloads(ctx, orc, cfg_kw):
+    name = cfg_kw.pop("name")
+    _compare(ctx, orc, _small(name, **cfg_kw))
+
+
+def test_generate_edge_cases(ctx, orc):
+    # every material rejected (max_materials 0) -> nothing placed, black output
+    cfg = _small("small", target_w=64, target_h=48, n_materials=10, material_side=16, grid_w=8, grid_h=6,
+                 max_materials=0)
+    from mosaic_gpu import job
+
+    inp = job.make_inputs(cfg)
+    holder = job.RequestHolder(inp)
+    holder.req.max_materials = 0
+    res, grid, image = job.generate(ctx, holder)
+    assert res.palette_size == 0 and np.all(grid == -1) and not image.any()
+    # one material only, optimisation on, colour on
+    _compare(ctx, orc, _small("recommended", target_w=96, target_h=72, n_materials=3, material_side=16,
+                              material_mode=0, grid_w=8, grid_h=6, tile_w=4, tile_h=4, iterations=50, chains=2))
+    # optimisation off, weight 0
+    _compare(ctx, orc, _small("small", target_w=200, target_h=150, n_materials=60, material_side=16, grid_w=10,
+                              grid_h=10, weight=0.0))
+    _compare(ctx, orc, _small("small", target_w=200, target_h=150, n_materials=60, material_side=16, grid_w=10,
+                              grid_h=10, enable_optimization=False))
+    # grid that does not divide the image (remainder ignored), max usage 1
+    _compare(ctx, orc, _small("recommended", target_w=203, target_h=157, n_materials=90, material_side=20,
+                              grid_w=11, grid_h=9, tile_w=0, tile_h=0, max_usage=1, iterations=300, chains=3))
+
+
+def test_device_thumbnails_equal_host_thumbnails(ctx, orc):
+    from mosaic_gpu import job
+
+    cfg = _small("recommended", target_w=240, target_h=180, n_materials=60, material_side=40, grid_w=10, grid_h=9,
+                 tile_w=9, tile_h=7, iterations=200, chains=2)
+    inp = job.make_inputs(cfg)
+    res_a, grid_a, img_a = job.generate(ctx, job.RequestHolder(inp))
+    inp_dev = job.Inputs(cfg, inp.target, inp.mats, None)
+    res_b, grid_b, img_b = job.generate(ctx, job.RequestHolder(inp_dev))
+    assert np.array_equal(grid_a, grid_b) and np.array_equal(img_a, img_b)
+
+
+def test_plan_rerun_is_deterministic(ctx):
+    from mosaic_gpu import job
+
+    cfg = _small("recommended", target_w=480, target_h=360, n_materials=150, material_side=64, grid_w=20, grid_h=15,
+                 tile_w=12, tile_h=12, iterations=500, chains=6)
+    inp = job.make_inputs(cfg)
+    plan = job.Plan(ctx, job.RequestHolder(inp))
+    plan.run()
+    r1, g1, i1 = plan.read()
+    plan.run()
+    r2, g2, i2 = plan.read()
+    assert np.array_equal(g1, g2) and np.array_equal(i1, i2) and r1.final_cost == r2.final_cost
+    ms = plan.stage_ms()
+    assert len(ms) == 8 and ms[-1] > 0
+    assert plan.launches() > 0
+    plan.close()
+
+
+def test_full_recommended_workload(ctx, orc):
+    """Full-size recommended-settings mosaic, bit-exact against the oracle."""
+    from mosaic_gpu import job
+
+    inp, res, grid, image, ref = _compare(ctx, orc, job.WORKLOADS["recommended"], threads=16)
+    assert grid.shape == (60, 80) and image.shape == (2880, 3840, 3)
+    assert res.palette_size > 400 and res.best_chain >= 0
