@@ -91,7 +91,7 @@ def test_nearest_bit_exact(ctx, orc, p, k, nq):
         pal[p // 2] = pal[1]
         pal[p - 1] = pal[1]
     q = rand_lab(rng, nq)
-    q[0] = pal[1]
+    q[0] = pal[min(1, p - 1)]
     idx, dist = ctx.nearest_n(pal, q, k)
     ridx, rdist = orc.nearest_n(pal, q, k)
     kk = min(k, p)
