@@ -51,6 +51,9 @@ unsigned long long mg_kernel_launches(void);
 int mg_ctx_create(int device, mg_ctx** out);
 int mg_ctx_destroy(mg_ctx* ctx);
 int mg_ctx_sync(mg_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), so a caller can order its own
+ * device work (and timing events) with the library's. */
+void* mg_ctx_stream(mg_ctx* ctx);
 /* Pinned host memory (for fast host<->device copies); NULL on failure. */
 void* mg_host_alloc(size_t bytes);
 void mg_host_free(void* p);

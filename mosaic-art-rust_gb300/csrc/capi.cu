@@ -184,6 +184,8 @@ int mg_ctx_sync(mg_ctx* ctx) {
   return finish(ctx);
 }
 
+void* mg_ctx_stream(mg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
 void* mg_host_alloc(size_t bytes) {
   void* p = nullptr;
   if (cudaHostAlloc(&p, bytes ? bytes : 16, cudaHostAllocPortable | cudaHostAllocMapped) != cudaSuccess) {

@@ -78,6 +78,7 @@ SIGNATURES = [
     ("mg_ctx_create", C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     ("mg_ctx_destroy", C.c_int, [C.c_void_p]),
     ("mg_ctx_sync", C.c_int, [C.c_void_p]),
+    ("mg_ctx_stream", C.c_void_p, [C.c_void_p]),
     ("mg_host_alloc", C.c_void_p, [C.c_size_t]),
     ("mg_host_free", None, [C.c_void_p]),
     ("mg_average_lab", C.c_int, [C.c_void_p, _u8p, C.c_int, C.c_int, C.c_int64, _f32p]),

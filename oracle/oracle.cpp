@@ -745,7 +745,8 @@ int orc_generate(const orc_job* J, orc_out* O) {
   });
   std::vector<float> cell_lab(3 * (size_t)N);
   std::vector<uint8_t> cell_rgb(3 * (size_t)N);
-  parallel_for(J->gh, J->threads, [&](int y) {
+  // Cells are sequential, as in the reference's row-major loop (main.rs:529-541).
+  parallel_for(J->gh, 1, [&](int y) {
     for (int x = 0; x < J->gw; ++x) {
       const uint8_t* base = J->target + (long)y * ch * J->tstride + 3L * x * cw;
       int c = y * J->gw + x;
