@@ -68,6 +68,23 @@ int mg_is_aspect_ratio_match(float img_aspect, float target_aspect, float tolera
  * (w/gw) x (h/gh).  lab_out: gw*gh*3 floats; avg_rgb_out (nullable): gw*gh*3. */
 int mg_cells_lab(mg_ctx* ctx, const uint8_t* img, int w, int h, int64_t stride, int gw, int gh,
                  float* lab_out, uint8_t* avg_rgb_out);
+/* No counterpart in the reference.  mg_cells_lab for callers that cannot
+ * allocate device memory where they call it -- e.g. a serving process whose
+ * device memory belongs to its own pool allocator under a fixed budget, or
+ * code that must not incur the device-wide synchronisation of cudaMalloc /
+ * cudaFree between other work.  Everything is caller-owned and
+ * device-accessible: d_img (stride bytes per row), d_lab4 (gw*gh x 4 floats:
+ * L, a, b, 0; 16-byte aligned), d_rgb4 (nullable, gw*gh x 4 bytes: R, G, B, 0).
+ * Work is queued on `stream` (a cudaStream_t, NULL = default stream) and no
+ * memory is allocated: the per-cell sums live in a fixed device array the
+ * library reserves on each GPU that loads it (1.5 MB), so at most 32768 cells
+ * per call (MG_ERR_ARG beyond).  The first call on a device resolves that
+ * array's address and uploads constants (it synchronises the device), so make
+ * it before any stream capture.  All calls share the array: calls whose work
+ * overlaps on the GPU (other streams, other threads) race and must be ordered
+ * by the caller.  Results equal mg_cells_lab's bit for bit. */
+int mg_cells_lab_noalloc(const uint8_t* d_img, int w, int h, int64_t stride, int gw, int gh, float* d_lab4,
+                         uint8_t* d_rgb4, void* stream);
 /* main.rs:193-208, 244-253 (process_tile -> calculate_average_lab for each
  * material) in one launch.  lab_out: n*3; avg_rgb_out (nullable): n*3. */
 int mg_images_lab(mg_ctx* ctx, const uint8_t* const* imgs, const int* w, const int* h,

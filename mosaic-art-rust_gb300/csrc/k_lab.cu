@@ -239,6 +239,61 @@ int launch_region_stats(const uint8_t* base, const CellGeom* geom, const Region*
   return MG_OK;
 }
 
+// ---- allocation-free cell statistics ------------------------------------------------------
+// Some callers of the cell reduction cannot allocate device memory at the
+// point where they call it: a serving process whose device memory is owned by
+// its own pool allocator under a fixed budget (an extra cudaMalloc there either
+// fails or breaks the budget), or code that must not pay cudaMalloc/cudaFree's
+// implicit device synchronisation in the middle of a stream of work.  For them
+// mg_cells_lab_noalloc takes device pointers and keeps its per-cell sums in the
+// file-scope array below, which the library reserves on every GPU that loads it
+// (kNoAllocMaxCells * 48 bytes = 1.5 MB) until the process exits.
+namespace {
+constexpr int kNoAllocMaxCells = 32768;
+static __device__ __align__(256) RegionSums g_noalloc_sums[kNoAllocMaxCells];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+RegionSums* g_noalloc_ptr[kMaxDevices] = {};
+}  // namespace
+
+}  // namespace mg
+
+extern "C" int mg_cells_lab_noalloc(const uint8_t* d_img, int w, int h, int64_t stride, int gw, int gh,
+                                    float* d_lab4, uint8_t* d_rgb4, void* stream) {
+  using namespace mg;
+  if (!d_img || !d_lab4 || w <= 0 || h <= 0 || stride < 3ll * w) return fail(MG_ERR_ARG, "invalid image");
+  if (gw <= 0 || gh <= 0 || w / gw <= 0 || h / gh <= 0) return fail(MG_ERR_ARG, "grid larger than the image");
+  if ((int64_t)gw * gh > kNoAllocMaxCells)
+    return fail(MG_ERR_ARG, "mg_cells_lab_noalloc handles at most " + std::to_string(kNoAllocMaxCells) +
+                                " cells; use mg_cells_lab for larger grids");
+  if ((reinterpret_cast<uintptr_t>(d_lab4) & 15) || (reinterpret_cast<uintptr_t>(d_rgb4) & 3))
+    return fail(MG_ERR_ARG, "lab output must be 16-byte aligned and rgb output 4-byte aligned");
+  int dev = 0;
+  MG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(MG_ERR_ARG, "device ordinal out of range");
+  RegionSums* sums = nullptr;
+  {
+    // First call on a device: resolve the array's device address (the host-side
+    // symbol is only a stand-in) and upload the Lab constants to that device.
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      MG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_sums));
+      upload_lab_consts(0);
+      MG_CUDA(cudaDeviceSynchronize());
+      g_noalloc_ptr[dev] = static_cast<RegionSums*>(p);
+    }
+    sums = g_noalloc_ptr[dev];
+  }
+  const int n = gw * gh;
+  CellGeom g{gw, gh, w / gw, h / gh, stride};
+  return launch_region_stats(d_img, &g, nullptr, n, (int64_t)g.cw * g.ch, reinterpret_cast<float4*>(d_lab4),
+                             reinterpret_cast<uchar4*>(d_rgb4), sums, 1, static_cast<cudaStream_t>(stream));
+}
+
+namespace mg {
+
 int launch_thumbnails(const uint8_t* base, const Region* regions, int n, int tw, int th, uint8_t* out,
                       cudaStream_t stream) {
   if (n <= 0) return MG_OK;

@@ -84,6 +84,8 @@ SIGNATURES = [
     ("mg_average_lab", C.c_int, [C.c_void_p, _u8p, C.c_int, C.c_int, C.c_int64, _f32p]),
     ("mg_is_aspect_ratio_match", C.c_int, [C.c_float, C.c_float, C.c_float]),
     ("mg_cells_lab", C.c_int, [C.c_void_p, _u8p, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_int, _f32p, _u8p]),
+    ("mg_cells_lab_noalloc", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_int, C.c_void_p,
+                                       C.c_void_p, C.c_void_p]),
     ("mg_images_lab", C.c_int, [C.c_void_p, C.POINTER(_u8p), C.POINTER(C.c_int), C.POINTER(C.c_int), _i64p,
                                 C.c_int, _f32p, _u8p]),
     ("mg_select_palette", C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_float, C.c_float,
