@@ -73,7 +73,7 @@ struct mg_plan {
   // device buffers
   DevBuf target, mats, regions, thumb_regions, thumbs, pal_lab, thumb_rgb, sim, cell_lab, cell_rgb, cand_idx,
       cand_dist, grid_greedy, resets, init_cost, greedy_job, chain_grids, chain_res, anneal_job, final_grid,
-      finals_ptr, best_chain, adj, out, sums, err;
+      finals_ptr, best_chain, adj, out, sums, err, usage;
   cudaEvent_t ev[8] = {};
   bool events = false;
   int launches = 0;
@@ -455,9 +455,10 @@ int mg_place_greedy(mg_ctx* ctx, const float* palette_lab, int p, const float* c
   auto q = to_f4(cell_lab, n);
   MG_CHECK(upload(ctx, ctx->in0, pal.data(), sizeof(float4) * p));
   MG_CHECK(upload(ctx, ctx->in1, q.data(), sizeof(float4) * n));
-  MG_CHECK(ctx->out0.ensure(sizeof(uint32_t) * (size_t)n * k));
-  MG_CHECK(ctx->out1.ensure(sizeof(float) * (size_t)n * k));
+  MG_CHECK(ctx->out0.ensure(sizeof(uint32_t) * padded_cells(n) * k));
+  MG_CHECK(ctx->out1.ensure(sizeof(float) * padded_cells(n) * k));
   MG_CHECK(ctx->out2.ensure(sizeof(int32_t) * n + 64));
+  MG_CHECK(ctx->sums.ensure(sizeof(uint32_t) * p));
   MG_CHECK(launch_nearest(ctx->in0.as<float4>(), p, ctx->in1.as<float4>(), n, k, ctx->out0.as<uint32_t>(),
                           ctx->out1.as<float>(), ctx->err.as<uint32_t>(), ctx->stream));
   int32_t* d_grid = ctx->out2.as<int32_t>();
@@ -465,12 +466,8 @@ int mg_place_greedy(mg_ctx* ctx, const float* palette_lab, int p, const float* c
   GreedyJob job{ctx->out0.as<uint32_t>(), ctx->out1.as<float>(), d_grid, gw, gh, k,
                 (uint32_t)cfg->max_usage_per_image, cfg->adjacency_penalty_weight, d_resets, nullptr};
   MG_CHECK(upload(ctx, ctx->regions, &job, sizeof(job)));
-  const size_t row_bytes = ((size_t)gw * 4 + 15) & ~(size_t)15;
-  const bool smem_usage = row_bytes + (size_t)p * 4 <= 190 * 1024;
-  if (!smem_usage) MG_CHECK(ctx->sums.ensure(sizeof(uint32_t) * p));
-  MG_CHECK(launch_greedy(ctx->in0.as<float4>(), p, ctx->regions.as<GreedyJob>(), 1,
-                         smem_usage ? nullptr : ctx->sums.as<uint32_t>(),
-                         (int)(row_bytes + (smem_usage ? (size_t)p * 4 : 0)), ctx->stream));
+  MG_CHECK(launch_greedy(ctx->in0.as<float4>(), p, ctx->regions.as<GreedyJob>(), 1, k, gw, ctx->sums.as<uint32_t>(),
+                         ctx->err.as<uint32_t>(), ctx->stream));
   MG_CUDA(cudaMemcpyAsync(grid_out, d_grid, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
   int resets = 0;
   MG_CUDA(cudaMemcpyAsync(&resets, d_resets, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -670,7 +667,7 @@ void plan_release(mg_plan* pl) {
   for (DevBuf* b : {&pl->target, &pl->mats, &pl->regions, &pl->thumb_regions, &pl->thumbs, &pl->pal_lab,
                     &pl->thumb_rgb, &pl->sim, &pl->cell_lab, &pl->cell_rgb, &pl->cand_idx, &pl->cand_dist,
                     &pl->grid_greedy, &pl->resets, &pl->init_cost, &pl->greedy_job, &pl->chain_grids, &pl->chain_res,
-                    &pl->anneal_job, &pl->final_grid, &pl->finals_ptr, &pl->best_chain, &pl->adj, &pl->out, &pl->sums,
+                    &pl->anneal_job, &pl->final_grid, &pl->finals_ptr, &pl->best_chain, &pl->adj, &pl->out, &pl->sums, &pl->usage,
                     &pl->err})
     b->release();
   if (pl->events)
@@ -775,8 +772,9 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r) {
   if (pl->build_sim) MG_CHECK(pl->sim.ensure(sizeof(float) * (size_t)std::max(P, 1) * std::max(P, 1)));
   MG_CHECK(pl->cell_lab.ensure(sizeof(float4) * N));
   MG_CHECK(pl->cell_rgb.ensure(sizeof(uchar4) * N));
-  MG_CHECK(pl->cand_idx.ensure(sizeof(uint32_t) * (size_t)N * k));
-  MG_CHECK(pl->cand_dist.ensure(sizeof(float) * (size_t)N * k));
+  MG_CHECK(pl->cand_idx.ensure(sizeof(uint32_t) * padded_cells(N) * k));
+  MG_CHECK(pl->usage.ensure(sizeof(uint32_t) * std::max(P, 1)));
+  MG_CHECK(pl->cand_dist.ensure(sizeof(float) * padded_cells(N) * k));
   MG_CHECK(pl->grid_greedy.ensure(sizeof(int32_t) * N));
   MG_CHECK(pl->resets.ensure(16));
   MG_CHECK(pl->init_cost.ensure(16));
@@ -860,12 +858,8 @@ int plan_run(mg_plan* pl) {
   MG_CUDA(cudaEventRecord(pl->ev[4], s));
   // [4] greedy placement
   if (P > 0) {
-    const size_t row_bytes = ((size_t)pl->gw * 4 + 15) & ~(size_t)15;
-    const bool smem_usage = row_bytes + (size_t)P * 4 <= 190 * 1024;
-    if (!smem_usage) MG_CHECK(pl->sums.ensure(sizeof(uint32_t) * P));
-    MG_CHECK(launch_greedy(pl->pal_lab.as<float4>(), P, pl->greedy_job.as<GreedyJob>(), 1,
-                           smem_usage ? nullptr : pl->sums.as<uint32_t>(),
-                           (int)(row_bytes + (smem_usage ? (size_t)P * 4 : 0)), s));
+    MG_CHECK(launch_greedy(pl->pal_lab.as<float4>(), P, pl->greedy_job.as<GreedyJob>(), 1, pl->k, pl->gw,
+                           pl->usage.as<uint32_t>(), pl->err.as<uint32_t>(), s));
   } else {
     MG_CUDA(cudaMemsetAsync(pl->grid_greedy.p, 0xFF, sizeof(int32_t) * N, s));
   }

@@ -12,23 +12,41 @@
 // of chain c, Philox4x32-10 with key (seed lo, seed hi) and counter
 // (t, c, stream, 2*(t>>32)) gives x1, y1, x2, y2 (multiply-high range
 // reduction) and counter (t, c, stream, 2*(t>>32)+1) gives the acceptance
-// uniform, so a CPU replay of the same stream makes the same decisions.
-// Lanes compute Philox for 32 iterations at once.  Per proposal, lanes 0-3
-// evaluate the neighbours of pos1 (up, down, left, right), lanes 4-7 those of
-// pos2, lane 8 the mutual pair; the old and new sums are then accumulated in
-// exactly the reference's order (absent terms are +0 and leave a sum as is).
+// uniform, so a CPU replay of the same stream makes the same decisions.  The
+// lanes fill a 64-entry ring of decoded proposals 32 at a time.
+//
+// A chain is sequential, and one proposal alone is a long dependent chain of
+// instructions, so the warp evaluates kGroups = 4 consecutive proposals at once
+// (8 lanes each: lanes 0-3 the up/down/left/right neighbours of pos1, 4-7 those
+// of pos2; the lane whose pos1 neighbour is pos2 supplies the mutual term) on
+// the same grid, and then commits them in order.  This is exact:
+//  - a proposal reads only pos1, pos2 and their neighbours, so its delta equals
+//    the sequential one unless an earlier proposal of the same round swapped one
+//    of those cells; the commit stops at the first proposal whose read cells lie
+//    within Manhattan distance 1 of an earlier accepted swap, and the next round
+//    re-evaluates it on the updated grid;
+//  - whether an iteration is skipped (pos1 == pos2 or an empty cell) does not
+//    depend on the grid's state (swaps never move empty cells), so the
+//    temperature of each proposal in the round -- T multiplied by the decay once
+//    per earlier non-skipped iteration, as in the reference -- is known before
+//    the commit, and so is the acceptance decision;
+//  - the costs are accumulated in the reference's order (old and new sums over
+//    the neighbour slots in order, the mutual term last; delta = new - old; the
+//    running cost += delta per accepted swap, in iteration order).
 // The acceptance test uses this library's own exp, identical on host and
-// device.  An iteration that draws pos1 == pos2 or an empty cell is skipped
-// without cooling, as in the reference.
+// device.
 #include "mg_internal.h"
 
 namespace mg {
 namespace {
 
 constexpr uint16_t kNone16 = 0xFFFFu;
+constexpr int kGroups = 4;     // proposals evaluated per round
+constexpr int kRing = 64;      // decoded proposals kept in shared memory
 
 __device__ __forceinline__ float wgt(const float4& a, const float4& b) {
-  return adj_weight_from_sim(lab_distance(a.x, a.y, a.z, b.x, b.y, b.z));
+  // 1/(sim+1): the correctly rounded reciprocal equals the correctly rounded 1.0/x.
+  return __frcp_rn(__fadd_rn(lab_distance(a.x, a.y, a.z, b.x, b.y, b.z), 1.0f));
 }
 
 template <bool kLabSmem>
@@ -42,8 +60,10 @@ __global__ void __launch_bounds__(32) anneal_kernel(const float4* __restrict__ p
   const int chain = chain_id ? chain_id[blockIdx.x] : (int)blockIdx.x;
   const AnnealJob J = jobs[jid];
   const int gw = J.gw, gh = J.gh, n = gw * gh;
-  float4* s_lab = reinterpret_cast<float4*>(smem);
-  uint16_t* s_grid = reinterpret_cast<uint16_t*>(smem + (kLabSmem ? (size_t)p * sizeof(float4) : 0));
+  int4* s_ring = reinterpret_cast<int4*>(smem);
+  float4* s_lab = reinterpret_cast<float4*>(smem + kRing * sizeof(int4));
+  uint16_t* s_grid =
+      reinterpret_cast<uint16_t*>(smem + kRing * sizeof(int4) + (kLabSmem ? (size_t)p * sizeof(float4) : 0));
   if (kLabSmem)
     for (int i = lane; i < p; i += 32) s_lab[i] = pal[i];
   for (int i = lane; i < n; i += 32) {
@@ -85,89 +105,133 @@ __global__ void __launch_bounds__(32) anneal_kernel(const float4* __restrict__ p
   const float decay = J.decay;
   const bool greedy_only = J.greedy_only != 0;
   const uint32_t k0 = J.key0, k1 = J.key1, strm = J.stream;
+  const long long iters = J.iters;
+  const int grp = lane >> 3, slot = lane & 7;
+  const int leader = grp << 3;
 
-  uint32_t rx1 = 0, ry1 = 0, rx2 = 0, ry2 = 0;
-  float ru = 0.0f;
-  for (long long it = 0; it < J.iters; ++it) {
-    const int src = (int)(it & 31);
-    if (src == 0) {
-      const long long my = it + lane;
-      const uint32_t hi = (uint32_t)((unsigned long long)my >> 32);
-      const u32x4 a = philox((uint32_t)my, (uint32_t)chain, strm, 2u * hi, k0, k1);
-      rx1 = range_u32(a.x, (uint32_t)gw);
-      ry1 = range_u32(a.y, (uint32_t)gh);
-      rx2 = range_u32(a.z, (uint32_t)gw);
-      ry2 = range_u32(a.w, (uint32_t)gh);
-      const u32x4 b = philox((uint32_t)my, (uint32_t)chain, strm, 2u * hi + 1u, k0, k1);
-      ru = unit_f32(b.x);
+  long long it = 0, filled = 0;
+  while (it < iters) {
+    if (filled < iters && filled - it < kGroups) {
+      const long long my = filled + lane;
+      if (my < iters) {
+        const uint32_t hi = (uint32_t)((unsigned long long)my >> 32);
+        const u32x4 a = philox((uint32_t)my, (uint32_t)chain, strm, 2u * hi, k0, k1);
+        const u32x4 b = philox((uint32_t)my, (uint32_t)chain, strm, 2u * hi + 1u, k0, k1);
+        const uint32_t x1 = range_u32(a.x, (uint32_t)gw), y1 = range_u32(a.y, (uint32_t)gh);
+        const uint32_t x2 = range_u32(a.z, (uint32_t)gw), y2 = range_u32(a.w, (uint32_t)gh);
+        s_ring[my & (kRing - 1)] = make_int4((int)(x1 | (y1 << 16)), (int)(x2 | (y2 << 16)),
+                                             __float_as_int(unit_f32(b.x)), 0);
+      }
+      filled += 32;
+      __syncwarp();
     }
-    const int x1 = (int)__shfl_sync(0xffffffffu, rx1, src), y1 = (int)__shfl_sync(0xffffffffu, ry1, src);
-    const int x2 = (int)__shfl_sync(0xffffffffu, rx2, src), y2 = (int)__shfl_sync(0xffffffffu, ry2, src);
-    const float u = __shfl_sync(0xffffffffu, ru, src);
+    // ---- evaluate proposal it + grp --------------------------------------------------
+    const long long i = it + grp;
+    const bool live = i < iters;
+    int4 e = make_int4(0, 0, 0, 0);
+    if (live) e = s_ring[i & (kRing - 1)];
+    const int x1 = e.x & 0xFFFF, y1 = (e.x >> 16) & 0xFFFF, x2 = e.y & 0xFFFF, y2 = (e.y >> 16) & 0xFFFF;
+    const float u = __int_as_float(e.z);
     const int p1 = y1 * gw + x1, p2 = y2 * gw + x2;
-    if (p1 == p2) continue;
-    const uint16_t g1 = s_grid[p1], g2 = s_grid[p2];
-    if (g1 == kNone16 || g2 == kNone16) continue;
-    float delta = 0.0f;
-    if (g1 != g2) {
-      float o = 0.0f, nw = 0.0f;
-      if (lane < 8) {
-        const bool first = lane < 4;
-        const int bx = first ? x1 : x2, by = first ? y1 : y2;
-        const int other = first ? p2 : p1;
-        const int dir = lane & 3;
-        int nx = bx, ny = by;
-        bool inb;
-        if (dir == 0) { ny = by - 1; inb = by > 0; }
-        else if (dir == 1) { ny = by + 1; inb = by < gh - 1; }
-        else if (dir == 2) { nx = bx - 1; inb = bx > 0; }
-        else { nx = bx + 1; inb = bx < gw - 1; }
-        if (inb) {
-          const int nb = ny * gw + nx;
-          if (nb != other) {
-            const uint16_t a = s_grid[nb];
-            if (a != kNone16) {
-              const float4 la = lab(a);
-              const float w1 = wgt(lab(g1), la), w2 = wgt(lab(g2), la);
-              o = first ? w1 : w2;
-              nw = first ? w2 : w1;
-            }
+    bool skip = !live || p1 == p2;
+    uint16_t g1 = 0, g2 = 0;
+    if (!skip) {
+      g1 = s_grid[p1];
+      g2 = s_grid[p2];
+      skip = g1 == kNone16 || g2 == kNone16;
+    }
+    const bool same = g1 == g2;
+    float o = 0.0f, nw = 0.0f, m = 0.0f;
+    if (!skip && !same) {
+      const bool first = slot < 4;
+      const int bx = first ? x1 : x2, by = first ? y1 : y2;
+      const int other = first ? p2 : p1;
+      const int dir = slot & 3;
+      int nx = bx, ny = by;
+      bool inb;
+      if (dir == 0) { ny = by - 1; inb = by > 0; }
+      else if (dir == 1) { ny = by + 1; inb = by < gh - 1; }
+      else if (dir == 2) { nx = bx - 1; inb = bx > 0; }
+      else { nx = bx + 1; inb = bx < gw - 1; }
+      if (inb) {
+        const int nb = ny * gw + nx;
+        if (nb == other) {
+          if (first) m = wgt(lab(g1), lab(g2));
+        } else {
+          const uint16_t a = s_grid[nb];
+          if (a != kNone16) {
+            const float4 la = lab(a);
+            const float w1 = wgt(lab(g1), la), w2 = wgt(lab(g2), la);
+            o = first ? w1 : w2;
+            nw = first ? w2 : w1;
           }
         }
-      } else if (lane == 8) {
-        const int dx = x1 - x2, dy = y1 - y2;
-        if ((dx == 0 && (dy == 1 || dy == -1)) || (dy == 0 && (dx == 1 || dx == -1))) {
-          const float c = wgt(lab(g1), lab(g2));
-          o = c;
-          nw = c;
+      }
+    }
+    float old_cost = 0.0f, new_cost = 0.0f;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      old_cost = __fadd_rn(old_cost, __shfl_sync(0xffffffffu, o, leader + t));
+      new_cost = __fadd_rn(new_cost, __shfl_sync(0xffffffffu, nw, leader + t));
+    }
+    const int dx = x2 - x1, dy = y2 - y1;
+    const bool adjacent = (dx == 0 && (dy == 1 || dy == -1)) || (dy == 0 && (dx == 1 || dx == -1));
+    const int dir12 = dy == -1 ? 0 : (dy == 1 ? 1 : (dx == -1 ? 2 : 3));
+    const float mm = __shfl_sync(0xffffffffu, m, leader + dir12);
+    if (adjacent) {
+      old_cost = __fadd_rn(old_cost, mm);
+      new_cost = __fadd_rn(new_cost, mm);
+    }
+    const float delta = same ? 0.0f : __fsub_rn(new_cost, old_cost);
+    // temperature of this proposal: one decay per earlier non-skipped proposal of the round
+    const unsigned live_mask = __ballot_sync(0xffffffffu, slot == 0 && !skip);
+    float t_i = temp;
+    if (!greedy_only) {
+      const int before = __popc(live_mask & ((1u << leader) - 1u));
+      for (int q = 0; q < before; ++q) t_i = __fmul_rn(t_i, decay);
+    }
+    bool acc = false;
+    if (!skip) {
+      if (greedy_only) acc = delta < 0.0f;
+      else acc = delta < 0.0f || u < exp_spec(__fdiv_rn(-delta, t_i));
+    }
+    // ---- commit in order, up to the first proposal that reads an earlier accepted swap --------
+    const unsigned acc_mask = __ballot_sync(0xffffffffu, slot == 0 && acc);
+    bool conflict = false;
+#pragma unroll
+    for (int h = 0; h < kGroups - 1; ++h) {
+      const int hx1 = __shfl_sync(0xffffffffu, x1, h * 8), hy1 = __shfl_sync(0xffffffffu, y1, h * 8);
+      const int hx2 = __shfl_sync(0xffffffffu, x2, h * 8), hy2 = __shfl_sync(0xffffffffu, y2, h * 8);
+      if (h < grp && ((acc_mask >> (h * 8)) & 1u)) {
+        const bool near = abs(hx1 - x1) + abs(hy1 - y1) <= 1 || abs(hx1 - x2) + abs(hy1 - y2) <= 1 ||
+                          abs(hx2 - x1) + abs(hy2 - y1) <= 1 || abs(hx2 - x2) + abs(hy2 - y2) <= 1;
+        conflict = conflict || near;
+      }
+    }
+    const unsigned cmask = __ballot_sync(0xffffffffu, slot == 0 && live && !skip && conflict);
+    const int gc = cmask ? ((__ffs(cmask) - 1) >> 3) : kGroups;  // >= 1: group 0 never conflicts
+    const long long remaining = iters - it;
+    const int ncommit = (int)min((long long)gc, remaining);
+    for (int h = 0; h < ncommit; ++h) {
+      const float dh = __shfl_sync(0xffffffffu, delta, h * 8);
+      if (!((live_mask >> (h * 8)) & 1u)) continue;  // skipped: no cooling
+      if ((acc_mask >> (h * 8)) & 1u) {
+        current = __fadd_rn(current, dh);
+        ++accepted;
+        if (current < best) {
+          best = current;
+          ++improved;
         }
       }
-      float old_cost = 0.0f, new_cost = 0.0f;
-#pragma unroll
-      for (int s = 0; s < 9; ++s) {
-        old_cost = __fadd_rn(old_cost, __shfl_sync(0xffffffffu, o, s));
-        new_cost = __fadd_rn(new_cost, __shfl_sync(0xffffffffu, nw, s));
-      }
-      delta = __fsub_rn(new_cost, old_cost);
+      if (!greedy_only) temp = __fmul_rn(temp, decay);
+      ++cooled;
     }
-    bool accept;
-    if (greedy_only) accept = delta < 0.0f;
-    else accept = delta < 0.0f || u < exp_spec(__fdiv_rn(-delta, temp));
-    if (accept) {
-      if (lane == 0) {
-        s_grid[p1] = g2;
-        s_grid[p2] = g1;
-      }
-      current = __fadd_rn(current, delta);
-      ++accepted;
-      if (current < best) {
-        best = current;
-        ++improved;
-      }
+    if (slot == 0 && grp < ncommit && acc) {
+      s_grid[p1] = g2;
+      s_grid[p2] = g1;
     }
+    it += ncommit;
     __syncwarp();
-    if (!greedy_only) temp = __fmul_rn(temp, decay);
-    ++cooled;
   }
   int32_t* out = J.chain_grids + (size_t)chain * n;
   for (int i = lane; i < n; i += 32) {
@@ -302,7 +366,7 @@ int launch_anneal(const float4* pal, int p, const AnnealJob* jobs_dev, const int
                   const int* chain_id_dev, int total_chains, int max_cells, cudaStream_t stream) {
   if (total_chains <= 0) return MG_OK;
   if (p >= 65535) return fail(MG_ERR_ARG, "annealing supports palettes below 65535 materials");
-  const size_t grid_bytes = ((size_t)max_cells * 2 + 15) & ~(size_t)15;
+  const size_t grid_bytes = kRing * sizeof(int4) + (((size_t)max_cells * 2 + 15) & ~(size_t)15);
   const size_t lab_bytes = (size_t)p * sizeof(float4);
   const size_t kMaxSmem = 200 * 1024;
   if (grid_bytes > kMaxSmem) return fail(MG_ERR_ARG, "grid too large for the annealer (max 102400 cells)");

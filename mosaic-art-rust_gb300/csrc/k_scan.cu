@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(kThreads) nearest_kernel(const float4* __restr
                                                            float* __restrict__ out_dist, uint32_t* __restrict__ err) {
   extern __shared__ __align__(128) uint8_t smem[];
   float4* stage0 = reinterpret_cast<float4*>(smem);
-  float4* stages[2] = {stage0, stage0 + kChunk};
+
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * kChunk * sizeof(float4));
   WarpLists* lists = reinterpret_cast<WarpLists*>(smem + 2 * kChunk * sizeof(float4) + 16);
 
@@ -106,11 +106,11 @@ __global__ void __launch_bounds__(kThreads) nearest_kernel(const float4* __restr
   const int my_groups = blockIdx.x < ngroups ? (ngroups - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   const long long total_seq = (long long)my_groups * nchunks;
 
-  auto chunk_len = [&](int c) { return min(kChunk, p - c * kChunk); };
-  auto issue = [&](int s, int c) {
+  auto chunk_len = [=](int c) { return min(kChunk, p - c * kChunk); };
+  auto issue = [=](int s, int c) {
     const uint32_t bytes = (uint32_t)chunk_len(c) * sizeof(float4);
     mbar_arrive_expect_tx(&bars[s], bytes);
-    tma_load_1d(stages[s], pal + (size_t)c * kChunk, bytes, &bars[s]);
+    tma_load_1d(stage0 + s * kChunk, pal + (size_t)c * kChunk, bytes, &bars[s]);
   };
 
   if (threadIdx.x == 0) {
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(kThreads) nearest_kernel(const float4* __restr
       if (total_seq > 1) issue(1, 1 % nchunks);
     }
   }
-  uint32_t parity[2] = {0, 0};
+  uint32_t parity = 0u;  // bit s: phase parity of stage s
   if (resident && total_seq > 0) {
     for (int c = 0; c < nchunks; ++c) {
       if (!mbar_wait_bounded(&bars[c], 0)) {
@@ -149,13 +149,13 @@ __global__ void __launch_bounds__(kThreads) nearest_kernel(const float4* __restr
     for (int c = 0; c < nchunks; ++c, ++seq) {
       const int s = resident ? c : (int)(seq & 1);
       if (!resident) {
-        if (!mbar_wait_bounded(&bars[s], parity[s])) {
+        if (!mbar_wait_bounded(&bars[s], (parity >> s) & 1u)) {
           atomicOr(err, kErrTimeout);
           return;
         }
-        parity[s] ^= 1u;
+        parity ^= 1u << s;
       }
-      const float4* sp = stages[s];
+      const float4* sp = stage0 + s * kChunk;
       const int n = chunk_len(c);
       const int gbase = c * kChunk;
       if (active) {
@@ -186,6 +186,7 @@ __global__ void __launch_bounds__(kThreads) nearest_kernel(const float4* __restr
         }
       }
       if (!resident) {
+        fence_proxy_async_smem();
         __syncthreads();  // every warp is done with stage s
         if (threadIdx.x == 0 && seq + 2 < total_seq) issue(s, (int)((seq + 2) % nchunks));
       }

@@ -90,8 +90,10 @@ struct GreedyJob {
   int* n_resets;             // 1 int
   float* total_cost;         // 1 float: calculate_total_cost of the placed grid
 };
-int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_jobs, uint32_t* usage_scratch,
-                  int smem_usage, cudaStream_t stream);
+// Candidate arrays must hold ceil(N/16)*16 rows (the walk streams 16 rows per copy).
+int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_jobs, int k, int max_gw,
+                  uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream);
+inline size_t padded_cells(int n) { return ((size_t)n + 15) / 16 * 16; }
 
 // (e) annealing chains.
 struct ChainResult {
