@@ -73,7 +73,11 @@ struct mg_plan {
   // device buffers
   DevBuf target, mats, regions, thumb_regions, thumbs, pal_lab, thumb_rgb, sim, cell_lab, cell_rgb, cand_idx,
       cand_dist, grid_greedy, resets, init_cost, greedy_job, chain_grids, chain_res, anneal_job, final_grid,
-      finals_ptr, best_chain, adj, out, sums, err, usage;
+      finals_ptr, best_chain, adj, out, sums, err, usage, gather_src;
+  // Where the kernels read the target (a device copy, or pinned host memory in place).
+  bool zero_copy = false;
+  const uint8_t* target_ptr = nullptr;
+  int64_t target_stride = 0;
   cudaEvent_t ev[8] = {};
   bool events = false;
   int launches = 0;
@@ -120,6 +124,17 @@ int ensure_err(mg_ctx* ctx) {
     MG_CUDA(cudaMemsetAsync(ctx->err.p, 0, 16, ctx->stream));
   }
   return MG_OK;
+}
+
+// Device address of caller memory that kernels may read in place: pinned,
+// mapped host memory (reached over the CPU-GPU link).  nullptr otherwise.
+const void* device_view(const void* p) {
+  cudaPointerAttributes a;
+  if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
 bool valid_image(const void* p, int w, int h, int64_t stride) {
@@ -667,7 +682,7 @@ void plan_release(mg_plan* pl) {
   for (DevBuf* b : {&pl->target, &pl->mats, &pl->regions, &pl->thumb_regions, &pl->thumbs, &pl->pal_lab,
                     &pl->thumb_rgb, &pl->sim, &pl->cell_lab, &pl->cell_rgb, &pl->cand_idx, &pl->cand_dist,
                     &pl->grid_greedy, &pl->resets, &pl->init_cost, &pl->greedy_job, &pl->chain_grids, &pl->chain_res,
-                    &pl->anneal_job, &pl->final_grid, &pl->finals_ptr, &pl->best_chain, &pl->adj, &pl->out, &pl->sums, &pl->usage,
+                    &pl->anneal_job, &pl->final_grid, &pl->finals_ptr, &pl->best_chain, &pl->adj, &pl->out, &pl->sums, &pl->usage, &pl->gather_src,
                     &pl->err})
     b->release();
   if (pl->events)
@@ -676,7 +691,7 @@ void plan_release(mg_plan* pl) {
 }
 
 // Validate the request, select the palette and upload the inputs.
-int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r) {
+int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r, bool zero_copy) {
   if (!r) return fail(MG_ERR_ARG, "null request");
   if (!valid_image(r->target, r->target_w, r->target_h, r->target_stride ? r->target_stride : 3ll * r->target_w))
     return fail(MG_ERR_ARG, "invalid target image");
@@ -689,6 +704,7 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r) {
   if (r->enable_optimization && (r->chains < 1 || r->optimization_iterations < 0))
     return fail(MG_ERR_ARG, "need chains >= 1 and iterations >= 0");
   pl->ctx = ctx;
+  pl->zero_copy = zero_copy;
   pl->W = r->target_w;
   pl->H = r->target_h;
   pl->gw = r->grid_w;
@@ -722,28 +738,49 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r) {
   pl->run_sa = pl->enable_opt && pl->weight > 0.0f && P > 0;  // main.rs:608
   if (pl->run_sa && (size_t)pl->N * 2 > 200 * 1024) return fail(MG_ERR_ARG, "grid too large for the annealer");
   cudaStream_t s = ctx->stream;
-  // target, packed rows
+  // Inputs in pinned host memory are read by the kernels in place over the
+  // CPU-GPU link when the plan allows it (mg_generate); otherwise (and for
+  // mg_plan_create, whose point is device-resident inputs) they are copied.
+  // Regions carry absolute device addresses, so both kinds mix freely.
+  // target
   const size_t trow = 3ull * pl->W;
-  MG_CHECK(pl->target.ensure(trow * pl->H));
-  MG_CUDA(cudaMemcpy2DAsync(pl->target.p, trow, r->target, r->target_stride ? r->target_stride : trow, trow, pl->H,
-                            cudaMemcpyHostToDevice, s));
-  // selected materials, packed with 16-byte aligned starts
-  pl->h_regions.resize(std::max(P, 1));
-  int64_t off = 0;
-  for (int i = 0; i < P; ++i) {
-    const int m = pl->selected[i];
-    pl->h_regions[i] = Region{off, r->material_w[m], r->material_h[m], 3ll * r->material_w[m]};
-    off += 3ll * r->material_w[m] * r->material_h[m];
-    off = (off + 15) & ~15ll;
+  const int64_t tstride = r->target_stride ? r->target_stride : (int64_t)trow;
+  const void* tdev = pl->zero_copy ? device_view(r->target) : nullptr;
+  if (tdev) {
+    pl->target_ptr = static_cast<const uint8_t*>(tdev);
+    pl->target_stride = tstride;
+  } else {
+    MG_CHECK(pl->target.ensure(trow * pl->H));
+    MG_CUDA(cudaMemcpy2DAsync(pl->target.p, trow, r->target, tstride, trow, pl->H, cudaMemcpyHostToDevice, s));
+    pl->target_ptr = pl->target.as<uint8_t>();
+    pl->target_stride = (int64_t)trow;
   }
-  MG_CHECK(pl->mats.ensure((size_t)off));
+  // selected materials
+  pl->h_regions.resize(std::max(P, 1));
+  std::vector<const void*> mdev(std::max(P, 1), nullptr);
+  int64_t off = 0;
   for (int i = 0; i < P; ++i) {
     const int m = pl->selected[i];
     const int64_t st = r->material_stride ? r->material_stride[m] : 3ll * r->material_w[m];
     if (!valid_image(r->materials[m], r->material_w[m], r->material_h[m], st))
       return fail(MG_ERR_ARG, "invalid material " + std::to_string(m));
+    mdev[i] = pl->zero_copy ? device_view(r->materials[m]) : nullptr;
+    if (mdev[i]) {
+      pl->h_regions[i] = Region{(int64_t)(uintptr_t)mdev[i], r->material_w[m], r->material_h[m], st};
+    } else {
+      pl->h_regions[i] = Region{off, r->material_w[m], r->material_h[m], 3ll * r->material_w[m]};
+      off += 3ll * r->material_w[m] * r->material_h[m];
+      off = (off + 15) & ~15ll;
+    }
+  }
+  if (off > 0) MG_CHECK(pl->mats.ensure((size_t)off));
+  for (int i = 0; i < P; ++i) {
+    if (mdev[i]) continue;
+    const int m = pl->selected[i];
+    const int64_t st = r->material_stride ? r->material_stride[m] : 3ll * r->material_w[m];
     MG_CUDA(cudaMemcpy2DAsync(pl->mats.as<uint8_t>() + pl->h_regions[i].offset, 3ull * r->material_w[m],
                               r->materials[m], st, 3ull * r->material_w[m], r->material_h[m], cudaMemcpyHostToDevice, s));
+    pl->h_regions[i].offset += (int64_t)(uintptr_t)pl->mats.p;
   }
   MG_CHECK(pl->regions.ensure(sizeof(Region) * std::max(P, 1)));
   MG_CUDA(cudaMemcpyAsync(pl->regions.p, pl->h_regions.data(), sizeof(Region) * std::max(P, 1), cudaMemcpyHostToDevice, s));
@@ -752,13 +789,24 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r) {
   MG_CHECK(pl->thumbs.ensure(tb * std::max(P, 1)));
   pl->device_thumbs = r->thumbnails == nullptr;
   if (!pl->device_thumbs) {
-    int i = 0;
-    while (i < P) {  // merge runs of consecutive selected materials into one copy
-      int j = i + 1;
-      while (j < P && pl->selected[j] == pl->selected[j - 1] + 1) ++j;
-      MG_CUDA(cudaMemcpyAsync(pl->thumbs.as<uint8_t>() + tb * i, r->thumbnails + tb * pl->selected[i], tb * (j - i),
-                              cudaMemcpyHostToDevice, s));
-      i = j;
+    const void* thdev = pl->zero_copy && P > 0 ? device_view(r->thumbnails) : nullptr;
+    if (thdev) {
+      // One gather kernel pulls the selected thumbnails across the link.
+      std::vector<int64_t> src(P);
+      for (int i = 0; i < P; ++i) src[i] = (int64_t)(uintptr_t)thdev + (int64_t)(tb * pl->selected[i]);
+      MG_CHECK(pl->gather_src.ensure(sizeof(int64_t) * P));
+      MG_CUDA(cudaMemcpyAsync(pl->gather_src.p, src.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, s));
+      MG_CHECK(launch_gather(pl->gather_src.as<int64_t>(), P, tb, pl->thumbs.as<uint8_t>(), s));
+      MG_CUDA(cudaStreamSynchronize(s));  // `src` goes out of scope
+    } else {
+      int i = 0;
+      while (i < P) {  // merge runs of consecutive selected materials into one copy
+        int j = i + 1;
+        while (j < P && pl->selected[j] == pl->selected[j - 1] + 1) ++j;
+        MG_CUDA(cudaMemcpyAsync(pl->thumbs.as<uint8_t>() + tb * i, r->thumbnails + tb * pl->selected[i], tb * (j - i),
+                                cudaMemcpyHostToDevice, s));
+        i = j;
+      }
     }
   }
   std::vector<Region> tregs(std::max(P, 1));
@@ -830,11 +878,11 @@ int plan_run(mg_plan* pl) {
   // [0] palette ingestion: thumbnails (when not given), material Lab, thumbnail means
   if (P > 0) {
     if (pl->device_thumbs)
-      MG_CHECK(launch_thumbnails(pl->mats.as<uint8_t>(), pl->regions.as<Region>(), P, pl->tw, pl->th,
+      MG_CHECK(launch_thumbnails(nullptr, pl->regions.as<Region>(), P, pl->tw, pl->th,
                                  pl->thumbs.as<uint8_t>(), s));
     int64_t maxpx = 0;
     for (int i = 0; i < P; ++i) maxpx = std::max<int64_t>(maxpx, (int64_t)pl->h_regions[i].w * pl->h_regions[i].h);
-    MG_CHECK(launch_region_stats(pl->mats.as<uint8_t>(), nullptr, pl->regions.as<Region>(), P, maxpx,
+    MG_CHECK(launch_region_stats(nullptr, nullptr, pl->regions.as<Region>(), P, maxpx,
                                  pl->pal_lab.as<float4>(), nullptr, pl->sums.as<RegionSums>(), 1, s));
     if (pl->strength > 0.0f)
       MG_CHECK(launch_region_stats(pl->thumbs.as<uint8_t>(), nullptr, pl->thumb_regions.as<Region>(), P,
@@ -847,8 +895,8 @@ int plan_run(mg_plan* pl) {
     MG_CHECK(launch_similarity(pl->pal_lab.as<float4>(), P, 0, pl->sim.as<float>(), s));
   MG_CUDA(cudaEventRecord(pl->ev[2], s));
   // [2] cell Lab + cell mean RGB
-  CellGeom g{pl->gw, pl->gh, pl->cw, pl->ch, 3ll * pl->W};
-  MG_CHECK(launch_region_stats(pl->target.as<uint8_t>(), &g, nullptr, N, (int64_t)pl->cw * pl->ch,
+  CellGeom g{pl->gw, pl->gh, pl->cw, pl->ch, pl->target_stride};
+  MG_CHECK(launch_region_stats(pl->target_ptr, &g, nullptr, N, (int64_t)pl->cw * pl->ch,
                                pl->cell_lab.as<float4>(), pl->cell_rgb.as<uchar4>(), pl->sums.as<RegionSums>(), 1, s));
   MG_CUDA(cudaEventRecord(pl->ev[3], s));
   // [3] k nearest per cell
@@ -929,7 +977,7 @@ int mg_plan_create(mg_ctx* ctx, const mg_request* req, mg_plan** out) {
   if (!out) return fail(MG_ERR_ARG, "null out");
   *out = nullptr;
   mg_plan* pl = new mg_plan();
-  int s = plan_setup(pl, ctx, req);
+  int s = plan_setup(pl, ctx, req, false);
   if (s != MG_OK) {
     std::string msg = g_error;
     plan_release(pl);
@@ -984,7 +1032,7 @@ int mg_generate(mg_ctx* ctx, const mg_request* req, mg_result* res) {
   MG_CHECK(check_ctx(ctx));
   if (!res) return fail(MG_ERR_ARG, "null result");
   if (!ctx->gen_plan) ctx->gen_plan = new mg_plan();
-  MG_CHECK(plan_setup(ctx->gen_plan, ctx, req));
+  MG_CHECK(plan_setup(ctx->gen_plan, ctx, req, true));
   MG_CHECK(plan_run(ctx->gen_plan));
   return plan_read(ctx->gen_plan, res);
 }

@@ -305,4 +305,28 @@ int launch_thumbnails(const uint8_t* base, const Region* regions, int n, int tw,
   return MG_OK;
 }
 
+namespace {
+// One CTA per item; 16-byte vector copies when source, destination and size allow.
+__global__ void __launch_bounds__(256) gather_kernel(const int64_t* __restrict__ src, size_t bytes,
+                                                     uint8_t* __restrict__ dst) {
+  const uint8_t* s = reinterpret_cast<const uint8_t*>((uintptr_t)src[blockIdx.x]);
+  uint8_t* d = dst + (size_t)blockIdx.x * bytes;
+  if ((((uintptr_t)s | (uintptr_t)d | bytes) & 15) == 0) {
+    const uint4* s4 = reinterpret_cast<const uint4*>(s);
+    uint4* d4 = reinterpret_cast<uint4*>(d);
+    for (size_t i = threadIdx.x; i < bytes / 16; i += blockDim.x) d4[i] = s4[i];
+  } else {
+    for (size_t i = threadIdx.x; i < bytes; i += blockDim.x) d[i] = s[i];
+  }
+}
+}  // namespace
+
+int launch_gather(const int64_t* src, int n, size_t bytes, uint8_t* dst, cudaStream_t stream) {
+  if (n <= 0 || bytes == 0) return MG_OK;
+  gather_kernel<<<n, 256, 0, stream>>>(src, bytes, dst);
+  g_launches += 1;
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
 }  // namespace mg

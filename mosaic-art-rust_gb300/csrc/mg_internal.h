@@ -68,6 +68,10 @@ int launch_region_stats(const uint8_t* base, const CellGeom* geom, const Region*
                         int want_lab, cudaStream_t stream);
 void upload_lab_consts(cudaStream_t stream);
 
+// Copy n items of `bytes` each from device-readable addresses src[i] to
+// dst + i*bytes (16-byte vector copies when aligned).
+int launch_gather(const int64_t* src, int n, size_t bytes, uint8_t* dst, cudaStream_t stream);
+
 // Area-average thumbnails of regions at tw x th.
 int launch_thumbnails(const uint8_t* base, const Region* regions, int n, int tw, int th, uint8_t* out,
                       cudaStream_t stream);

@@ -69,6 +69,19 @@ def test_generate_edge_cases(ctx, orc):
                               grid_w=11, grid_h=9, tile_w=0, tile_h=0, max_usage=1, iterations=300, chains=3))
 
 
+def test_pinned_inputs_read_in_place(ctx, orc):
+    """Inputs in pinned host memory are read by the kernels over the CPU-GPU link (no staging copies)."""
+    from mosaic_gpu import _capi, job
+
+    cfg = _small("recommended", target_w=480, target_h=360, n_materials=150, material_side=64, grid_w=20, grid_h=15,
+                 tile_w=12, tile_h=12, iterations=500, chains=6)
+    inp = job.make_inputs(cfg, allocator=_capi.load().mg_host_alloc)
+    res, grid, image = job.generate(ctx, job.RequestHolder(inp))
+    ref = orc.generate(inp, threads=8)
+    assert np.array_equal(grid, ref["grid"]) and np.array_equal(image, ref["image"])
+    assert np.float32(res.final_cost) == np.float32(ref["final_cost"])
+
+
 def test_device_thumbnails_equal_host_thumbnails(ctx, orc):
     from mosaic_gpu import job
 
