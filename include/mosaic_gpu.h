@@ -239,6 +239,75 @@ int mg_plan_stage_ms(mg_plan* plan, float* ms, int cap);
 /* Number of kernels one mg_plan_run launches. */
 int mg_plan_launches(mg_plan* plan);
 
+/* ---- resident palettes and batches of mosaics ---------------------------------------
+ * No single reference function: the reference builds its palette once per
+ * process (MosaicGenerator::new, main.rs:105-164) and then generates one
+ * mosaic (main.rs:477-685).  Here the palette stays in device memory and many
+ * mosaics of uneven size run through one batched pipeline whose sequential
+ * stages (greedy walk, annealing chains) are work items of one persistent
+ * launch; results equal mg_generate's for each mosaic bit for bit. */
+typedef struct mg_palette mg_palette;
+typedef struct mg_batch mg_batch;
+
+typedef struct mg_palette_desc {
+  int n_materials;
+  const uint8_t* const* materials;
+  const int* material_w;
+  const int* material_h;
+  const int64_t* material_stride;  /* nullable -> 3*w */
+  const uint8_t* thumbnails;       /* nullable: n x tile_h x tile_w x 3; NULL -> area-average resize */
+  int tile_w, tile_h;              /* output tile size of every mosaic using the palette (> 0) */
+  float target_aspect;             /* load_tiles selection (main.rs:166-261) for this target aspect */
+  float aspect_tolerance;
+  int max_materials;
+  int build_similarity;            /* 1: keep the P x P similarity database resident */
+} mg_palette_desc;
+
+typedef struct mg_mosaic {         /* one request: a target and the generate_mosaic settings */
+  const uint8_t* target;           /* host (pinned or pageable) or device memory */
+  int target_w, target_h;
+  int64_t target_stride;           /* 0 -> 3*target_w */
+  int grid_w, grid_h;
+  int max_usage_per_image;
+  float adjacency_penalty_weight;
+  float color_adjustment_strength;
+  int enable_optimization;
+  int64_t optimization_iterations;
+  float initial_temperature, temperature_decay;
+  int chains;
+  uint64_t seed;
+  uint32_t stream;
+} mg_mosaic;
+
+void mg_palette_desc_default(mg_palette_desc* desc);
+int mg_palette_create(mg_ctx* ctx, const mg_palette_desc* desc, mg_palette** out);
+int mg_palette_size(const mg_palette* pal);
+int64_t mg_palette_device_bytes(const mg_palette* pal);
+/* similarity.rs:105-109 get_lab_color for every tile: P x 3 floats. */
+int mg_palette_read_lab(mg_palette* pal, float* lab_out);
+/* The resident similarity database (similarity.rs:69-103), P x P floats. */
+int mg_palette_read_similarity(mg_palette* pal, float* out);
+int mg_palette_destroy(mg_palette* pal);
+
+void mg_mosaic_default(mg_mosaic* m);
+/* A batch with its inputs copied to device memory; the first mg_batch_run
+ * autotunes launch shapes, later runs replay one CUDA graph. */
+int mg_batch_create(mg_ctx* ctx, mg_palette* pal, const mg_mosaic* mosaics, int n, mg_batch** out);
+int mg_batch_run(mg_batch* batch);
+/* Mosaic i's grid (original material indices), image (grid_h*tile_h x
+ * grid_w*tile_w x 3) and annealing summary. */
+int mg_batch_read(mg_batch* batch, int i, mg_result* res);
+/* [0] cell statistics, [1] k-nearest, [2] walks + chains, [3] adjust +
+ * composite, [4] total; ms of the last run. */
+int mg_batch_stage_ms(mg_batch* batch, float* ms, int cap);
+/* The launch shapes the autotuner picked. */
+int mg_batch_tuning(mg_batch* batch, int* cells_per_cta, int* nearest_chunk, int* workers_per_cta);
+int mg_batch_launches(mg_batch* batch);
+int mg_batch_destroy(mg_batch* batch);
+/* One batch from host buffers to host buffers (targets in pinned host memory
+ * are read in place). */
+int mg_generate_batch(mg_ctx* ctx, mg_palette* pal, const mg_mosaic* mosaics, int n, mg_result* results);
+
 #ifdef __cplusplus
 }
 #endif

@@ -8,7 +8,7 @@
 #include <string>
 #include <vector>
 
-#include "mg_internal.h"
+#include "capi_internal.h"
 
 namespace mg {
 
@@ -52,15 +52,10 @@ void DevBuf::release() {
 
 using namespace mg;
 
-struct mg_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  DevBuf in0, in1, in2, out0, out1, out2, sums, regions, err;
-  mg_plan* gen_plan = nullptr;
-};
 
 struct mg_plan {
   mg_ctx* ctx = nullptr;
+  int device = 0;  // destroy must not touch ctx, which may already be gone
   // geometry and configuration
   int W = 0, H = 0, gw = 0, gh = 0, cw = 0, ch = 0, tw = 0, th = 0, N = 0, P = 0, K = 0, k = 0;
   int64_t iters = 0;
@@ -84,7 +79,7 @@ struct mg_plan {
   bool ran = false;
 };
 
-namespace {
+namespace mg {
 
 int check_ctx(mg_ctx* ctx) {
   if (!ctx) return fail(MG_ERR_ARG, "null context");
@@ -137,11 +132,31 @@ const void* device_view(const void* p) {
   return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
+const void* device_view_or_device(const void* p) {
+  cudaPointerAttributes a;
+  if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+    return a.devicePointer;
+  return nullptr;
+}
+
 bool valid_image(const void* p, int w, int h, int64_t stride) {
   return p && w > 0 && h > 0 && stride >= 3ll * w;
 }
 
-}  // namespace
+const LabConsts* device_lab_consts(mg_ctx* ctx) {
+  if (!ctx->lab_consts.p) {
+    if (ctx->lab_consts.ensure(sizeof(LabConsts)) != MG_OK) return nullptr;
+    if (cudaMemcpy(ctx->lab_consts.p, &host_lab_consts(), sizeof(LabConsts), cudaMemcpyHostToDevice) != cudaSuccess)
+      return nullptr;
+  }
+  return ctx->lab_consts.as<LabConsts>();
+}
+
+}  // namespace mg
 
 extern "C" {
 
@@ -187,7 +202,7 @@ int mg_ctx_destroy(mg_ctx* ctx) {
   if (ctx->gen_plan) mg_plan_destroy(ctx->gen_plan);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->in0, &ctx->in1, &ctx->in2, &ctx->out0, &ctx->out1, &ctx->out2, &ctx->sums, &ctx->regions,
-                    &ctx->err})
+                    &ctx->err, &ctx->lab_consts})
     b->release();
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -704,6 +719,7 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r, bool zero_copy) {
   if (r->enable_optimization && (r->chains < 1 || r->optimization_iterations < 0))
     return fail(MG_ERR_ARG, "need chains >= 1 and iterations >= 0");
   pl->ctx = ctx;
+  pl->device = ctx->device;
   pl->zero_copy = zero_copy;
   pl->W = r->target_w;
   pl->H = r->target_h;
@@ -1003,10 +1019,8 @@ int mg_plan_read(mg_plan* pl, mg_result* res) {
 
 int mg_plan_destroy(mg_plan* pl) {
   if (!pl) return MG_OK;
-  if (pl->ctx) {
-    cudaSetDevice(pl->ctx->device);
-    cudaStreamSynchronize(pl->ctx->stream);
-  }
+  cudaSetDevice(pl->device);
+  cudaDeviceSynchronize();
   plan_release(pl);
   delete pl;
   return MG_OK;

@@ -1,0 +1,29 @@
+// capi_internal.h -- the context object and host helpers shared by the C ABI
+// translation units (capi.cu, capi_batch.cu).
+#pragma once
+#include <vector>
+
+#include "mg_internal.h"
+
+struct mg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  mg::DevBuf in0, in1, in2, out0, out1, out2, sums, regions, err, lab_consts;
+  mg_plan* gen_plan = nullptr;
+};
+
+namespace mg {
+int check_ctx(mg_ctx* ctx);
+std::vector<float4> to_f4(const float* lab3, int n);
+int upload(mg_ctx* ctx, DevBuf& b, const void* src, size_t bytes);
+int finish(mg_ctx* ctx);
+int ensure_err(mg_ctx* ctx);
+// Device address of caller memory that kernels may read in place: pinned,
+// mapped host memory (reached over the CPU-GPU link).  nullptr otherwise.
+const void* device_view(const void* p);
+// Like device_view, and also device memory itself.
+const void* device_view_or_device(const void* p);
+bool valid_image(const void* p, int w, int h, int64_t stride);
+// Device copy of the Lab conversion constants (for kernels outside k_lab.cu).
+const LabConsts* device_lab_consts(mg_ctx* ctx);
+}  // namespace mg

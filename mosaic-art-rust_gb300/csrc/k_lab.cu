@@ -207,6 +207,11 @@ __global__ void thumbnail_kernel(const uint8_t* __restrict__ base, const Region*
 
 }  // namespace
 
+const LabConsts& host_lab_consts() {
+  static HostLabConsts h;
+  return h.c;
+}
+
 void upload_lab_consts(cudaStream_t stream) {
   static HostLabConsts h;
   cudaMemcpyToSymbolAsync(c_lab, &h.c, sizeof(LabConsts), 0, cudaMemcpyHostToDevice, stream);

@@ -21,7 +21,6 @@ namespace {
 
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
-constexpr int kChunk = 2048;   // palette entries per shared-memory stage (32 KB)
 constexpr int kListCap = 128;  // k <= 100
 constexpr int kBufCap = 128;   // candidate buffer; merged when it could overflow
 constexpr unsigned long long kMaxKey = ~0ull;
@@ -32,7 +31,8 @@ struct WarpLists {
   unsigned long long buf[kBufCap];
 };
 
-constexpr size_t kSmemBytes = 2 * kChunk * sizeof(float4) + 16 + kWarps * sizeof(WarpLists);
+template <int kChunk>
+constexpr size_t smem_bytes() { return 2 * kChunk * sizeof(float4) + 16 + kWarps * sizeof(WarpLists); }
 
 __device__ __forceinline__ int lower_bound_u64(const unsigned long long* a, int n, unsigned long long key) {
   int lo = 0, hi = n;
@@ -89,6 +89,7 @@ __device__ void warp_merge(WarpLists& W, int& len, int& nbuf, unsigned long long
   thr = (len == k) ? W.list[k - 1] : kMaxKey;
 }
 
+template <int kChunk>  // palette entries per shared-memory stage
 __global__ void __launch_bounds__(kThreads) nearest_kernel(const float4* __restrict__ pal, int p,
                                                            const float4* __restrict__ queries, int nq, int k,
                                                            int out_stride, uint32_t* __restrict__ out_idx,
@@ -204,10 +205,34 @@ __global__ void __launch_bounds__(kThreads) nearest_kernel(const float4* __restr
   }
 }
 
+template <int kChunk>
+int launch_nearest_t(const float4* pal, int p, const float4* queries, int nq, int keff, int k, uint32_t* idx, float* dist,
+                     uint32_t* err, cudaStream_t stream) {
+  constexpr size_t kSmem = smem_bytes<kChunk>();
+  static int configured_device = -1;
+  int dev = 0;
+  MG_CUDA(cudaGetDevice(&dev));
+  if (configured_device != dev) {
+    MG_CUDA(cudaFuncSetAttribute(nearest_kernel<kChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem));
+    configured_device = dev;
+  }
+  int sms = 0, per_sm = 0;
+  MG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nearest_kernel<kChunk>, kThreads, kSmem));
+  if (per_sm < 1) per_sm = 1;
+  const int ngroups = (nq + kWarps - 1) / kWarps;
+  const int grid = min(ngroups, sms * per_sm);
+  // Rows shorter than k (p < k) are padded by the kernel with index ~0 / +inf.
+  nearest_kernel<kChunk><<<grid, kThreads, kSmem, stream>>>(pal, p, queries, nq, keff, k, idx, dist, err);
+  g_launches += 1;
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
 }  // namespace
 
 int launch_nearest(const float4* pal, int p, const float4* queries, int nq, int k, uint32_t* idx, float* dist,
-                   uint32_t* err, cudaStream_t stream) {
+                   uint32_t* err, cudaStream_t stream, int chunk) {
   if (nq <= 0) return MG_OK;
   if (k <= 0 || k > 100) return fail(MG_ERR_ARG, "k must be in 1..100");
   const int keff = min(k, p);
@@ -215,24 +240,8 @@ int launch_nearest(const float4* pal, int p, const float4* queries, int nq, int 
     MG_CUDA(cudaMemsetAsync(idx, 0xFF, sizeof(uint32_t) * (size_t)nq * k, stream));
     return MG_OK;
   }
-  static int configured_device = -1;
-  int dev = 0;
-  MG_CUDA(cudaGetDevice(&dev));
-  if (configured_device != dev) {
-    MG_CUDA(cudaFuncSetAttribute(nearest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
-    configured_device = dev;
-  }
-  int sms = 0, per_sm = 0;
-  MG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nearest_kernel, kThreads, kSmemBytes));
-  if (per_sm < 1) per_sm = 1;
-  const int ngroups = (nq + kWarps - 1) / kWarps;
-  const int grid = min(ngroups, sms * per_sm);
-  // Rows shorter than k (p < k) are padded by the kernel with index ~0 / +inf.
-  nearest_kernel<<<grid, kThreads, kSmemBytes, stream>>>(pal, p, queries, nq, keff, k, idx, dist, err);
-  g_launches += 1;
-  MG_CUDA(cudaGetLastError());
-  return MG_OK;
+  if (chunk == 4096) return launch_nearest_t<4096>(pal, p, queries, nq, keff, k, idx, dist, err, stream);
+  return launch_nearest_t<2048>(pal, p, queries, nq, keff, k, idx, dist, err, stream);
 }
 
 }  // namespace mg

@@ -77,8 +77,9 @@ int launch_thumbnails(const uint8_t* base, const Region* regions, int n, int tw,
                       cudaStream_t stream);
 
 // (b) k nearest palette entries for every query (ties -> lowest index).
+// chunk: palette entries per shared-memory stage (2048 or 4096).
 int launch_nearest(const float4* pal, int p, const float4* queries, int nq, int k, uint32_t* idx,
-                   float* dist, uint32_t* err, cudaStream_t stream);
+                   float* dist, uint32_t* err, cudaStream_t stream, int chunk = 2048);
 
 // (c) similarity matrix, full (P x P) or strict upper triangle.
 int launch_similarity(const float4* pal, int p, int triangular, float* out, cudaStream_t stream);
@@ -124,6 +125,47 @@ int launch_swap_delta(const float4* pal, const int32_t* grid, int gw, int gh, co
                       cudaStream_t stream);
 int launch_penalty(const float4* pal, const int32_t* grid, int gw, int gh, float weight, const int4* cxy, int n,
                    float* out, cudaStream_t stream);
+
+// ---- batches of mosaics over one resident palette (k_batch.cu) --------------
+struct BatchMosaic {
+  const uint8_t* target;  // device-readable RGB8
+  int64_t stride;
+  int gw, gh, cw, ch, n, cell_base;  // cell_base: first of the mosaic's cells in the flat cell arrays (multiple of 16)
+  uint32_t max_usage;
+  float weight, strength;
+  int run_sa, chains;
+  long long iters;
+  float t0, decay;
+  uint32_t key0, key1, stream;
+  int32_t* grid;          // greedy grid (n)
+  int32_t* chain_grids;   // chains x n
+  ChainResult* results;   // chains
+  int32_t* final_grid;    // n
+  int* n_resets;
+  float* init_cost;
+  int* best_chain;
+  uint8_t* out;           // (gh*th) x (gw*tw) x 3
+};
+struct BatchQueue {
+  unsigned long long* items;  // capacity total
+  unsigned* ready;            // per slot: 1 once published
+  unsigned* head;             // next slot to take
+  unsigned* tail;             // next slot to publish
+  unsigned* chains_left;      // per mosaic
+  unsigned total;             // walks + chains of the batch
+  const uint32_t* cand_idx;
+  const float* cand_dist;
+};
+const LabConsts& host_lab_consts();
+int launch_fill_u32(unsigned* p, unsigned n, unsigned v, cudaStream_t stream);
+int launch_batch_cells(const BatchMosaic* mos, int nm, int total_cells, const LabConsts* consts, float4* lab,
+                       uchar4* rgb, int warps, cudaStream_t stream);
+size_t batch_worker_smem(int k, int max_gw, int max_cells, int p, bool lab_smem);
+int launch_batch_place(const float4* pal, int p, const BatchMosaic* mos, const BatchQueue& q, int k, int max_gw,
+                       int max_cells, int workers, uint32_t* err, cudaStream_t stream);
+int launch_batch_finish(const BatchMosaic* mos, int nm, int total_cells, const uchar4* thumb_rgb,
+                        const uchar4* cell_rgb, float4* adj, const uint8_t* thumbs, int tw, int th, int max_out_px,
+                        cudaStream_t stream);
 
 // (f) colour adjustment + composite.
 int launch_cell_adjust(const int32_t* grid, int n_cells, const uchar4* thumb_rgb, const uchar4* cell_rgb,

@@ -70,8 +70,40 @@ class Result(C.Structure):
                 ("accepted_count", C.c_int64), ("improved_count", C.c_int64)]
 
 
+class PaletteDesc(C.Structure):
+    _fields_ = [("n_materials", C.c_int), ("materials", C.POINTER(_u8p)), ("material_w", C.POINTER(C.c_int)),
+                ("material_h", C.POINTER(C.c_int)), ("material_stride", _i64p), ("thumbnails", _u8p),
+                ("tile_w", C.c_int), ("tile_h", C.c_int), ("target_aspect", C.c_float),
+                ("aspect_tolerance", C.c_float), ("max_materials", C.c_int), ("build_similarity", C.c_int)]
+
+
+class Mosaic(C.Structure):
+    _fields_ = [("target", C.c_void_p), ("target_w", C.c_int), ("target_h", C.c_int), ("target_stride", C.c_int64),
+                ("grid_w", C.c_int), ("grid_h", C.c_int), ("max_usage_per_image", C.c_int),
+                ("adjacency_penalty_weight", C.c_float), ("color_adjustment_strength", C.c_float),
+                ("enable_optimization", C.c_int), ("optimization_iterations", C.c_int64),
+                ("initial_temperature", C.c_float), ("temperature_decay", C.c_float), ("chains", C.c_int),
+                ("seed", C.c_uint64), ("stream", C.c_uint32)]
+
+
 # (name, restype, argtypes) for every exported symbol of mosaic_gpu.h.
 SIGNATURES = [
+    ("mg_palette_desc_default", None, [C.POINTER(PaletteDesc)]),
+    ("mg_palette_create", C.c_int, [C.c_void_p, C.POINTER(PaletteDesc), C.POINTER(C.c_void_p)]),
+    ("mg_palette_size", C.c_int, [C.c_void_p]),
+    ("mg_palette_device_bytes", C.c_int64, [C.c_void_p]),
+    ("mg_palette_read_lab", C.c_int, [C.c_void_p, _f32p]),
+    ("mg_palette_read_similarity", C.c_int, [C.c_void_p, _f32p]),
+    ("mg_palette_destroy", C.c_int, [C.c_void_p]),
+    ("mg_mosaic_default", None, [C.POINTER(Mosaic)]),
+    ("mg_batch_create", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Mosaic), C.c_int, C.POINTER(C.c_void_p)]),
+    ("mg_batch_run", C.c_int, [C.c_void_p]),
+    ("mg_batch_read", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    ("mg_batch_stage_ms", C.c_int, [C.c_void_p, _f32p, C.c_int]),
+    ("mg_batch_tuning", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("mg_batch_launches", C.c_int, [C.c_void_p]),
+    ("mg_batch_destroy", C.c_int, [C.c_void_p]),
+    ("mg_generate_batch", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Mosaic), C.c_int, C.c_void_p]),
     ("mg_version", C.c_int, []),
     ("mg_last_error", C.c_char_p, []),
     ("mg_kernel_launches", C.c_ulonglong, []),

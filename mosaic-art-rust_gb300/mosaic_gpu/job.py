@@ -182,3 +182,134 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+# ---- resident palettes and batches -------------------------------------------------------
+class Palette:
+    """A resident palette (mg_palette): selection, material Lab, thumbnails, similarity."""
+
+    def __init__(self, ctx: capi.Context, mats: synth.Materials, thumbs, tile_w: int, tile_h: int,
+                 target_aspect: float, aspect_tolerance: float = 0.1, max_materials: int = 0,
+                 build_similarity: bool = True):
+        self.ctx = ctx
+        n = len(mats)
+        self._ptrs = (capi._u8p * max(n, 1))(*[C.cast(mats.buf.ctypes.data + int(o), capi._u8p) for o in mats.off])
+        self._w = (C.c_int * max(n, 1))(*[int(v) for v in mats.w])
+        self._h = (C.c_int * max(n, 1))(*[int(v) for v in mats.h])
+        d = capi.PaletteDesc()
+        ctx.lib.mg_palette_desc_default(C.byref(d))
+        d.n_materials = n
+        d.materials, d.material_w, d.material_h = self._ptrs, self._w, self._h
+        d.material_stride = None
+        d.thumbnails = capi.ptr(thumbs, C.c_uint8) if thumbs is not None else None
+        d.tile_w, d.tile_h = tile_w, tile_h
+        d.target_aspect, d.aspect_tolerance = target_aspect, aspect_tolerance
+        d.max_materials = max_materials or n
+        d.build_similarity = 1 if build_similarity else 0
+        h = C.c_void_p()
+        capi.check(ctx.lib.mg_palette_create(ctx.h, C.byref(d), C.byref(h)))
+        self.h = h
+        self.tile = (tile_w, tile_h)
+
+    @property
+    def size(self) -> int:
+        return int(self.ctx.lib.mg_palette_size(self.h))
+
+    def lab(self):
+        out = np.zeros((max(self.size, 1), 3), np.float32)
+        capi.check(self.ctx.lib.mg_palette_read_lab(self.h, capi.ptr(out, C.c_float)))
+        return out[:self.size]
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.mg_palette_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mosaic_request(target: np.ndarray | int, w: int, h: int, gw: int, gh: int, *, max_usage=3, weight=0.25,
+                   strength=0.4, enable_opt=True, iterations=1000, chains=1, seed=20251203, stream=0,
+                   t0=100.0, decay=0.99995) -> capi.Mosaic:
+    m = capi.Mosaic()
+    capi.load().mg_mosaic_default(C.byref(m))
+    m.target = target if isinstance(target, int) else target.ctypes.data
+    m.target_w, m.target_h, m.target_stride = w, h, 3 * w
+    m.grid_w, m.grid_h = gw, gh
+    m.max_usage_per_image, m.adjacency_penalty_weight, m.color_adjustment_strength = max_usage, weight, strength
+    m.enable_optimization = 1 if enable_opt else 0
+    m.optimization_iterations, m.chains, m.seed, m.stream = iterations, chains, seed, stream
+    m.initial_temperature, m.temperature_decay = t0, decay
+    return m
+
+
+class Batch:
+    """A device-resident batch of mosaics over one palette (mg_batch)."""
+
+    def __init__(self, ctx: capi.Context, palette: Palette, mosaics: list):
+        self.ctx, self.palette = ctx, palette
+        self.n = len(mosaics)
+        self._arr = (capi.Mosaic * max(self.n, 1))(*mosaics)
+        self._meta = [(m.grid_w, m.grid_h) for m in mosaics]
+        h = C.c_void_p()
+        capi.check(ctx.lib.mg_batch_create(ctx.h, palette.h, self._arr, self.n, C.byref(h)))
+        self.h = h
+
+    def run(self):
+        capi.check(self.ctx.lib.mg_batch_run(self.h))
+
+    def read(self, i: int, want_image: bool = True):
+        gw, gh = self._meta[i]
+        tw, th = self.palette.tile
+        grid = np.zeros(gw * gh, np.int32)
+        image = np.zeros((gh * th, gw * tw, 3), np.uint8) if want_image else None
+        res = capi.Result()
+        res.grid = capi.ptr(grid, C.c_int32)
+        res.image = capi.ptr(image, C.c_uint8) if want_image else None
+        capi.check(self.ctx.lib.mg_batch_read(self.h, i, C.byref(res)))
+        return res, grid.reshape(gh, gw), image
+
+    def stage_ms(self):
+        ms = np.zeros(5, np.float32)
+        n = self.ctx.lib.mg_batch_stage_ms(self.h, capi.ptr(ms, C.c_float), 5)
+        return ms[:max(n, 0)]
+
+    def tuning(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        capi.check(self.ctx.lib.mg_batch_tuning(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"cells_per_cta": a.value, "nearest_chunk": b.value, "workers_per_cta": c.value}
+
+    def launches(self) -> int:
+        return int(self.ctx.lib.mg_batch_launches(self.h))
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.mg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def generate_batch(ctx: capi.Context, palette: Palette, mosaics: list):
+    n = len(mosaics)
+    arr = (capi.Mosaic * max(n, 1))(*mosaics)
+    tw, th = palette.tile
+    grids, images = [], []
+    results = (capi.Result * max(n, 1))()
+    for i, m in enumerate(mosaics):
+        g = np.zeros(m.grid_w * m.grid_h, np.int32)
+        im = np.zeros((m.grid_h * th, m.grid_w * tw, 3), np.uint8)
+        results[i].grid = capi.ptr(g, C.c_int32)
+        results[i].image = capi.ptr(im, C.c_uint8)
+        grids.append(g.reshape(m.grid_h, m.grid_w))
+        images.append(im)
+    capi.check(ctx.lib.mg_generate_batch(ctx.h, palette.h, arr, n, results))
+    return list(results)[:n], grids, images

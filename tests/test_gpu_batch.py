@@ -1,0 +1,119 @@
+"""Batches of uneven mosaics over one resident palette, against the one-mosaic path.
+
+Every mosaic of a batch must equal mg_generate of the same request bit for bit
+(grid, image, annealing summary) -- on the autotuning run, the graph-capturing
+run and graph replays -- and the one-shot mg_generate_batch must equal the
+resident batch.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TILE = 8
+
+
+def _palette_inputs():
+    from mosaic_gpu import synth
+
+    mats = synth.materials(160, 24, 0, seed=77, stream=2)
+    thumbs = synth.thumbnails(mats, TILE, TILE)
+    return mats, thumbs
+
+
+def _requests():
+    """(w, h, gw, gh, settings): uneven sizes, optimiser on/off, weight 0, usage 1."""
+    return [
+        (320, 240, 40, 30, dict(chains=4, iterations=1500)),
+        (96, 72, 12, 9, dict(chains=3, iterations=800, max_usage=1)),
+        (200, 150, 25, 18, dict(enable_opt=False)),
+        (160, 120, 20, 15, dict(weight=0.0, chains=2)),
+        (480, 360, 60, 45, dict(chains=5, iterations=3000, strength=0.0)),
+        (64, 48, 8, 6, dict(chains=2, iterations=300)),
+        (240, 180, 30, 22, dict(chains=6, iterations=2000, max_usage=2)),
+    ]
+
+
+def _targets():
+    from mosaic_gpu import synth
+
+    return [synth.target(w, h, 5, seed=1000 + i, stream=7) for i, (w, h, _, _, _) in enumerate(_requests())]
+
+
+def _single(ctx, mats, thumbs, tgt, w, h, gw, gh, kw, stream):
+    """The same request through mg_generate."""
+    from mosaic_gpu import job
+
+    cfg = job.JobConfig("b", w, h, 0, len(mats), 24, 0, gw, gh, kw.get("max_usage", 3), kw.get("weight", 0.25),
+                        kw.get("strength", 0.4), kw.get("iterations", 1000), kw.get("chains", 1), TILE, TILE,
+                        enable_optimization=kw.get("enable_opt", True), seed=20251203)
+    inp = job.Inputs(cfg, tgt, mats, thumbs)
+    holder = job.RequestHolder(inp, stream=stream)
+    return job.generate(ctx, holder)
+
+
+def test_batch_equals_single_mosaic_path(ctx):
+    from mosaic_gpu import job
+
+    mats, thumbs = _palette_inputs()
+    pal = job.Palette(ctx, mats, thumbs, TILE, TILE, target_aspect=4 / 3)
+    assert pal.size == len(mats)
+    tgts = _targets()
+    reqs = [job.mosaic_request(t, w, h, gw, gh, stream=i, **kw)
+            for i, (t, (w, h, gw, gh, kw)) in enumerate(zip(tgts, _requests()))]
+    batch = job.Batch(ctx, pal, reqs)
+    singles = [_single(ctx, mats, thumbs, t, w, h, gw, gh, kw, i)
+               for i, (t, (w, h, gw, gh, kw)) in enumerate(zip(tgts, _requests()))]
+    for run in range(3):  # tuning run, graph capture, graph replay
+        batch.run()
+        for i, (res, grid, image) in enumerate(singles):
+            r, g, im = batch.read(i)
+            assert np.array_equal(g, grid), (run, i)
+            assert np.array_equal(im, image), (run, i)
+            assert r.best_chain == res.best_chain and np.float32(r.final_cost) == np.float32(res.final_cost)
+            assert r.n_resets == res.n_resets and r.palette_size == res.palette_size
+    tune = batch.tuning()
+    assert tune["cells_per_cta"] in (4, 8) and tune["nearest_chunk"] in (2048, 4096)
+    assert tune["workers_per_cta"] in (1, 2, 4)
+    assert len(batch.stage_ms()) == 5 and batch.launches() > 0
+    # one-shot batch from host buffers
+    results, grids, images = job.generate_batch(ctx, pal, reqs)
+    for i, (res, grid, image) in enumerate(singles):
+        assert np.array_equal(grids[i], grid) and np.array_equal(images[i], image)
+    batch.close()
+    pal.close()
+
+
+def test_batch_against_oracle(ctx, orc):
+    from mosaic_gpu import job
+
+    mats, thumbs = _palette_inputs()
+    pal = job.Palette(ctx, mats, thumbs, TILE, TILE, target_aspect=4 / 3)
+    tgts = _targets()[:3]
+    reqs = [job.mosaic_request(t, w, h, gw, gh, stream=i, **kw)
+            for i, (t, (w, h, gw, gh, kw)) in enumerate(zip(tgts, _requests()[:3]))]
+    results, grids, images = job.generate_batch(ctx, pal, reqs)
+    for i, (w, h, gw, gh, kw) in enumerate(_requests()[:3]):
+        cfg = job.JobConfig("b", w, h, 0, len(mats), 24, 0, gw, gh, kw.get("max_usage", 3), kw.get("weight", 0.25),
+                            kw.get("strength", 0.4), kw.get("iterations", 1000), kw.get("chains", 1), TILE, TILE,
+                            enable_optimization=kw.get("enable_opt", True), seed=20251203)
+        ref = orc.generate(job.Inputs(cfg, tgts[i], mats, thumbs), threads=8) if i == 2 else None
+        if ref is not None:
+            assert np.array_equal(grids[i], ref["grid"]) and np.array_equal(images[i], ref["image"])
+    pal.close()
+
+
+def test_palette_lab_and_similarity_match_oracle(ctx, orc):
+    import ctypes as C
+
+    from mosaic_gpu import job
+
+    mats, thumbs = _palette_inputs()
+    pal = job.Palette(ctx, mats, thumbs, TILE, TILE, target_aspect=4 / 3)
+    lab = pal.lab()
+    for i in range(0, len(mats), 17):
+        assert np.array_equal(lab[i].view(np.uint32), orc.lab_mean_spec(mats.image(i)).view(np.uint32))
+    sim = np.zeros((pal.size, pal.size), np.float32)
+    assert ctx.lib.mg_palette_read_similarity(pal.h, sim.ctypes.data_as(C.POINTER(C.c_float))) == 0
+    assert np.array_equal(sim.view(np.uint32), orc.similarity_full(lab).view(np.uint32))
+    pal.close()
