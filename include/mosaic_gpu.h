@@ -308,6 +308,40 @@ int mg_batch_destroy(mg_batch* batch);
  * are read in place). */
 int mg_generate_batch(mg_ctx* ctx, mg_palette* pal, const mg_mosaic* mosaics, int n, mg_result* results);
 
+/* ---- serving: a request loop over one resident palette ------------------------------
+ * No counterpart in the reference.  Requests submitted from any thread wait in
+ * a FIFO queue; a dispatcher admits them, within the device-memory budget, into
+ * the next free slot (a stream with reusable batch buffers) as one batch, so
+ * requests that arrive while others run are folded into the next batch and
+ * batches overlap on the device; a completion thread copies each request's
+ * grid and image into the caller's buffers.  A request's results do not depend
+ * on which requests share its batch.  Buffers passed to mg_server_submit (the
+ * target and the outputs) must stay valid until the request completes. */
+typedef struct mg_server mg_server;
+typedef struct mg_server_config {
+  int slots;                   /* batches in flight (streams), default 3 */
+  int max_batch;               /* requests per batch, default 64 */
+  int64_t memory_budget_bytes; /* device memory the admitted requests may use, default 120 GB */
+} mg_server_config;
+typedef struct mg_server_stats {
+  int64_t submitted, completed, rejected, batches, pending, bytes_in_use, peak_bytes_in_use;
+} mg_server_stats;
+void mg_server_config_default(mg_server_config* cfg);
+int mg_server_create(mg_ctx* ctx, mg_palette* pal, const mg_server_config* cfg, mg_server** out);
+/* grid_out: grid_w*grid_h ints; image_out: (grid_h*tile_h) x (grid_w*tile_w) x 3 (both nullable). */
+int mg_server_submit(mg_server* srv, const mg_mosaic* m, int32_t* grid_out, uint8_t* image_out, uint64_t* ticket);
+/* Status of a finished request (MG_OK, or MG_ERR_BUDGET when it can never fit
+ * the budget), or -1 while it is still pending.  latency_ms: submission to
+ * results on the host. */
+int mg_server_poll(mg_server* srv, uint64_t ticket, mg_result* res, double* latency_ms);
+int mg_server_wait(mg_server* srv, uint64_t ticket, mg_result* res, double* latency_ms);
+int mg_server_get_stats(mg_server* srv, mg_server_stats* stats);
+/* Device bytes the request would hold while admitted (what admission counts
+ * against the budget); -1 on a null argument. */
+int64_t mg_server_request_bytes(mg_server* srv, const mg_mosaic* m);
+/* Finishes queued and in-flight requests, then stops. */
+int mg_server_destroy(mg_server* srv);
+
 #ifdef __cplusplus
 }
 #endif

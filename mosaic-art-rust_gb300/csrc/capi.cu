@@ -12,7 +12,7 @@
 
 namespace mg {
 
-unsigned long long g_launches = 0;
+std::atomic<unsigned long long> g_launches{0};
 
 namespace {
 thread_local std::string g_error;

@@ -360,7 +360,7 @@ int batch_tune(mg_batch* b) {
   b->cells_warps = best_cw;
   best = 1e30f;
   int best_nn = 2048;
-  for (int ch : {2048, 4096}) {
+  for (int ch : {1024, 2048, 4096}) {
     b->nn_chunk = ch;
     MG_CHECK(batch_enqueue(b, true));
     MG_CUDA(cudaStreamSynchronize(s));
@@ -434,14 +434,18 @@ int batch_read(mg_batch* b, int i, mg_result* res) {
   std::vector<int32_t> grid(M.n);
   int best = -1, resets = 0;
   ChainResult cr{};
+  // every chain's summary comes back with the grid, so one synchronisation serves the read
+  std::vector<ChainResult> chains(M.run_sa && M.chains > 0 ? M.chains : 0);
   if (res->image)
     MG_CUDA(cudaMemcpyAsync(res->image, M.out, (size_t)b->out_w[i] * b->out_h[i] * 3, cudaMemcpyDeviceToHost, s));
   MG_CUDA(cudaMemcpyAsync(grid.data(), M.final_grid, sizeof(int32_t) * M.n, cudaMemcpyDeviceToHost, s));
   MG_CUDA(cudaMemcpyAsync(&resets, M.n_resets, sizeof(int), cudaMemcpyDeviceToHost, s));
   MG_CUDA(cudaMemcpyAsync(&best, M.best_chain, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (!chains.empty())
+    MG_CUDA(cudaMemcpyAsync(chains.data(), M.results, sizeof(ChainResult) * chains.size(), cudaMemcpyDeviceToHost, s));
   MG_CUDA(cudaStreamSynchronize(s));
   MG_CHECK(batch_check(b));
-  if (M.run_sa && best >= 0) MG_CUDA(cudaMemcpy(&cr, M.results + best, sizeof(cr), cudaMemcpyDeviceToHost));
+  if (M.run_sa && best >= 0 && best < (int)chains.size()) cr = chains[best];
   if (res->grid)
     for (int c = 0; c < M.n; ++c) res->grid[c] = grid[c] < 0 ? -1 : b->pal->selected[grid[c]];
   res->out_w = b->out_w[i];
@@ -610,3 +614,48 @@ int mg_generate_batch(mg_ctx* ctx, mg_palette* pal, const mg_mosaic* mosaics, in
 }
 
 }  // extern "C"
+
+// ---- hooks for the request loop (capi_server.cu) ----------------------------------
+namespace mg {
+
+mg_batch* server_batch_new() { return new mg_batch(); }
+
+void server_batch_free(mg_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  cudaDeviceSynchronize();
+  batch_release(b);
+  delete b;
+}
+
+// Reuses the batch's device buffers (they only grow); inputs in pinned host or
+// device memory are read in place; default launch shapes, no graph.
+int server_batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, int n) {
+  MG_CHECK(check_ctx(ctx));
+  MG_CHECK(batch_setup(b, ctx, pal, ms, n, true));
+  b->tuned = true;
+  return MG_OK;
+}
+
+int server_batch_enqueue(mg_batch* b) {
+  MG_CHECK(batch_enqueue(b, false));
+  b->ran = true;
+  return MG_OK;
+}
+
+int server_batch_read(mg_batch* b, int i, mg_result* res) { return batch_read(b, i, res); }
+
+// Device bytes a request adds to a batch (upper bound; a target in host memory
+// that cannot be read in place counts as copied).
+int64_t server_request_bytes(const mg_palette* pal, const mg_mosaic* m) {
+  const int64_t N = (int64_t)m->grid_w * m->grid_h;
+  const int64_t padded = (int64_t)padded_cells((int)N);
+  const int64_t k = std::max(pal->k, 1);
+  const int64_t chains = m->enable_optimization ? std::max(m->chains, 1) : 0;
+  int64_t bytes = padded * (16 + 4 + 8 * k + 16) + N * 8 + chains * (N * 4 + 32) +
+                  N * pal->tw * pal->th * 3 + 4096;
+  if (!device_view_or_device(m->target)) bytes += 3ll * m->target_w * m->target_h;
+  return bytes;
+}
+
+}  // namespace mg

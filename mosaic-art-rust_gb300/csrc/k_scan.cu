@@ -19,7 +19,7 @@
 namespace mg {
 namespace {
 
-constexpr int kWarps = 8;
+constexpr int kWarps = 16;
 constexpr int kThreads = kWarps * 32;
 constexpr int kListCap = 128;  // k <= 100
 constexpr int kBufCap = 128;   // candidate buffer; merged when it could overflow
@@ -160,28 +160,41 @@ __global__ void __launch_bounds__(kThreads) nearest_kernel(const float4* __restr
       const int n = chunk_len(c);
       const int gbase = c * kChunk;
       if (active) {
-        for (int base = 0; base < n; base += 128) {
-          unsigned long long key[4];
+        // 8 entries per lane per step; in steady state the k-th best is tight and
+        // a single warp vote rejects all 256 entries.
+        for (int base = 0; base < n; base += 256) {
+          uint32_t db[8];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
+          for (int u = 0; u < 8; ++u) {
             const int j = base + u * 32 + lane;
-            key[u] = kMaxKey;
+            db[u] = 0xFFFFFFFFu;
             if (j < n) {
               const float4 e = sp[j];
-              const float d = sq_dist(q.x, q.y, q.z, e.x, e.y, e.z);
-              key[u] = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)(gbase + j);
+              db[u] = __float_as_uint(sq_dist(q.x, q.y, q.z, e.x, e.y, e.z));
             }
           }
+          const uint32_t thr_d = (uint32_t)(thr >> 32), thr_i = (uint32_t)thr;
+          bool anyp = false;
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const bool pass = key[u] < thr;
-            const unsigned mask = __ballot_sync(0xffffffffu, pass);
-            if (mask) {
-              const int pos = nbuf + __popc(mask & ((1u << lane) - 1u));
-              if (pass) W.buf[pos] = key[u];
-              nbuf += __popc(mask);
-              __syncwarp();
-              if (nbuf > kBufCap - 32) warp_merge(W, len, nbuf, thr, k, lane);
+          for (int u = 0; u < 8; ++u) {
+            const uint32_t gi = (uint32_t)(gbase + base + u * 32 + lane);
+            anyp = anyp || db[u] < thr_d || (db[u] == thr_d && gi < thr_i);
+          }
+          if (__any_sync(0xffffffffu, anyp)) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int j = base + u * 32 + lane;
+              const unsigned long long key =
+                  j < n ? (((unsigned long long)db[u] << 32) | (unsigned)(gbase + j)) : kMaxKey;
+              const bool pass = key < thr;
+              const unsigned mask = __ballot_sync(0xffffffffu, pass);
+              if (mask) {
+                const int pos = nbuf + __popc(mask & ((1u << lane) - 1u));
+                if (pass) W.buf[pos] = key;
+                nbuf += __popc(mask);
+                __syncwarp();
+                if (nbuf > kBufCap - 32) warp_merge(W, len, nbuf, thr, k, lane);
+              }
             }
           }
         }
@@ -241,6 +254,7 @@ int launch_nearest(const float4* pal, int p, const float4* queries, int nq, int 
     return MG_OK;
   }
   if (chunk == 4096) return launch_nearest_t<4096>(pal, p, queries, nq, keff, k, idx, dist, err, stream);
+  if (chunk == 1024) return launch_nearest_t<1024>(pal, p, queries, nq, keff, k, idx, dist, err, stream);
   return launch_nearest_t<2048>(pal, p, queries, nq, keff, k, idx, dist, err, stream);
 }
 

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 
 #include "../../include/mosaic_gpu.h"
@@ -77,7 +78,7 @@ int launch_thumbnails(const uint8_t* base, const Region* regions, int n, int tw,
                       cudaStream_t stream);
 
 // (b) k nearest palette entries for every query (ties -> lowest index).
-// chunk: palette entries per shared-memory stage (2048 or 4096).
+// chunk: palette entries per shared-memory stage (1024, 2048 or 4096).
 int launch_nearest(const float4* pal, int p, const float4* queries, int nq, int k, uint32_t* idx,
                    float* dist, uint32_t* err, cudaStream_t stream, int chunk = 2048);
 
@@ -178,6 +179,6 @@ int launch_optimal_adjustment(const uint8_t* tile_rgb, const uint8_t* target_rgb
                               float4* out, cudaStream_t stream);
 
 // Number of kernel launches issued by this library since load (for reporting).
-extern unsigned long long g_launches;
+extern std::atomic<unsigned long long> g_launches;
 
 }  // namespace mg

@@ -86,6 +86,15 @@ class Mosaic(C.Structure):
                 ("seed", C.c_uint64), ("stream", C.c_uint32)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_int), ("max_batch", C.c_int), ("memory_budget_bytes", C.c_int64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "rejected", "batches", "pending",
+                                         "bytes_in_use", "peak_bytes_in_use")]
+
+
 # (name, restype, argtypes) for every exported symbol of mosaic_gpu.h.
 SIGNATURES = [
     ("mg_palette_desc_default", None, [C.POINTER(PaletteDesc)]),
@@ -104,6 +113,14 @@ SIGNATURES = [
     ("mg_batch_launches", C.c_int, [C.c_void_p]),
     ("mg_batch_destroy", C.c_int, [C.c_void_p]),
     ("mg_generate_batch", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Mosaic), C.c_int, C.c_void_p]),
+    ("mg_server_config_default", None, [C.POINTER(ServerConfig)]),
+    ("mg_server_create", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    ("mg_server_submit", C.c_int, [C.c_void_p, C.POINTER(Mosaic), _i32p, _u8p, C.POINTER(C.c_uint64)]),
+    ("mg_server_poll", C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.POINTER(C.c_double)]),
+    ("mg_server_wait", C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.POINTER(C.c_double)]),
+    ("mg_server_get_stats", C.c_int, [C.c_void_p, C.POINTER(ServerStats)]),
+    ("mg_server_request_bytes", C.c_int64, [C.c_void_p, C.POINTER(Mosaic)]),
+    ("mg_server_destroy", C.c_int, [C.c_void_p]),
     ("mg_version", C.c_int, []),
     ("mg_last_error", C.c_char_p, []),
     ("mg_kernel_launches", C.c_ulonglong, []),

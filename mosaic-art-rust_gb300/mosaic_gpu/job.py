@@ -313,3 +313,145 @@ def generate_batch(ctx: capi.Context, palette: Palette, mosaics: list):
         images.append(im)
     capi.check(ctx.lib.mg_generate_batch(ctx.h, palette.h, arr, n, results))
     return list(results)[:n], grids, images
+
+
+# ---- the batched and served workloads ----------------------------------------------------
+@dataclass
+class MosaicSpec:
+    w: int
+    h: int
+    gw: int
+    gh: int
+    target: np.ndarray
+
+
+def uneven_grids(n: int, lo: int, hi: int, seed: int):
+    """Grid widths log-uniform in [lo, hi], aspect 4:3."""
+    rng = np.random.default_rng(seed)
+    gw = np.exp(rng.uniform(np.log(lo), np.log(hi), n)).round().astype(int)
+    gh = np.maximum(1, (gw * 3 / 4).round().astype(int))
+    return gw, gh
+
+
+def batched_workload(n=256, cell_px=32, n_materials=10000, seed=20251203, allocator=None, scale=1.0):
+    """256 mosaics, grid widths log-uniform in 20..160 (4:3), 32 px per cell, targets from the
+    blob+noise generator (8 blobs); one palette of 10 000 128x128 materials; 32x32 tiles."""
+    gw, gh = uneven_grids(n, max(2, int(20 * scale)), max(3, int(160 * scale)), seed)
+    specs = []
+    for i in range(n):
+        w, h = int(gw[i]) * cell_px, int(gh[i]) * cell_px
+        specs.append(MosaicSpec(w, h, int(gw[i]), int(gh[i]), synth.target(w, h, 8, seed, 100 + i, allocator)))
+    mats = synth.materials(n_materials, 128, 0, seed, 2, allocator)
+    thumbs = synth.thumbnails(mats, cell_px, cell_px, allocator)
+    return specs, mats, thumbs
+
+
+def batched_requests(specs, iterations=5000, chains=8, max_usage=4, weight=0.25, strength=0.4, seed=20251203):
+    return [mosaic_request(s.target, s.w, s.h, s.gw, s.gh, max_usage=max_usage, weight=weight, strength=strength,
+                           iterations=iterations, chains=chains, seed=seed, stream=i) for i, s in enumerate(specs)]
+
+
+def served_grids(n: int, seed: int, lo: int = 500, hi: int = 50000):
+    """Cells per request log-uniform in [lo, hi], aspect 4:3: (grid widths, grid heights)."""
+    rng = np.random.default_rng(seed)
+    cells = np.exp(rng.uniform(np.log(lo), np.log(hi), n))
+    gw = np.maximum(1, np.sqrt(cells * 4 / 3).round().astype(int))
+    gh = np.maximum(1, (gw * 3 / 4).round().astype(int))
+    return gw, gh
+
+
+def served_workload(n_targets=64, cell_px=24, n_materials=20000, seed=20251203, allocator=None, scale=1.0):
+    """The served stream's inputs: a pool of targets (cells log-uniform in 500..50 000 at 4:3,
+    blob+noise generator with 8 blobs, 24 px per cell) and one palette of 20 000 128x128
+    materials with 24x24 thumbnails.  `scale` shrinks the cell range for small runs."""
+    gw, gh = served_grids(n_targets, seed, max(4, int(500 * scale)), max(12, int(50000 * scale)))
+    pool = []
+    for i in range(n_targets):
+        w, h = int(gw[i]) * cell_px, int(gh[i]) * cell_px
+        pool.append(MosaicSpec(w, h, int(gw[i]), int(gh[i]), synth.target(w, h, 8, seed, 5000 + i, allocator)))
+    mats = synth.materials(n_materials, 128, 0, seed, 2, allocator)
+    thumbs = synth.thumbnails(mats, cell_px, cell_px, allocator)
+    return pool, mats, thumbs
+
+
+def served_stream(pool, n: int, seed: int, iterations=2000, chains=4, max_usage=5, weight=0.25, strength=0.4):
+    """n requests drawn from the target pool (request j: pool entry picked by a seeded draw,
+    Philox stream id j): [(pool index, mg_mosaic)]."""
+    rng = np.random.default_rng(seed ^ 0x5EED)
+    picks = rng.integers(0, len(pool), n)
+    out = []
+    for j, p in enumerate(picks):
+        s = pool[int(p)]
+        out.append((int(p), mosaic_request(s.target, s.w, s.h, s.gw, s.gh, max_usage=max_usage, weight=weight,
+                                           strength=strength, iterations=iterations, chains=chains, seed=seed,
+                                           stream=j)))
+    return out
+
+
+def poisson_arrivals(rate: float, n: int, seed: int):
+    """Arrival offsets (s) of a Poisson process of the given rate."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, n))
+
+
+class Server:
+    """The request loop over one resident palette (mg_server)."""
+
+    def __init__(self, ctx: capi.Context, palette: Palette, slots: int = 3, max_batch: int = 64,
+                 memory_budget_bytes: int = 120 << 30):
+        self.ctx, self.palette = ctx, palette
+        cfg = capi.ServerConfig()
+        ctx.lib.mg_server_config_default(C.byref(cfg))
+        cfg.slots, cfg.max_batch, cfg.memory_budget_bytes = slots, max_batch, memory_budget_bytes
+        h = C.c_void_p()
+        capi.check(ctx.lib.mg_server_create(ctx.h, palette.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._live = {}  # ticket -> (mosaic, grid, image) kept alive until completion
+
+    def submit(self, m: capi.Mosaic, grid: np.ndarray | None = None, image: np.ndarray | None = None) -> int:
+        """Queue one request; grid/image (caller-owned, e.g. pinned) receive the results."""
+        m = capi.Mosaic.from_buffer_copy(m)
+        t = C.c_uint64()
+        capi.check(self.ctx.lib.mg_server_submit(
+            self.h, C.byref(m), capi.ptr(grid, C.c_int32) if grid is not None else None,
+            capi.ptr(image, C.c_uint8) if image is not None else None, C.byref(t)))
+        self._live[t.value] = (m, grid, image)
+        return t.value
+
+    def _finish(self, fn, ticket: int):
+        res = capi.Result()
+        lat = C.c_double()
+        st = fn(self.h, ticket, C.byref(res), C.byref(lat))
+        if st == -1:
+            return None
+        self._live.pop(ticket, None)
+        return st, res, lat.value
+
+    def wait(self, ticket: int):
+        """(status, Result, latency_ms) of a request, blocking until it completes."""
+        return self._finish(self.ctx.lib.mg_server_wait, ticket)
+
+    def poll(self, ticket: int):
+        """(status, Result, latency_ms), or None while the request is pending."""
+        return self._finish(self.ctx.lib.mg_server_poll, ticket)
+
+    def request_bytes(self, m: capi.Mosaic) -> int:
+        """Device bytes admission counts for the request against the budget."""
+        return int(self.ctx.lib.mg_server_request_bytes(self.h, C.byref(m)))
+
+    def stats(self) -> dict:
+        s = capi.ServerStats()
+        capi.check(self.ctx.lib.mg_server_get_stats(self.h, C.byref(s)))
+        return {n: int(getattr(s, n)) for n, _ in capi.ServerStats._fields_}
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.mg_server_destroy(self.h)
+            self.h = None
+            self._live.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
