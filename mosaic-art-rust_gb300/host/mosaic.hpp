@@ -1,0 +1,703 @@
+// mosaic.hpp -- C++ mirror of the mosaic-rust crate's public API for the tile
+// matching-and-placement path, over the C ABI of libmosaic_gpu.so
+// (include/mosaic_gpu.h).  Header-only, C++17.
+//
+// Names, argument meaning and results follow the crate:
+//   MosaicGenerator / MosaicGeneratorImpl   lib.rs:52-123
+//   UsageTracker                            lib.rs:57-89
+//   SimilarityDatabase                      similarity.rs:30-138
+//   calculate_lab_distance                  similarity.rs:141-146
+//   GridPosition                            adjacency.rs:5-46
+//   AdjacencyPenaltyCalculator              adjacency.rs:48-214
+//   OptimizationConfig / MosaicOptimizer /
+//   OptimizationResult                      optimizer.rs:7-221
+//   ColorAdjustment /
+//   calculate_optimal_adjustment            color_adjustment.rs:6-154
+//   generate_mosaic                         main.rs:105-164 + 477-685
+// plus RAII handles for the resident palette, batches and the request loop.
+//
+// Error behaviour: where the crate returns Option the mirror returns
+// std::optional; where it returns anyhow::Result (file I/O) or where the device
+// fails, the mirror throws mosaic::Error carrying the library's status code and
+// message.  The library itself never throws, aborts or unwinds.
+//
+// Differences a caller can observe, all at edges the crate leaves undefined or
+// nondeterministic:
+//  - Annealing draws from a seeded Philox stream (OptimizationConfig::seed,
+//    ::stream) instead of the crate's unseeded thread_rng, so runs repeat.
+//  - The optimiser works on palette indices: every tile placed in a grid it
+//    optimises must be in the similarity database (Error otherwise).
+//  - save_to_file writes a binary file (JSON for a 20 000-tile database is
+//    several GB); load_from_file reads that format.
+//  - The adjacency functions need build_similarities to have run over every
+//    tile added (Error with MG_ERR_STATE otherwise); the crate would look pairs
+//    up in a missing or stale matrix.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <filesystem>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <optional>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "mosaic_gpu.h"
+
+namespace mosaic {
+
+using Path = std::filesystem::path;
+using Grid = std::vector<std::vector<std::optional<Path>>>;
+
+class Error : public std::runtime_error {
+ public:
+  Error(int code, const std::string& msg) : std::runtime_error(msg), code_(code) {}
+  int code() const { return code_; }
+
+ private:
+  int code_;
+};
+
+namespace detail {
+inline void check(int status) {
+  if (status != MG_OK) {
+    const char* m = mg_last_error();
+    throw Error(status, std::string("mosaic_gpu: ") + (m ? m : "error ") + " (status " + std::to_string(status) + ")");
+  }
+}
+}  // namespace detail
+
+// ---- context -------------------------------------------------------------------------
+// One CUDA stream of the library.  The crate has no such object; every mirror
+// function takes an optional Context and otherwise uses default_context()
+// (device 0, or the device named by MOSAIC_GPU_DEVICE).
+class Context {
+ public:
+  explicit Context(int device = 0) { detail::check(mg_ctx_create(device, &h_)); }
+  ~Context() {
+    if (h_) mg_ctx_destroy(h_);
+  }
+  Context(const Context&) = delete;
+  Context& operator=(const Context&) = delete;
+  mg_ctx* get() const { return h_; }
+  void sync() { detail::check(mg_ctx_sync(h_)); }
+
+ private:
+  mg_ctx* h_ = nullptr;
+};
+
+inline Context& default_context() {
+  static Context ctx([] {
+    const char* d = std::getenv("MOSAIC_GPU_DEVICE");
+    return d ? std::atoi(d) : 0;
+  }());
+  return ctx;
+}
+
+// ---- colours and images ----------------------------------------------------------------
+struct Lab {  // palette::Lab<D65, f32>
+  float l = 0.0f, a = 0.0f, b = 0.0f;
+};
+struct Rgb {  // image::Rgb<u8>
+  uint8_t r = 0, g = 0, b = 0;
+};
+// A borrowed RGB8 image (DynamicImage after to_rgb8()).
+struct RgbImageView {
+  const uint8_t* data = nullptr;
+  int width = 0, height = 0;
+  int64_t stride = 0;  // bytes between rows; 0 -> 3*width
+  int64_t row_bytes() const { return stride ? stride : 3 * (int64_t)width; }
+};
+struct RgbImage {
+  int width = 0, height = 0;
+  std::vector<uint8_t> pixels;  // height x width x 3
+  RgbImageView view() const { return {pixels.data(), width, height, 3 * (int64_t)width}; }
+};
+
+// similarity.rs:141-146
+inline float calculate_lab_distance(const Lab& a, const Lab& b) {
+  const float x[3] = {a.l, a.a, a.b}, y[3] = {b.l, b.a, b.b};
+  return mg_lab_distance(x, y);
+}
+
+// ---- lib.rs --------------------------------------------------------------------------
+// lib.rs:93-123 (the MosaicGenerator trait's one implementation)
+struct MosaicGeneratorImpl {
+  // Mean of the per-pixel Lab colours (not the Lab of the mean RGB).
+  static Lab calculate_average_lab(const RgbImageView& img, Context& ctx = default_context()) {
+    float lab[3];
+    detail::check(mg_average_lab(ctx.get(), img.data, img.width, img.height, img.row_bytes(), lab));
+    return {lab[0], lab[1], lab[2]};
+  }
+  static bool is_aspect_ratio_match(float img_aspect, float target_aspect, float tolerance) {
+    return mg_is_aspect_ratio_match(img_aspect, target_aspect, tolerance) != 0;
+  }
+};
+
+// lib.rs:57-89.  Host bookkeeping, as in the crate (the device walk keeps its
+// own counters).
+class UsageTracker {
+ public:
+  explicit UsageTracker(size_t max_usage_per_image) : max_(max_usage_per_image) {}
+  bool can_use_image(const Path& p) const { return get_usage_count(p) < max_; }
+  void use_image(const Path& p) { counts_[p] = get_usage_count(p) + 1; }
+  size_t get_usage_count(const Path& p) const {
+    auto it = counts_.find(p);
+    return it == counts_.end() ? 0 : it->second;
+  }
+  void reset() { counts_.clear(); }
+
+ private:
+  std::map<Path, size_t> counts_;
+  size_t max_;
+};
+
+// ---- similarity.rs ---------------------------------------------------------------------
+class SimilarityDatabase {
+ public:
+  SimilarityDatabase() = default;
+
+  // similarity.rs:61-66; the index is the insertion order.
+  void add_tile(const Path& path, const Lab& lab) {
+    const size_t index = labs_.size();
+    path_to_index_[path] = index;
+    index_to_path_[index] = path;
+    labs_.push_back(lab);
+  }
+
+  // similarity.rs:69-82: every pair i < j, strict upper triangle in row order,
+  // computed on the device.
+  void build_similarities(Context& ctx = default_context()) {
+    const size_t n = labs_.size();
+    sims_.assign(n > 1 ? n * (n - 1) / 2 : 0, 0.0f);
+    built_n_ = n;
+    if (n < 2) return;
+    detail::check(mg_similarity_build(ctx.get(), flat_lab().data(), (int)n, MG_SIM_TRIANGULAR, sims_.data()));
+  }
+
+  // similarity.rs:85-103: None when a path is unknown or the pair has no entry.
+  std::optional<float> get_similarity(const Path& a, const Path& b) const {
+    auto ia = path_to_index_.find(a), ib = path_to_index_.find(b);
+    if (ia == path_to_index_.end() || ib == path_to_index_.end()) return std::nullopt;
+    if (ia->second == ib->second) return 0.0f;
+    size_t i = ia->second, j = ib->second;
+    if (i > j) std::swap(i, j);
+    const size_t n = labs_.size();
+    const size_t pos = i * n - i * (i + 1) / 2 + j - i - 1;
+    if (pos >= sims_.size()) return std::nullopt;
+    return sims_[pos];
+  }
+
+  // similarity.rs:106-109
+  std::optional<Lab> get_lab_color(const Path& p) const {
+    auto it = path_to_index_.find(p);
+    if (it == path_to_index_.end() || it->second >= labs_.size()) return std::nullopt;
+    return labs_[it->second];
+  }
+
+  // similarity.rs:112-116 (the crate writes JSON; this writes the binary format
+  // described below).  Throws Error on I/O failure.
+  void save_to_file(const Path& file) const {
+    std::ofstream f(file, std::ios::binary | std::ios::trunc);
+    if (!f) throw Error(MG_ERR_ARG, "cannot create " + file.string());
+    const uint64_t n = labs_.size(), ns = sims_.size();
+    f.write(kMagic, 8);
+    put<uint32_t>(f, kVersion);
+    put<uint64_t>(f, n);
+    put<uint64_t>(f, ns);
+    for (uint64_t i = 0; i < n; ++i) {
+      const std::string s = index_to_path_.at(i).generic_string();
+      put<uint32_t>(f, (uint32_t)s.size());
+      f.write(s.data(), (std::streamsize)s.size());
+    }
+    for (const Lab& c : labs_) {
+      put<float>(f, c.l);
+      put<float>(f, c.a);
+      put<float>(f, c.b);
+    }
+    if (ns) f.write(reinterpret_cast<const char*>(sims_.data()), (std::streamsize)(ns * sizeof(float)));
+    if (!f) throw Error(MG_ERR_ARG, "write failed: " + file.string());
+  }
+
+  // similarity.rs:119-123.  Throws Error when the file is missing or malformed.
+  static SimilarityDatabase load_from_file(const Path& file) {
+    std::ifstream f(file, std::ios::binary);
+    if (!f) throw Error(MG_ERR_ARG, "cannot open " + file.string());
+    char magic[8];
+    f.read(magic, 8);
+    if (!f || std::memcmp(magic, kMagic, 8) != 0) throw Error(MG_ERR_ARG, "not a similarity database: " + file.string());
+    if (get<uint32_t>(f, file) != kVersion) throw Error(MG_ERR_ARG, "unsupported version: " + file.string());
+    const uint64_t n = get<uint64_t>(f, file), ns = get<uint64_t>(f, file);
+    if (ns != 0 && ns != n * (n - 1) / 2) throw Error(MG_ERR_ARG, "inconsistent sizes: " + file.string());
+    SimilarityDatabase db;
+    std::vector<Path> paths(n);
+    for (uint64_t i = 0; i < n; ++i) {
+      const uint32_t len = get<uint32_t>(f, file);
+      std::string s(len, '\0');
+      f.read(s.data(), len);
+      if (!f) throw Error(MG_ERR_ARG, "truncated file: " + file.string());
+      paths[i] = Path(s);
+    }
+    for (uint64_t i = 0; i < n; ++i) {
+      Lab c;
+      c.l = get<float>(f, file);
+      c.a = get<float>(f, file);
+      c.b = get<float>(f, file);
+      db.add_tile(paths[i], c);
+    }
+    db.sims_.resize(ns);
+    if (ns) f.read(reinterpret_cast<char*>(db.sims_.data()), (std::streamsize)(ns * sizeof(float)));
+    if (!f) throw Error(MG_ERR_ARG, "truncated file: " + file.string());
+    db.built_n_ = ns ? n : 0;
+    return db;
+  }
+
+  // similarity.rs:126-138 (same messages on stdout).
+  static SimilarityDatabase load_or_new(const Path& file) {
+    try {
+      SimilarityDatabase db = load_from_file(file);
+      std::printf("Loaded similarity database from \"%s\"\n", file.string().c_str());
+      return db;
+    } catch (const Error&) {
+      std::printf("Creating new similarity database\n");
+      return SimilarityDatabase();
+    }
+  }
+
+  // Index view for the device calls (no counterpart in the crate).
+  size_t len() const { return labs_.size(); }
+  std::optional<size_t> index_of(const Path& p) const {
+    auto it = path_to_index_.find(p);
+    if (it == path_to_index_.end()) return std::nullopt;
+    return it->second;
+  }
+  const Path& path_of(size_t i) const { return index_to_path_.at(i); }
+  // True when build_similarities covered every tile added so far.
+  bool built() const { return built_n_ == labs_.size() && !labs_.empty(); }
+  std::vector<float> flat_lab() const {
+    std::vector<float> v(3 * labs_.size());
+    for (size_t i = 0; i < labs_.size(); ++i) {
+      v[3 * i] = labs_[i].l;
+      v[3 * i + 1] = labs_[i].a;
+      v[3 * i + 2] = labs_[i].b;
+    }
+    return v;
+  }
+  const std::vector<float>& similarities() const { return sims_; }
+
+ private:
+  // File layout (little-endian): "MGSIMDB1", u32 version, u64 n, u64 number of
+  // similarity entries (0 or n(n-1)/2), n x (u32 length + UTF-8 path), n x 3
+  // f32 Lab, then the strict upper triangle in row order as f32.
+  static constexpr char kMagic[9] = "MGSIMDB1";
+  static constexpr uint32_t kVersion = 1;
+  template <class T>
+  static void put(std::ofstream& f, T v) {
+    f.write(reinterpret_cast<const char*>(&v), sizeof(T));
+  }
+  template <class T>
+  static T get(std::ifstream& f, const Path& file) {
+    T v;
+    f.read(reinterpret_cast<char*>(&v), sizeof(T));
+    if (!f) throw Error(MG_ERR_ARG, "truncated file: " + file.string());
+    return v;
+  }
+
+  std::map<Path, size_t> path_to_index_;
+  std::map<size_t, Path> index_to_path_;
+  std::vector<Lab> labs_;
+  std::vector<float> sims_;
+  size_t built_n_ = 0;
+};
+
+// ---- adjacency.rs ------------------------------------------------------------------------
+struct GridPosition {  // adjacency.rs:5-46
+  size_t x = 0, y = 0;
+  GridPosition() = default;
+  GridPosition(size_t x_, size_t y_) : x(x_), y(y_) {}
+  bool operator==(const GridPosition& o) const { return x == o.x && y == o.y; }
+  bool operator!=(const GridPosition& o) const { return !(*this == o); }
+  // Up, down, left, right -- the order the penalty sums in.
+  std::vector<GridPosition> get_adjacent_positions(size_t grid_width, size_t grid_height) const {
+    std::vector<GridPosition> v;
+    if (y > 0) v.emplace_back(x, y - 1);
+    if (y + 1 < grid_height) v.emplace_back(x, y + 1);
+    if (x > 0) v.emplace_back(x - 1, y);
+    if (x + 1 < grid_width) v.emplace_back(x + 1, y);
+    return v;
+  }
+};
+
+class AdjacencyPenaltyCalculator {
+ public:
+  AdjacencyPenaltyCalculator(const SimilarityDatabase& db, float penalty_weight, Context& ctx = default_context())
+      : db_(&db), weight_(penalty_weight), ctx_(&ctx) {}
+
+  // adjacency.rs:63-88: weight * sum over placed neighbours of 1/(sim+1); a
+  // neighbour or candidate unknown to the database contributes nothing.
+  float calculate_penalty(const Path& candidate, GridPosition pos, const Grid& grid, size_t grid_width,
+                          size_t grid_height) const {
+    require_built();
+    auto ci = db_->index_of(candidate);
+    if (!ci || grid_width == 0 || grid_height == 0) return 0.0f;
+    std::vector<int32_t> g = indices(grid, grid_width, grid_height, false);
+    const int32_t cxy[3] = {(int32_t)*ci, (int32_t)pos.x, (int32_t)pos.y};
+    float out = 0.0f;
+    const std::vector<float> lab = db_->flat_lab();
+    detail::check(mg_penalty_batch(ctx_->get(), lab.data(), (int)db_->len(), g.data(), (int)grid_width,
+                                   (int)grid_height, weight_, cxy, 1, &out));
+    return out;
+  }
+
+  // adjacency.rs:91-130: unweighted sum over right and down pairs.
+  float calculate_total_cost(const Grid& grid) const {
+    require_built();
+    if (grid.empty() || grid[0].empty()) return 0.0f;
+    const size_t gw = grid[0].size(), gh = grid.size();
+    std::vector<int32_t> g = indices(grid, gw, gh, false);
+    float out = 0.0f;
+    const std::vector<float> lab = db_->flat_lab();
+    detail::check(mg_total_cost(ctx_->get(), lab.data(), (int)db_->len(), g.data(), (int)gw, (int)gh, &out));
+    return out;
+  }
+
+  // adjacency.rs:133-214
+  float calculate_swap_delta(const Grid& grid, GridPosition a, GridPosition b) const {
+    require_built();
+    if (grid.empty() || grid[0].empty()) return 0.0f;
+    const size_t gw = grid[0].size(), gh = grid.size();
+    std::vector<int32_t> g = indices(grid, gw, gh, false);
+    const int32_t pairs[4] = {(int32_t)a.x, (int32_t)a.y, (int32_t)b.x, (int32_t)b.y};
+    float out = 0.0f;
+    const std::vector<float> lab = db_->flat_lab();
+    detail::check(mg_swap_delta_batch(ctx_->get(), lab.data(), (int)db_->len(), g.data(), (int)gw, (int)gh, pairs, 1,
+                                      &out));
+    return out;
+  }
+
+  void require_built() const {
+    if (!db_->built()) throw Error(MG_ERR_STATE, "build_similarities has not run over every tile");
+  }
+  const SimilarityDatabase& database() const { return *db_; }
+  float weight() const { return weight_; }
+  Context& context() const { return *ctx_; }
+
+  // Row-major palette indices, -1 for an empty cell (and, unless `strict`, for
+  // a tile the database does not know, which the crate's lookups skip too).
+  std::vector<int32_t> indices(const Grid& grid, size_t gw, size_t gh, bool strict) const {
+    std::vector<int32_t> g(gw * gh, -1);
+    for (size_t y = 0; y < gh; ++y) {
+      if (grid[y].size() != gw) throw Error(MG_ERR_ARG, "ragged grid");
+      for (size_t x = 0; x < gw; ++x) {
+        const auto& cell = grid[y][x];
+        if (!cell) continue;
+        auto i = db_->index_of(*cell);
+        if (i) g[y * gw + x] = (int32_t)*i;
+        else if (strict) throw Error(MG_ERR_ARG, "tile not in the similarity database: " + cell->string());
+      }
+    }
+    return g;
+  }
+
+ private:
+  const SimilarityDatabase* db_;
+  float weight_;
+  Context* ctx_;
+};
+
+// ---- optimizer.rs ---------------------------------------------------------------------------
+struct OptimizationConfig {  // optimizer.rs:7-27 (+ seeded stream and chains)
+  size_t max_iterations = 1000;
+  float initial_temperature = 100.0f;
+  float temperature_decay = 0.99995f;
+  size_t report_interval = 100;  // kept for the crate's field set; nothing is printed
+  uint64_t seed = 0;
+  uint32_t stream = 0;
+  int chains = 1;  // independent chains; the grid takes the lowest final cost
+};
+
+struct OptimizationResult {  // optimizer.rs:203-221
+  float initial_cost = 0.0f, final_cost = 0.0f, best_cost = 0.0f;
+  size_t improved_count = 0, accepted_count = 0, iterations = 0;
+  float improvement_percentage() const {
+    mg_sa_result r{};
+    r.initial_cost = initial_cost;
+    r.final_cost = final_cost;
+    return mg_improvement_percentage(&r);
+  }
+};
+
+class MosaicOptimizer {
+ public:
+  MosaicOptimizer(const AdjacencyPenaltyCalculator& calc, OptimizationConfig cfg) : calc_(&calc), cfg_(cfg) {}
+
+  // optimizer.rs:41-129
+  OptimizationResult optimize(Grid& grid) const { return run(grid, cfg_.max_iterations, false); }
+  // optimizer.rs:132-198
+  OptimizationResult optimize_greedy(Grid& grid, size_t max_iterations) const { return run(grid, max_iterations, true); }
+
+ private:
+  OptimizationResult run(Grid& grid, size_t iters, bool greedy) const {
+    if (grid.empty()) return {};
+    const size_t gw = grid[0].size(), gh = grid.size();
+    const SimilarityDatabase& db = calc_->database();
+    calc_->require_built();
+    std::vector<int32_t> g = calc_->indices(grid, gw, gh, true);
+    mg_sa_config c;
+    mg_sa_config_default(&c);
+    c.max_iterations = (int64_t)iters;
+    c.initial_temperature = cfg_.initial_temperature;
+    c.temperature_decay = cfg_.temperature_decay;
+    c.chains = cfg_.chains;
+    c.seed = cfg_.seed;
+    c.stream = cfg_.stream;
+    c.greedy_only = greedy ? 1 : 0;
+    mg_sa_result best{};
+    const std::vector<float> lab = db.flat_lab();
+    detail::check(mg_optimize(calc_->context().get(), lab.data(), (int)db.len(), g.data(), (int)gw, (int)gh, &c,
+                              &best, nullptr, nullptr));
+    for (size_t y = 0; y < gh; ++y)
+      for (size_t x = 0; x < gw; ++x) {
+        const int32_t i = g[y * gw + x];
+        grid[y][x] = i >= 0 ? std::optional<Path>(db.path_of((size_t)i)) : std::nullopt;
+      }
+    OptimizationResult r;
+    r.initial_cost = best.initial_cost;
+    r.final_cost = best.final_cost;
+    r.best_cost = best.best_cost;
+    r.improved_count = (size_t)best.improved_count;
+    r.accepted_count = (size_t)best.accepted_count;
+    r.iterations = (size_t)best.iterations;
+    return r;
+  }
+
+  const AdjacencyPenaltyCalculator* calc_;
+  OptimizationConfig cfg_;
+};
+
+// ---- color_adjustment.rs -----------------------------------------------------------------------
+struct ColorAdjustment {  // color_adjustment.rs:6-26
+  float brightness = 0.0f, contrast = 1.0f, hue_shift = 0.0f, saturation = 1.0f;
+
+  // color_adjustment.rs:30-37 (ColorAdjustment::new, clamping each field)
+  static ColorAdjustment create(float brightness, float contrast, float hue_shift, float saturation) {
+    const mg_color_adjustment a = mg_color_adjustment_new(brightness, contrast, hue_shift, saturation);
+    return {a.brightness, a.contrast, a.hue_shift, a.saturation};
+  }
+  mg_color_adjustment raw() const { return {brightness, contrast, hue_shift, saturation}; }
+
+  // color_adjustment.rs:53-89
+  Rgb adjust_pixel(Rgb px, Context& ctx = default_context()) const {
+    const uint8_t in[3] = {px.r, px.g, px.b};
+    uint8_t out[3];
+    const mg_color_adjustment a = raw();
+    detail::check(mg_apply_adjustment(ctx.get(), &a, in, 1, 1, 3, out));
+    return {out[0], out[1], out[2]};
+  }
+  // color_adjustment.rs:40-51
+  RgbImage apply_to_image(const RgbImageView& img, Context& ctx = default_context()) const {
+    RgbImage out;
+    out.width = img.width;
+    out.height = img.height;
+    out.pixels.resize((size_t)img.width * img.height * 3);
+    const mg_color_adjustment a = raw();
+    detail::check(mg_apply_adjustment(ctx.get(), &a, img.data, img.width, img.height, img.row_bytes(),
+                                      out.pixels.data()));
+    return out;
+  }
+};
+
+// color_adjustment.rs:99-154
+inline ColorAdjustment calculate_optimal_adjustment(Rgb tile_avg, Rgb target_avg, float strength,
+                                                    Context& ctx = default_context()) {
+  const uint8_t t[3] = {tile_avg.r, tile_avg.g, tile_avg.b}, g[3] = {target_avg.r, target_avg.g, target_avg.b};
+  mg_color_adjustment a;
+  detail::check(mg_optimal_adjustment_batch(ctx.get(), t, g, 1, strength, &a));
+  return {a.brightness, a.contrast, a.hue_shift, a.saturation};
+}
+
+// ---- the generator (main.rs) --------------------------------------------------------------------
+// The CLI options of main.rs:21-88 that reach the path.
+struct MosaicOptions {
+  int grid_w = 50, grid_h = 28;
+  int max_materials = 500;
+  float aspect_tolerance = 0.1f;
+  int max_usage_per_image = 3;
+  float adjacency_penalty_weight = 0.3f;
+  bool enable_optimization = true;
+  int64_t optimization_iterations = 1000;
+  float color_adjustment_strength = 0.3f;
+  int tile_w = 0, tile_h = 0;  // 0 -> cell size
+  int chains = 1;
+  uint64_t seed = 0;
+  uint32_t stream = 0;
+  bool build_similarity = true;
+};
+
+struct MosaicOutput {
+  Grid grid;  // grid[y][x]: the material's path, or empty
+  RgbImage image;
+  int palette_size = 0, n_resets = 0;
+  OptimizationResult optimization;
+};
+
+// main.rs:105-164 (palette ingestion) + main.rs:477-685 (generate_mosaic) from
+// decoded images; materials[i] is named paths[i].  When no material survives
+// load_tiles every cell stays empty (main.rs:342-345 returns None per cell).
+inline MosaicOutput generate_mosaic(const RgbImageView& target, const std::vector<RgbImageView>& materials,
+                                                   const std::vector<Path>& paths, const MosaicOptions& o,
+                                                   const uint8_t* thumbnails = nullptr,
+                                                   Context& ctx = default_context()) {
+  if (materials.size() != paths.size()) throw Error(MG_ERR_ARG, "one path per material");
+  const int n = (int)materials.size();
+  std::vector<const uint8_t*> ptrs(n);
+  std::vector<int> w(n), h(n);
+  std::vector<int64_t> s(n);
+  for (int i = 0; i < n; ++i) {
+    ptrs[i] = materials[i].data;
+    w[i] = materials[i].width;
+    h[i] = materials[i].height;
+    s[i] = materials[i].row_bytes();
+  }
+  mg_request r;
+  mg_request_default(&r);
+  r.target = target.data;
+  r.target_w = target.width;
+  r.target_h = target.height;
+  r.target_stride = target.row_bytes();
+  r.n_materials = n;
+  r.materials = ptrs.data();
+  r.material_w = w.data();
+  r.material_h = h.data();
+  r.material_stride = s.data();
+  r.thumbnails = thumbnails;
+  r.tile_w = o.tile_w;
+  r.tile_h = o.tile_h;
+  r.grid_w = o.grid_w;
+  r.grid_h = o.grid_h;
+  r.max_materials = o.max_materials;
+  r.aspect_tolerance = o.aspect_tolerance;
+  r.max_usage_per_image = o.max_usage_per_image;
+  r.adjacency_penalty_weight = o.adjacency_penalty_weight;
+  r.color_adjustment_strength = o.color_adjustment_strength;
+  r.enable_optimization = o.enable_optimization ? 1 : 0;
+  r.optimization_iterations = o.optimization_iterations;
+  r.chains = o.chains;
+  r.seed = o.seed;
+  r.stream = o.stream;
+  r.build_similarity = o.build_similarity ? 1 : 0;
+  const int tw = o.tile_w ? o.tile_w : (o.grid_w > 0 ? target.width / o.grid_w : 0);
+  const int th = o.tile_h ? o.tile_h : (o.grid_h > 0 ? target.height / o.grid_h : 0);
+  std::vector<int32_t> grid((size_t)std::max(o.grid_w, 0) * std::max(o.grid_h, 0));
+  MosaicOutput out;
+  out.image.width = o.grid_w * tw;
+  out.image.height = o.grid_h * th;
+  out.image.pixels.resize((size_t)out.image.width * out.image.height * 3);
+  mg_result res{};
+  res.grid = grid.data();
+  res.image = out.image.pixels.data();
+  detail::check(mg_generate(ctx.get(), &r, &res));
+  out.palette_size = res.palette_size;
+  out.n_resets = res.n_resets;
+  out.optimization.initial_cost = res.initial_cost;
+  out.optimization.final_cost = res.final_cost;
+  out.optimization.best_cost = res.best_cost;
+  out.optimization.accepted_count = (size_t)res.accepted_count;
+  out.optimization.improved_count = (size_t)res.improved_count;
+  out.optimization.iterations = o.enable_optimization ? (size_t)o.optimization_iterations : 0;
+  out.grid.assign(o.grid_h, std::vector<std::optional<Path>>(o.grid_w));
+  for (int y = 0; y < o.grid_h; ++y)
+    for (int x = 0; x < o.grid_w; ++x) {
+      const int32_t i = grid[(size_t)y * o.grid_w + x];
+      if (i >= 0) out.grid[y][x] = paths[(size_t)i];
+    }
+  return out;
+}
+
+// ---- resident palette, batches, serving (no counterpart in the crate) -------------------------------
+class Palette {
+ public:
+  Palette(const std::vector<RgbImageView>& materials, const uint8_t* thumbnails, int tile_w, int tile_h,
+          float target_aspect, float aspect_tolerance = 0.1f, int max_materials = 0, bool build_similarity = true,
+          Context& ctx = default_context()) {
+    const int n = (int)materials.size();
+    std::vector<const uint8_t*> ptrs(n);
+    std::vector<int> w(n), h(n);
+    std::vector<int64_t> s(n);
+    for (int i = 0; i < n; ++i) {
+      ptrs[i] = materials[i].data;
+      w[i] = materials[i].width;
+      h[i] = materials[i].height;
+      s[i] = materials[i].row_bytes();
+    }
+    mg_palette_desc d;
+    mg_palette_desc_default(&d);
+    d.n_materials = n;
+    d.materials = ptrs.data();
+    d.material_w = w.data();
+    d.material_h = h.data();
+    d.material_stride = s.data();
+    d.thumbnails = thumbnails;
+    d.tile_w = tile_w;
+    d.tile_h = tile_h;
+    d.target_aspect = target_aspect;
+    d.aspect_tolerance = aspect_tolerance;
+    d.max_materials = max_materials ? max_materials : n;
+    d.build_similarity = build_similarity ? 1 : 0;
+    detail::check(mg_palette_create(ctx.get(), &d, &h_));
+  }
+  ~Palette() {
+    if (h_) mg_palette_destroy(h_);
+  }
+  Palette(const Palette&) = delete;
+  Palette& operator=(const Palette&) = delete;
+  mg_palette* get() const { return h_; }
+  int size() const { return mg_palette_size(h_); }
+
+ private:
+  mg_palette* h_ = nullptr;
+};
+
+class Server {
+ public:
+  Server(Palette& pal, int slots = 3, int max_batch = 64, int64_t memory_budget_bytes = 120ll << 30,
+         Context& ctx = default_context()) {
+    mg_server_config c;
+    mg_server_config_default(&c);
+    c.slots = slots;
+    c.max_batch = max_batch;
+    c.memory_budget_bytes = memory_budget_bytes;
+    detail::check(mg_server_create(ctx.get(), pal.get(), &c, &h_));
+  }
+  ~Server() {
+    if (h_) mg_server_destroy(h_);
+  }
+  Server(const Server&) = delete;
+  Server& operator=(const Server&) = delete;
+  // The target and outputs must stay valid until the request completes.
+  uint64_t submit(const mg_mosaic& m, int32_t* grid_out, uint8_t* image_out) {
+    uint64_t t = 0;
+    detail::check(mg_server_submit(h_, &m, grid_out, image_out, &t));
+    return t;
+  }
+  // Status (MG_OK or MG_ERR_BUDGET), the result summary and the latency in ms.
+  int wait(uint64_t ticket, mg_result* res, double* latency_ms) { return mg_server_wait(h_, ticket, res, latency_ms); }
+  mg_server_stats stats() const {
+    mg_server_stats s{};
+    detail::check(mg_server_get_stats(h_, &s));
+    return s;
+  }
+
+ private:
+  mg_server* h_ = nullptr;
+};
+
+}  // namespace mosaic
