@@ -8,28 +8,32 @@
 //
 // Two kernels:
 //  - greedy_kernel: one warp walks one mosaic (greedy_walk.cuh).  Used for
-//    palettes whose counters do not fit in shared memory and for grids narrower
-//    than 8 cells.
-//  - greedy_scout_kernel: one 16-warp CTA per mosaic.  The walk is a chain of
-//    dependent decisions, so its speed is the latency of one decision.  Warp 0
-//    (the walker) makes the decisions; twelve scout warps, on the other three
-//    SM sub-partitions, prepare each cell's decision ahead of the walker from a
-//    snapshot of the usage counters:
-//      e0', e1'  the first two candidates (list order) that pass the usage cap
-//                and differ from the cell above, in the snapshot;
-//      clear     whether no later such candidate lies inside the 2*weight
-//                window of e0' (resp. e1'), i.e. whether the penalty cannot
-//                change the decision.
-//    Counters only grow between resets, so a candidate that fails the cap in
-//    the snapshot still fails it when the walker arrives, and the walker's
-//    first eligible candidate is e0' if e0' still passes (fresh counter, left
-//    neighbour), else e1' if that passes.  With `clear` set that candidate is
-//    the reference's choice, bit for bit; in every other case (window not
-//    clear, both fail, no candidate, a reset since the snapshot) the walker
-//    evaluates the cell in full, exactly as greedy_walk does.  A scout reads
-//    the cell above only after the walker has committed it (acquire/release
-//    on a progress counter) and a reset bumps an epoch that invalidates older
-//    snapshots.  The walker's fast path is a few shared-memory loads per cell.
+//    palettes whose counters do not fit in shared memory, palettes above 65535
+//    materials and grids narrower than 8 cells.
+//  - greedy_pair_kernel: a cluster of two CTAs per mosaic.  The walk is a chain
+//    of dependent decisions, so its speed is the latency of one decision.  One
+//    warp of CTA 0 (the walker) makes the decisions; sixteen scout warps in
+//    CTA 1, on another SM, prepare each cell's decision ahead of the walker
+//    from a snapshot of the usage counters, reading the walk's state and
+//    writing their records through distributed shared memory:
+//      the first 32 candidates (list order) that differ from the cell above
+//      and were under the usage cap in the snapshot, and for each whether the
+//      next such candidate lies outside its 2*weight window (`clear`: then the
+//      penalty cannot change the decision if that candidate is the first
+//      eligible one); also the first 32 candidates regardless of the counters,
+//      for use after a reset.
+//    Counters only grow between resets, so a candidate that failed the cap in
+//    the snapshot still fails it when the walker arrives: the walker's first
+//    eligible candidate is the first record entry that passes the fresh
+//    counter and differs from the left neighbour -- one warp minimum -- and
+//    with its `clear` bit set it is the reference's choice, bit for bit.  In
+//    every other case (window not clear, no entry passes, a reset since the
+//    snapshot for the filtered list) the walker evaluates the cell in full,
+//    exactly as greedy_walk does.  A scout reads the cell above only after the
+//    walker has committed it (acquire/release on a progress counter) and a
+//    reset bumps an epoch that invalidates older snapshots.  After the walk
+//    the scout CTA computes calculate_total_cost: terms in parallel, one
+//    sequential FP32 sum in the reference's order.
 #include "greedy_walk.cuh"
 
 namespace mg {
@@ -47,11 +51,16 @@ __global__ void __launch_bounds__(32) greedy_kernel(const float4* __restrict__ p
 }
 
 // ---- the scouted walk -------------------------------------------------------------------
-constexpr int kScoutWarps = 16;  // warp 0 walks; warps w with w % 4 != 0 scout
-constexpr int kScouts = 12;
+// A cluster of two CTAs per mosaic.  CTA 0 walks (warp 0; the state of the
+// walk lives in its shared memory); CTA 1, on another SM, holds the scouts,
+// which read the walk's state and write their records through distributed
+// shared memory, so the walker's SM runs nothing but the walk.
+constexpr int kWarps = 16;   // per CTA
+constexpr int kScouts = 16;  // every warp of CTA 1
 constexpr uint32_t kInvalidEpoch = 0xFFFFFFFFu;
 constexpr uint32_t kWalkPolls = 1u << 24;
 constexpr uint32_t kScoutPolls = 1u << 24;
+constexpr int kCostChunk = 2048;  // cells per pass of the final cost sum
 enum Ctrl { kProgress = 0, kEpoch = 1, kAbort = 2 };
 
 // A cell's prepared decision: two candidate lists of up to 32 entries in list
@@ -60,18 +69,21 @@ enum Ctrl { kProgress = 0, kEpoch = 1, kAbort = 2 };
 //  f: the candidates under the usage cap in the scout's snapshot (valid while
 //     the epoch is unchanged);
 //  r: all candidates (valid in any epoch, used after a reset).
-// Entry i is the key (i << 16 | palette index), ~0 where the list is
-// shorter; the lowest key among eligible entries is the first eligible one.
-// clear_*: bit i set when no later entry of the list (nor anything beyond it)
-// lies inside the 2*weight window of entry i -- then, if entry i is the first
-// eligible one, the penalty cannot change the decision.  Palette indices are
-// 16-bit (palettes of at most 65535).
+// Entry i is the key (i << 17 | blocked << 16 | palette index), ~0 where the
+// list is shorter, so the lowest key among eligible entries is the first
+// eligible one.  `blocked` is clear when no later entry of the list (nor
+// anything beyond it) lies inside the 2*weight window of entry i -- then, if
+// entry i is the first eligible one, the penalty cannot change the decision.
+// Palette indices are 16-bit (palettes of at most 65535).
 struct __align__(16) CellRecord {
   uint32_t kf[32];
   uint32_t kr[32];
-  float df[32];
-  float dr[32];
-  uint32_t clear_f, clear_r, epoch, pad;
+  uint32_t epoch, pad[3];
+};
+// A scout's working copy of one record (in its own CTA).
+struct ScoutStage {
+  uint32_t kf[32], kr[32];
+  float df[32], dr[32];
 };
 
 // Records live in a ring.  A scout writes cell c's record once the walker has
@@ -79,18 +91,27 @@ struct __align__(16) CellRecord {
 // up to c - gw + 1; a ring of more than gw + 1 slots keeps that slot free.
 __host__ __device__ inline int ring_size(int gw) {
   int r = 32;
-  while (r < gw + kScouts + 4) r <<= 1;
+  while (r < gw + 4) r <<= 1;
   return r;
 }
 
-__host__ __device__ inline size_t scout_smem_bytes(int gw, int p, bool lab_smem) {
+// Shared memory of the walker CTA: control words, record ring, sequence
+// words, the row above, usage counters, optionally the palette Lab.
+__host__ __device__ inline size_t walker_smem_bytes(int gw, int p, bool lab_smem) {
   const int R = ring_size(gw);
-  size_t b = 16;                                    // control words
-  b += (size_t)R * sizeof(CellRecord) + (size_t)R * 4;  // records + sequence words
-  b += align16((size_t)gw * 4);                        // the row above
-  b += align16((size_t)p * 4);                         // usage counters
+  size_t b = 16 + (size_t)R * sizeof(CellRecord) + (size_t)R * 4;
+  b += align16((size_t)gw * 4);
+  b += align16((size_t)p * 4);
   if (lab_smem) b += (size_t)p * 16;
   return b;
+}
+// Shared memory of the scout CTA: staging per warp, then the cost terms.
+__host__ __device__ inline size_t scout_cta_smem_bytes() {
+  return (size_t)kWarps * sizeof(ScoutStage) + (size_t)kCostChunk * 8;
+}
+__host__ __device__ inline size_t pair_smem_bytes(int gw, int p, bool lab_smem) {
+  const size_t a = walker_smem_bytes(gw, p, lab_smem), b = scout_cta_smem_bytes();
+  return a > b ? a : b;
 }
 
 // The exact decision for one cell (greedy_walk's per-cell rule, candidate rows
@@ -176,20 +197,42 @@ __device__ int full_cell(LabFn lab, const uint32_t* __restrict__ ci, const float
       if (mask) t = __shfl_sync(0xffffffffu, tj, __ffs(mask) - 1);
     }
     if (t < 0) t = (int)__ldg(ci);
-    __threadfence_block();
+    fence_cluster();
     __syncwarp();
     ++epoch;
     if (lane == 0) {
       usage[t] = 1u;
-      st_release_cta(&ctrl[kEpoch], epoch);
+      st_release_cluster(smem_u32(&ctrl[kEpoch]), epoch);
     }
   }
   return t;
 }
 
-// A scout warp: prepares the records of cells s, s + 12, s + 24, ...
-__device__ void scout_cells(int s, const GreedyJob& J, int p, const uint32_t* usage, const int32_t* row,
-                            CellRecord* rec, uint32_t* seq, uint32_t* ctrl, int R, uint32_t* err) {
+// The walker CTA's shared-memory layout (both CTAs compute it; the scouts map
+// it into the walker CTA's window).
+struct WalkerLayout {
+  uint32_t* ctrl;
+  CellRecord* rec;
+  uint32_t* seq;
+  int32_t* row;
+  uint32_t* usage;
+  float4* lab;
+};
+__device__ inline WalkerLayout walker_layout(uint8_t* smem, int gw, int p, int R) {
+  WalkerLayout L;
+  L.ctrl = reinterpret_cast<uint32_t*>(smem);
+  L.rec = reinterpret_cast<CellRecord*>(smem + 16);
+  L.seq = reinterpret_cast<uint32_t*>(L.rec + R);
+  L.row = reinterpret_cast<int32_t*>(L.seq + R);
+  L.usage = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(L.row) + align16((size_t)gw * 4));
+  L.lab = reinterpret_cast<float4*>(reinterpret_cast<uint8_t*>(L.usage) + align16((size_t)p * 4));
+  return L;
+}
+
+// A scout warp (CTA 1): prepares the records of cells s, s + 16, s + 32, ...
+// Returns false when the walk was aborted.
+__device__ bool scout_cells(int s, const GreedyJob& J, int p, const WalkerLayout& L, ScoutStage& S, int R,
+                            uint32_t* err) {
   const int lane = threadIdx.x & 31;
   const int gw = J.gw, k = J.k, n = gw * J.gh;
   const uint32_t max_usage = J.max_usage;
@@ -198,6 +241,11 @@ __device__ void scout_cells(int s, const GreedyJob& J, int p, const uint32_t* us
   const int nr = (k + 31) >> 5;
   const float inf = __int_as_float(0x7f800000);
   const unsigned lt = (1u << lane) - 1u;
+  // the walker CTA's words, in the cluster window
+  const uint32_t r_progress = cluster_map(&L.ctrl[kProgress], 0), r_epoch = cluster_map(&L.ctrl[kEpoch], 0);
+  const uint32_t r_abort = cluster_map(&L.ctrl[kAbort], 0);
+  const uint32_t r_usage = cluster_map(L.usage, 0), r_row = cluster_map(L.row, 0);
+  const uint32_t r_rec = cluster_map(L.rec, 0), r_seq = cluster_map(L.seq, 0);
   for (int c = s; c < n; c += kScouts) {
     const int x = c % gw, y = c / gw;
     const uint32_t* ci = J.cand_idx + (size_t)c * k;
@@ -218,37 +266,36 @@ __device__ void scout_cells(int s, const GreedyJob& J, int p, const uint32_t* us
     if (y > 0) {
       const uint32_t need = (uint32_t)(c - gw + 1);
       uint32_t polls = 0;
-      while (ld_acquire_cta(&ctrl[kProgress]) < need) {
-        if (ld_volatile_u32(&ctrl[kAbort])) return;
+      while (ld_acquire_cluster(r_progress) < need) {
+        if (ld_cluster_u32(r_abort)) return false;
         if (++polls > kScoutPolls) {
           if (lane == 0) {
             atomicOr(err, kErrTimeout);
-            *reinterpret_cast<volatile uint32_t*>(&ctrl[kAbort]) = 1u;
+            st_cluster_u32(r_abort, 1u);
           }
-          return;
+          return false;
         }
-        __nanosleep(32);
+        __nanosleep(64);
       }
-      up = row[x];
+      up = (int)ld_cluster_u32(r_row + 4u * (uint32_t)x);
     }
-    CellRecord& Rc = rec[c & (R - 1)];
-    const uint32_t ep0 = ld_acquire_cta(&ctrl[kEpoch]);
+    const uint32_t ep0 = ld_acquire_cluster(r_epoch);
     int bf = 0, br = 0;
     float af = inf, ar = inf;  // distance of the 33rd entry
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       if (r < nr && (bf <= 32 || br <= 32)) {
         const bool in = t[r] < (uint32_t)p && (int)t[r] != up;
-        const bool okf = in && usage[t[r]] < max_usage;
+        const bool okf = in && ld_cluster_u32(r_usage + 4u * t[r]) < max_usage;
         const unsigned mf = __ballot_sync(0xffffffffu, okf), mr = __ballot_sync(0xffffffffu, in);
         const int pf = bf + __popc(mf & lt), pr = br + __popc(mr & lt);
         if (okf && pf < 32) {
-          Rc.kf[pf] = ((uint32_t)pf << 16) | t[r];
-          Rc.df[pf] = d[r];
+          S.kf[pf] = ((uint32_t)pf << 17) | t[r];
+          S.df[pf] = d[r];
         }
         if (in && pr < 32) {
-          Rc.kr[pr] = ((uint32_t)pr << 16) | t[r];
-          Rc.dr[pr] = d[r];
+          S.kr[pr] = ((uint32_t)pr << 17) | t[r];
+          S.dr[pr] = d[r];
         }
         const unsigned f32 = __ballot_sync(0xffffffffu, okf && pf == 32);
         const unsigned r32 = __ballot_sync(0xffffffffu, in && pr == 32);
@@ -258,58 +305,116 @@ __device__ void scout_cells(int s, const GreedyJob& J, int p, const uint32_t* us
         br += __popc(mr);
       }
     }
-    __threadfence_block();
-    const uint32_t ep1 = ld_volatile_u32(&ctrl[kEpoch]);
+    fence_cluster();
+    const uint32_t ep1 = ld_acquire_cluster(r_epoch);
     __syncwarp();
     const int cf = min(bf, 32), cr = min(br, 32);
     // static window test of entry `lane` against the next entry of its list
-    const float dfi = lane < cf ? Rc.df[lane] : inf, dfn = lane + 1 < cf ? Rc.df[lane + 1] : af;
-    const float dri = lane < cr ? Rc.dr[lane] : inf, drn = lane + 1 < cr ? Rc.dr[lane + 1] : ar;
-    const unsigned clear_f = __ballot_sync(0xffffffffu, lane < cf && (!use_pen || !(dfn < __fadd_rn(dfi, two_w))));
-    const unsigned clear_r = __ballot_sync(0xffffffffu, lane < cr && (!use_pen || !(drn < __fadd_rn(dri, two_w))));
-    if (lane >= cf) Rc.kf[lane] = 0xFFFFFFFFu;
-    if (lane >= cr) Rc.kr[lane] = 0xFFFFFFFFu;
-    if (lane == 0) {
-      Rc.clear_f = clear_f;
-      Rc.clear_r = clear_r;
-      Rc.epoch = ep0 == ep1 ? ep0 : kInvalidEpoch;
-    }
-    __threadfence_block();
+    const float dfi = lane < cf ? S.df[lane] : inf, dfn = lane + 1 < cf ? S.df[lane + 1] : af;
+    const float dri = lane < cr ? S.dr[lane] : inf, drn = lane + 1 < cr ? S.dr[lane + 1] : ar;
+    const bool blocked_f = use_pen && dfn < __fadd_rn(dfi, two_w);
+    const bool blocked_r = use_pen && drn < __fadd_rn(dri, two_w);
+    const uint32_t slot = (uint32_t)(c & (R - 1));
+    const uint32_t rr = r_rec + slot * (uint32_t)sizeof(CellRecord);
+    st_cluster_u32(rr + 4u * lane, lane < cf ? S.kf[lane] | (blocked_f ? 0x10000u : 0u) : 0xFFFFFFFFu);
+    st_cluster_u32(rr + 128u + 4u * lane, lane < cr ? S.kr[lane] | (blocked_r ? 0x10000u : 0u) : 0xFFFFFFFFu);
+    if (lane == 0) st_cluster_u32(rr + 256u, ep0 == ep1 ? ep0 : kInvalidEpoch);
+    fence_cluster();
     __syncwarp();
-    if (lane == 0) st_release_cta(&seq[c & (R - 1)], (uint32_t)(c + 1));
+    if (lane == 0) st_release_cluster(r_seq + 4u * slot, (uint32_t)(c + 1));
   }
+  return true;
 }
 
 template <bool kLabSmem>
-__global__ void __launch_bounds__(kScoutWarps * 32) greedy_scout_kernel(const float4* __restrict__ pal, int p,
-                                                                        const GreedyJob* __restrict__ jobs,
-                                                                        uint32_t* err) {
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
+    greedy_pair_kernel(const float4* __restrict__ pal, int p, const GreedyJob* __restrict__ jobs, uint32_t* err) {
   extern __shared__ __align__(128) uint8_t smem[];
-  const GreedyJob J = jobs[blockIdx.x];
+  const GreedyJob J = jobs[blockIdx.x >> 1];
+  const uint32_t rank = cluster_ctarank();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gw = J.gw, gh = J.gh, k = J.k, n = gw * gh;
   const int R = ring_size(gw);
-  uint32_t* ctrl = reinterpret_cast<uint32_t*>(smem);
-  CellRecord* rec = reinterpret_cast<CellRecord*>(smem + 16);
-  uint32_t* seq = reinterpret_cast<uint32_t*>(rec + R);
-  int32_t* row = reinterpret_cast<int32_t*>(seq + R);
-  uint32_t* usage = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(row) + align16((size_t)gw * 4));
-  float4* s_lab = reinterpret_cast<float4*>(reinterpret_cast<uint8_t*>(usage) + align16((size_t)p * 4));
-  for (int i = threadIdx.x; i < p; i += blockDim.x) {
-    usage[i] = 0;
-    if (kLabSmem) s_lab[i] = pal[i];
+  const WalkerLayout L = walker_layout(smem, gw, p, R);
+  if (rank == 0) {
+    for (int i = threadIdx.x; i < p; i += blockDim.x) {
+      L.usage[i] = 0;
+      if (kLabSmem) L.lab[i] = pal[i];
+    }
+    for (int i = threadIdx.x; i < R; i += blockDim.x) L.seq[i] = 0;
+    if (threadIdx.x < 4) L.ctrl[threadIdx.x] = 0;
   }
-  for (int i = threadIdx.x; i < R; i += blockDim.x) seq[i] = 0;
-  if (threadIdx.x < 4) ctrl[threadIdx.x] = 0;
-  __syncthreads();
+  cluster_sync_all();  // the walker CTA's state exists before any scout reads it
 
+  if (rank == 1) {
+    // ---- the scouts, then the final cost of the walk
+    ScoutStage* stage = reinterpret_cast<ScoutStage*>(smem);
+    float* terms = reinterpret_cast<float*>(smem + (size_t)kWarps * sizeof(ScoutStage));
+    bool ok = scout_cells(warp, J, p, L, stage[warp], R, err);
+    // calculate_total_cost (adjacency.rs:91-130) of the placed grid once the
+    // walk is complete: terms in parallel, one sequential FP32 sum in the
+    // reference's order (right then down, row-major).
+    __shared__ uint32_t s_ok;
+    if (threadIdx.x == 0) s_ok = 1u;
+    __syncthreads();
+    if (!ok) s_ok = 0u;
+    __syncthreads();
+    if (threadIdx.x == 0 && s_ok) {
+      const uint32_t r_progress = cluster_map(&L.ctrl[kProgress], 0), r_abort = cluster_map(&L.ctrl[kAbort], 0);
+      uint32_t polls = 0;
+      while (ld_acquire_cluster(r_progress) < (uint32_t)n) {
+        if (ld_cluster_u32(r_abort) || ++polls > kScoutPolls) {
+          s_ok = 0u;
+          break;
+        }
+        __nanosleep(256);
+      }
+    }
+    __syncthreads();
+    if (s_ok) {
+      float total = 0.0f;
+      for (int c0 = 0; c0 < n; c0 += kCostChunk) {
+        const int m = min(kCostChunk, n - c0);
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+          const int c = c0 + i, x = c % gw, y = c / gw;
+          const int cur = J.grid[c];
+          float tr = 0.0f, td = 0.0f;
+          if (cur >= 0) {
+            const float4 lc = __ldg(pal + cur);
+            if (x < gw - 1) {
+              const int r = J.grid[c + 1];
+              if (r >= 0) tr = wgt(lc, __ldg(pal + r));
+            }
+            if (y < gh - 1) {
+              const int d = J.grid[c + gw];
+              if (d >= 0) td = wgt(lc, __ldg(pal + d));
+            }
+          }
+          terms[2 * i] = tr;
+          terms[2 * i + 1] = td;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+          for (int i = 0; i < 2 * m; ++i) total = __fadd_rn(total, terms[i]);
+        __syncthreads();
+      }
+      if (threadIdx.x == 0 && J.total_cost) *J.total_cost = total;
+    }
+    cluster_sync_all();
+    return;
+  }
   if (warp != 0) {
-    if ((warp & 3) == 0) return;  // shares the walker's sub-partition
-    scout_cells((warp >> 2) * 3 + (warp & 3) - 1, J, p, usage, row, rec, seq, ctrl, R, err);
+    cluster_sync_all();
     return;
   }
 
-  // ---- warp 0: the walker
+  // ---- CTA 0, warp 0: the walker
+  uint32_t* ctrl = L.ctrl;
+  CellRecord* rec = L.rec;
+  uint32_t* seq = L.seq;
+  int32_t* row = L.row;
+  uint32_t* usage = L.usage;
+  const float4* s_lab = L.lab;
   const uint32_t max_usage = J.max_usage;
   const float weight = J.weight;
   auto lab = [=](int i) -> float4 { return kLabSmem ? s_lab[i] : __ldg(pal + i); };
@@ -318,17 +423,17 @@ __global__ void __launch_bounds__(kScoutWarps * 32) greedy_scout_kernel(const fl
   int ready_until = 0;  // records of cells [.., ready_until) are published
   bool aborted = false;
   // Whether the record of cell c is published.  Records [0, ready_until) are
-  // known to be; a probe checks the next eight (lane i acquires the sequence
-  // word of cell ready_until + i).  With `block` it waits (bounded).
+  // known to be; a probe checks the next 32 (lane i acquires the sequence word
+  // of cell ready_until + i).  With `block` it waits (bounded).
   auto ready = [&](int c, bool block) -> bool {
     if (c < ready_until) return true;
     uint32_t polls = 0;
     for (;;) {
       const int base = ready_until;
-      const int cc = base + (lane & 7);
-      const bool mine = lane >= 8 || cc >= n || ld_acquire_cta(&seq[cc & (R - 1)]) == (uint32_t)(cc + 1);
+      const int cc = base + lane;
+      const bool mine = cc >= n || ld_acquire_cluster(smem_u32(&seq[cc & (R - 1)])) == (uint32_t)(cc + 1);
       const unsigned pending = __ballot_sync(0xffffffffu, !mine);
-      const int nready = pending ? __ffs(pending) - 1 : 8;
+      const int nready = pending ? __ffs(pending) - 1 : 32;
       if (nready > 0) {
         ready_until = min(n, base + nready);
         __syncwarp();  // the acquiring lanes' view reaches every lane
@@ -342,69 +447,62 @@ __global__ void __launch_bounds__(kScoutWarps * 32) greedy_scout_kernel(const fl
     }
   };
   // The walk is a chain of dependent decisions; per cell the critical path is
-  // the eligibility test, one warp minimum and the clear bit.  Record reads are
+  // the eligibility test, one warp minimum and a flag test.  Record reads are
   // software-pipelined around it: the header of cell c + 2 and the counters of
-  // cell c + 1 are read while cell c is decided, and everything uncommon (the
-  // full evaluation, row ends, progress releases, records not yet published)
-  // sits behind one branch.
+  // cell c + 1 are read while cell c is decided, unconditionally (a record not
+  // yet published is read again once it is), and everything uncommon (the
+  // full evaluation, row ends, progress releases, late records) sits behind
+  // one branch.  Progress is released every `rel` cells (a power of two, at
+  // most half a row: a scout waiting for the cell above never waits on the
+  // walker's own wait).
   struct Head {
-    uint32_t ep, kf, kr, cf, cr;
+    uint32_t ep, kf, kr;
   };
   struct Cur {
-    uint32_t key, ti, ui, clear;
+    uint32_t key, ti, ui;
   };
   auto load_head = [&](int c) {
     const CellRecord& Rc = rec[c & (R - 1)];
-    Head h;
-    h.ep = Rc.epoch;
-    h.kf = Rc.kf[lane];
-    h.kr = Rc.kr[lane];
-    h.cf = Rc.clear_f;
-    h.cr = Rc.clear_r;
-    return h;
+    return Head{Rc.epoch, Rc.kf[lane], Rc.kr[lane]};
   };
   auto finish = [&](const Head& h) {
-    const bool f = h.ep == epoch;
     Cur r;
-    r.key = f ? h.kf : h.kr;
-    r.clear = f ? h.cf : h.cr;
+    r.key = h.ep == epoch ? h.kf : h.kr;
     r.ti = r.key & 0xFFFFu;
-    r.ui = r.key != 0xFFFFFFFFu ? usage[r.ti] : 0xFFFFFFFFu;
+    r.ui = (r.key != 0xFFFFFFFFu && r.ti < (uint32_t)p) ? usage[r.ti] : 0xFFFFFFFFu;
     return r;
   };
-  Cur cur{0xFFFFFFFFu, 0u, 0xFFFFFFFFu, 0u};
-  Head h1{};
+  int rel = 4;
+  while (rel * 4 <= gw && rel < 32) rel <<= 1;
+  Cur cur{0xFFFFFFFFu, 0u, 0xFFFFFFFFu};
+  Head h1{0u, 0xFFFFFFFFu, 0xFFFFFFFFu};
   bool h1_ok = false;
   if (n > 0 && ready(0, true)) {
     cur = finish(load_head(0));
     h1_ok = n > 1 && ready(1, false);
-    if (h1_ok) h1 = load_head(1);
+    h1 = load_head(1 < n ? 1 : 0);
   }
+  int next_event = min(n - 1, min(gw - 1, rel - 1));  // the next row end or release point
   for (int c = 0; c < n && !aborted; ++c) {
-    // (a) header of cell c + 2, if published (waiting here, before this
-    // cell's progress release, could wait on a scout that waits on this cell)
-    Head h2{};
+    // (a) header of cell c + 2 (waiting here, before this cell's progress
+    // release, could wait on a scout that waits on this cell)
     const bool h2_ok = c + 2 < n && ready(c + 2, false);
-    if (h2_ok) h2 = load_head(c + 2);
+    const Head h2 = load_head(c + 2);
     // (b) counters of cell c + 1, read before this cell's commit: the choice
     // made here is that cell's left neighbour (row starts are re-read below)
-    Cur nxt = cur;
-    if (h1_ok) nxt = finish(h1);
+    Cur nxt = finish(h1);
     // (c) this cell: the lowest key among entries that pass the counters and
     // the left neighbour (the lists already exclude the cell above)
     const int left = x > 0 ? last : -1;
     const bool ok = cur.ui < max_usage && cur.ti != (uint32_t)left;
     const uint32_t best = __reduce_min_sync(0xffffffffu, ok ? cur.key : 0xFFFFFFFFu);
-    const int e = (int)(best >> 16);
-    const bool fast = best != 0xFFFFFFFFu && ((cur.clear >> (e & 31)) & 1u);
+    const bool fast = best != 0xFFFFFFFFu && !(best & 0x10000u);  // found, window clear
     int t = (int)(best & 0xFFFFu);
-    if (fast && lane == e) {
+    if (fast && lane == (int)(best >> 17)) {
       usage[cur.ti] = cur.ui + 1u;
       row[x] = t;
     }
-    const bool row_end = x + 1 == gw;
-    const bool rare = !fast || row_end || ((c + 1) & 7) == 0 || c + 1 == n || !h1_ok;
-    if (rare) {
+    if (!fast || c == next_event || !h1_ok) {
       if (!fast) {
         const int up = y > 0 ? row[x] : -1;
         t = full_cell(lab, J.cand_idx + (size_t)c * k, J.cand_dist + (size_t)c * k, k, p, up, left, usage,
@@ -412,19 +510,25 @@ __global__ void __launch_bounds__(kScoutWarps * 32) greedy_scout_kernel(const fl
         if (lane == 0) row[x] = t;
       }
       __syncwarp();
-      if (row_end) {
-        // the finished row goes to global memory in one coalesced pass
-        for (int i = lane; i < gw; i += 32) J.grid[(size_t)y * gw + i] = row[i];
+      if (c == next_event) {
+        if (x + 1 == gw) {
+          // the finished row goes to global memory in one coalesced pass
+          for (int i = lane; i < gw; i += 32) J.grid[(size_t)y * gw + i] = row[i];
+          __syncwarp();  // ordered before the progress release below
+        }
+        if (lane == 0 && (((c + 1) & (rel - 1)) == 0 || c + 1 == n))
+          st_release_cluster(smem_u32(&ctrl[kProgress]), (uint32_t)(c + 1));
+        // the next row end or release point after this cell
+        next_event = min(n - 1, min(((c + 1) / gw) * gw + gw - 1, (c + 1) | (rel - 1)));
       }
-      if (lane == 0 && (((c + 1) & 7) == 0 || c + 1 == n)) st_release_cta(&ctrl[kProgress], (uint32_t)(c + 1));
       if (c + 1 < n) {
         if (!h1_ok) {
           h1_ok = ready(c + 1, true);
-          if (h1_ok) h1 = load_head(c + 1);
+          h1 = load_head(c + 1);
         }
         // the counters moved (a full evaluation), or the next cell starts a row
         // and may take this cell's choice, or its record came late: read afresh
-        if (h1_ok) nxt = finish(h1);
+        nxt = finish(h1);
       }
     } else {
       __syncwarp();
@@ -443,14 +547,10 @@ __global__ void __launch_bounds__(kScoutWarps * 32) greedy_scout_kernel(const fl
       atomicOr(err, kErrTimeout);
       *reinterpret_cast<volatile uint32_t*>(&ctrl[kAbort]) = 1u;
     }
-    return;
+  } else if (lane == 0 && J.n_resets) {
+    *J.n_resets = resets;
   }
-  __syncwarp();
-  const float total = warp_total_cost(lab, J.grid, gw, gh, lane);
-  if (lane == 0) {
-    if (J.n_resets) *J.n_resets = resets;
-    if (J.total_cost) *J.total_cost = total;
-  }
+  cluster_sync_all();  // the scouts are done with this CTA's shared memory
 }
 
 }  // namespace
@@ -471,20 +571,20 @@ int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_job
     MG_CUDA(cudaFuncSetAttribute(greedy_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
     MG_CUDA(cudaFuncSetAttribute(greedy_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
     MG_CUDA(cudaFuncSetAttribute(greedy_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
-    MG_CUDA(cudaFuncSetAttribute(greedy_scout_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
-    MG_CUDA(cudaFuncSetAttribute(greedy_scout_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
     configured_device = dev;
   }
   // The scouted walk: counters in shared memory, 16-bit palette indices, rows
   // of at least 8 cells.
   if (max_gw >= 8 && p <= 65535) {
-    bool lab_smem = scout_smem_bytes(max_gw, p, true) <= kMaxSmem;
-    const size_t bytes = scout_smem_bytes(max_gw, p, lab_smem);
+    bool lab_smem = pair_smem_bytes(max_gw, p, true) <= kMaxSmem;
+    const size_t bytes = pair_smem_bytes(max_gw, p, lab_smem);
     if (bytes <= kMaxSmem) {
       if (lab_smem)
-        greedy_scout_kernel<true><<<n_jobs, kScoutWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
+        greedy_pair_kernel<true><<<2 * n_jobs, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
       else
-        greedy_scout_kernel<false><<<n_jobs, kScoutWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
+        greedy_pair_kernel<false><<<2 * n_jobs, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
       g_launches += 1;
       MG_CUDA(cudaGetLastError());
       return MG_OK;
