@@ -1,12 +1,24 @@
-// k_anneal.cu -- (e) the standalone annealing kernel (one warp per chain; the
-// chain itself is anneal_chain.cuh) and the batched adjacency evaluators of the
+// k_anneal.cu -- (e) the standalone annealing kernels (one CTA per chain,
+// anneal_cta.cuh; or one warp per chain, anneal_chain.cuh, for grids whose
+// state does not fit beside the CTA's round buffers) and the batched adjacency evaluators of the
 // C ABI (adjacency.rs:63-214), one thread per item, the reference's loops
 // verbatim.
-#include "anneal_chain.cuh"
+#include "anneal_cta.cuh"
 
 namespace mg {
 namespace {
 using namespace anneal_detail;
+
+template <bool kLabSmem>
+__global__ void __launch_bounds__(anneal_cta_detail::kThreads)
+    anneal_cta_kernel(const float4* __restrict__ pal, int p, const AnnealJob* __restrict__ jobs,
+                      const int* __restrict__ chain_job, const int* __restrict__ chain_id) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int jid = chain_job ? chain_job[blockIdx.x] : 0;
+  const int chain = chain_id ? chain_id[blockIdx.x] : (int)blockIdx.x;
+  const AnnealJob J = jobs[jid];
+  anneal_cta_detail::anneal_chain_cta<kLabSmem>(pal, p, J, chain, smem);
+}
 
 template <bool kLabSmem>
 __global__ void __launch_bounds__(32) anneal_kernel(const float4* __restrict__ pal, int p,
@@ -144,7 +156,25 @@ int launch_anneal(const float4* pal, int p, const AnnealJob* jobs_dev, const int
   if (configured_device != dev) {
     MG_CUDA(cudaFuncSetAttribute(anneal_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
     MG_CUDA(cudaFuncSetAttribute(anneal_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    MG_CUDA(cudaFuncSetAttribute(anneal_cta_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    MG_CUDA(cudaFuncSetAttribute(anneal_cta_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
     configured_device = dev;
+  }
+  // A CTA of several warps per chain (more proposals per round) when it fits.
+  {
+    using anneal_cta_detail::anneal_cta_smem_bytes;
+    const size_t with_lab = anneal_cta_smem_bytes(max_cells, p, true), no_lab = anneal_cta_smem_bytes(max_cells, p, false);
+    if (with_lab <= kMaxSmem || no_lab <= kMaxSmem) {
+      if (with_lab <= kMaxSmem)
+        anneal_cta_kernel<true><<<total_chains, anneal_cta_detail::kThreads, with_lab, stream>>>(
+            pal, p, jobs_dev, chain_job_dev, chain_id_dev);
+      else
+        anneal_cta_kernel<false><<<total_chains, anneal_cta_detail::kThreads, no_lab, stream>>>(
+            pal, p, jobs_dev, chain_job_dev, chain_id_dev);
+      g_launches += 1;
+      MG_CUDA(cudaGetLastError());
+      return MG_OK;
+    }
   }
   if (grid_bytes + lab_bytes <= kMaxSmem)
     anneal_kernel<true><<<total_chains, 32, grid_bytes + lab_bytes, stream>>>(pal, p, jobs_dev, chain_job_dev, chain_id_dev);
