@@ -126,47 +126,34 @@ __device__ __forceinline__ void anneal_chain_cta(const float4* __restrict__ pal,
       __syncthreads();
     }
     // ---- 1. evaluate proposal it + q_mine ------------------------------------------------
+    // Branch-free: every lane of a group computes two weights on clamped
+    // operands and keeps what its slot needs (lanes 0-3: neighbours of pos1 in
+    // up, down, left, right order; 4-7: those of pos2).
     const long long i = it + q_mine;
     const bool live = i < iters;
-    int4 e = make_int4(0, 0, 0, 0);
-    if (live) e = s_ring[i & (kCtaRing - 1)];
+    const int4 e = s_ring[(live ? i : it) & (kCtaRing - 1)];
     const int x1 = e.x & 0xFFFF, y1 = (e.x >> 16) & 0xFFFF, x2 = e.y & 0xFFFF, y2 = (e.y >> 16) & 0xFFFF;
     const int p1 = y1 * gw + x1, p2 = y2 * gw + x2;
-    bool skip = !live || p1 == p2;
-    uint16_t g1 = 0, g2 = 0;
-    if (!skip) {
-      g1 = s_grid[p1];
-      g2 = s_grid[p2];
-      skip = g1 == kNone16 || g2 == kNone16;
-    }
+    const uint16_t g1 = s_grid[p1], g2 = s_grid[p2];
+    const bool skip = !live || p1 == p2 || g1 == kNone16 || g2 == kNone16;
     const bool same = g1 == g2;
-    float o = 0.0f, nw = 0.0f, m = 0.0f;
-    if (!skip && !same) {
-      const bool first = slot < 4;
-      const int bx = first ? x1 : x2, by = first ? y1 : y2;
-      const int other = first ? p2 : p1;
-      const int dir = slot & 3;
-      int nx = bx, ny = by;
-      bool inb;
-      if (dir == 0) { ny = by - 1; inb = by > 0; }
-      else if (dir == 1) { ny = by + 1; inb = by < gh - 1; }
-      else if (dir == 2) { nx = bx - 1; inb = bx > 0; }
-      else { nx = bx + 1; inb = bx < gw - 1; }
-      if (inb) {
-        const int nb = ny * gw + nx;
-        if (nb == other) {
-          if (first) m = wgt(lab(g1), lab(g2));
-        } else {
-          const uint16_t a = s_grid[nb];
-          if (a != kNone16) {
-            const float4 la = lab(a);
-            const float w1 = wgt(lab(g1), la), w2 = wgt(lab(g2), la);
-            o = first ? w1 : w2;
-            nw = first ? w2 : w1;
-          }
-        }
-      }
-    }
+    const bool first = slot < 4;
+    const int dir = slot & 3;
+    const int bx = first ? x1 : x2, by = first ? y1 : y2;
+    const int nx = bx + (dir == 2 ? -1 : (dir == 3 ? 1 : 0)), ny = by + (dir == 0 ? -1 : (dir == 1 ? 1 : 0));
+    const bool inb = nx >= 0 && nx < gw && ny >= 0 && ny < gh;
+    const int nb = inb ? ny * gw + nx : p1;
+    const bool mutual = inb && nb == (first ? p2 : p1);
+    const uint16_t an = s_grid[nb];
+    const bool work = !skip && !same && inb;
+    const bool nbr = work && !mutual && an != kNone16;  // a placed neighbour
+    const uint16_t gs1 = skip ? (uint16_t)0 : g1, gs2 = skip ? (uint16_t)0 : g2;
+    const uint16_t c_idx = mutual ? gs2 : (an != kNone16 ? an : gs1);
+    const float4 la1 = lab(gs1), la2 = lab(gs2), lc = lab(c_idx);
+    const float w1 = wgt(la1, lc), w2 = wgt(la2, lc);
+    const float o = nbr ? (first ? w1 : w2) : 0.0f;
+    const float nw = nbr ? (first ? w2 : w1) : 0.0f;
+    const float m = (work && mutual && first) ? w1 : 0.0f;
     float old_cost = 0.0f, new_cost = 0.0f;
 #pragma unroll
     for (int t = 0; t < 8; ++t) {
@@ -220,16 +207,19 @@ __device__ __forceinline__ void anneal_chain_cta(const float4* __restrict__ pal,
     }
     const unsigned acc_mask = __ballot_sync(0xffffffffu, lane < kRound && acc_q);
     // proposal q reads a cell within distance 1 of an earlier accepted swap?
-    auto near = [](uint32_t a, uint32_t b) {
-      return abs((int)(a & 0xFFFFu) - (int)(b & 0xFFFFu)) + abs((int)(a >> 16) - (int)(b >> 16)) <= 1;
-    };
-    bool conf = false;
+    // (branch-free: Manhattan distances of the four position pairs)
+    const int qx1 = (int)(rq.pos1 & 0xFFFFu), qy1 = (int)(rq.pos1 >> 16);
+    const int qx2 = (int)(rq.pos2 & 0xFFFFu), qy2 = (int)(rq.pos2 >> 16);
+    unsigned conf_bits = 0u;
 #pragma unroll
     for (int h = 0; h < kRound - 1; ++h) {
       const uint32_t hp1 = __shfl_sync(0xffffffffu, rq.pos1, h), hp2 = __shfl_sync(0xffffffffu, rq.pos2, h);
-      const bool hit = near(hp1, rq.pos1) || near(hp1, rq.pos2) || near(hp2, rq.pos1) || near(hp2, rq.pos2);
-      conf = conf || (h < q && ((acc_mask >> h) & 1u) && hit);
+      const int hx1 = (int)(hp1 & 0xFFFFu), hy1 = (int)(hp1 >> 16), hx2 = (int)(hp2 & 0xFFFFu), hy2 = (int)(hp2 >> 16);
+      const unsigned hit = (unsigned)(abs(hx1 - qx1) + abs(hy1 - qy1) <= 1) | (unsigned)(abs(hx1 - qx2) + abs(hy1 - qy2) <= 1) |
+                           (unsigned)(abs(hx2 - qx1) + abs(hy2 - qy1) <= 1) | (unsigned)(abs(hx2 - qx2) + abs(hy2 - qy2) <= 1);
+      conf_bits |= hit & (acc_mask >> h) & (unsigned)(h < q);
     }
+    const bool conf = (conf_bits & 1u) != 0u;
     const unsigned cmask = __ballot_sync(0xffffffffu, lane < kRound && !skip_q && conf);
     const int gc = cmask ? __ffs(cmask) - 1 : kRound;  // >= 1: proposal 0 never conflicts
     const int ncommit = (int)min((long long)gc, iters - it);
