@@ -496,8 +496,8 @@ int mg_place_greedy(mg_ctx* ctx, const float* palette_lab, int p, const float* c
   GreedyJob job{ctx->out0.as<uint32_t>(), ctx->out1.as<float>(), d_grid, gw, gh, k,
                 (uint32_t)cfg->max_usage_per_image, cfg->adjacency_penalty_weight, d_resets, nullptr};
   MG_CHECK(upload(ctx, ctx->regions, &job, sizeof(job)));
-  MG_CHECK(launch_greedy(ctx->in0.as<float4>(), p, ctx->regions.as<GreedyJob>(), 1, k, gw, ctx->sums.as<uint32_t>(),
-                         ctx->err.as<uint32_t>(), ctx->stream));
+  MG_CHECK(launch_greedy(ctx->in0.as<float4>(), p, ctx->regions.as<GreedyJob>(), 1, k, gw, n,
+                         ctx->sums.as<uint32_t>(), ctx->err.as<uint32_t>(), ctx->stream));
   MG_CUDA(cudaMemcpyAsync(grid_out, d_grid, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
   int resets = 0;
   MG_CUDA(cudaMemcpyAsync(&resets, d_resets, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -922,7 +922,7 @@ int plan_run(mg_plan* pl) {
   MG_CUDA(cudaEventRecord(pl->ev[4], s));
   // [4] greedy placement
   if (P > 0) {
-    MG_CHECK(launch_greedy(pl->pal_lab.as<float4>(), P, pl->greedy_job.as<GreedyJob>(), 1, pl->k, pl->gw,
+    MG_CHECK(launch_greedy(pl->pal_lab.as<float4>(), P, pl->greedy_job.as<GreedyJob>(), 1, pl->k, pl->gw, N,
                            pl->usage.as<uint32_t>(), pl->err.as<uint32_t>(), s));
   } else {
     MG_CUDA(cudaMemsetAsync(pl->grid_greedy.p, 0xFF, sizeof(int32_t) * N, s));

@@ -12,7 +12,7 @@
 //    materials and grids narrower than 8 cells.
 //  - greedy_pair_kernel: a cluster of two CTAs per mosaic.  The walk is a chain
 //    of dependent decisions, so its speed is the latency of one decision.  One
-//    warp of CTA 0 (the walker) makes the decisions; sixteen scout warps in
+//    warp of CTA 0 (the walker) makes the decisions; 32 scout warps in
 //    CTA 1, on another SM, prepare each cell's decision ahead of the walker
 //    from a snapshot of the usage counters, reading the walk's state and
 //    writing their records through distributed shared memory:
@@ -55,8 +55,8 @@ __global__ void __launch_bounds__(32) greedy_kernel(const float4* __restrict__ p
 // walk lives in its shared memory); CTA 1, on another SM, holds the scouts,
 // which read the walk's state and write their records through distributed
 // shared memory, so the walker's SM runs nothing but the walk.
-constexpr int kWarps = 16;   // per CTA
-constexpr int kScouts = 16;  // every warp of CTA 1
+constexpr int kWarps = 32;   // per CTA
+constexpr int kScouts = 32;  // every warp of CTA 1
 constexpr uint32_t kInvalidEpoch = 0xFFFFFFFFu;
 constexpr uint32_t kWalkPolls = 1u << 24;
 constexpr uint32_t kScoutPolls = 1u << 24;
@@ -87,8 +87,8 @@ struct ScoutStage {
 };
 
 // Records live in a ring.  A scout writes cell c's record once the walker has
-// committed the cell above (c - gw), so the walker is done with every record
-// up to c - gw + 1; a ring of more than gw + 1 slots keeps that slot free.
+// placed the cell above (c - gw), so the walker is done with every record up
+// to c - gw + 2; a ring of more than gw + 2 slots keeps that slot free.
 __host__ __device__ inline int ring_size(int gw) {
   int r = 32;
   while (r < gw + 4) r <<= 1;
@@ -96,11 +96,13 @@ __host__ __device__ inline int ring_size(int gw) {
 }
 
 // Shared memory of the walker CTA: control words, record ring, sequence
-// words, the row above, usage counters, optionally the palette Lab.
-__host__ __device__ inline size_t walker_smem_bytes(int gw, int p, bool lab_smem) {
+// words, the placed grid (16-bit, kUnplaced until placed), usage counters,
+// optionally the palette Lab.
+constexpr uint16_t kUnplaced = 0xFFFFu;
+__host__ __device__ inline size_t walker_smem_bytes(int gw, int n, int p, bool lab_smem) {
   const int R = ring_size(gw);
   size_t b = 16 + (size_t)R * sizeof(CellRecord) + (size_t)R * 4;
-  b += align16((size_t)gw * 4);
+  b += align16((size_t)n * 2);
   b += align16((size_t)p * 4);
   if (lab_smem) b += (size_t)p * 16;
   return b;
@@ -109,8 +111,8 @@ __host__ __device__ inline size_t walker_smem_bytes(int gw, int p, bool lab_smem
 __host__ __device__ inline size_t scout_cta_smem_bytes() {
   return (size_t)kWarps * sizeof(ScoutStage) + (size_t)kCostChunk * 8;
 }
-__host__ __device__ inline size_t pair_smem_bytes(int gw, int p, bool lab_smem) {
-  const size_t a = walker_smem_bytes(gw, p, lab_smem), b = scout_cta_smem_bytes();
+__host__ __device__ inline size_t pair_smem_bytes(int gw, int n, int p, bool lab_smem) {
+  const size_t a = walker_smem_bytes(gw, n, p, lab_smem), b = scout_cta_smem_bytes();
   return a > b ? a : b;
 }
 
@@ -214,22 +216,22 @@ struct WalkerLayout {
   uint32_t* ctrl;
   CellRecord* rec;
   uint32_t* seq;
-  int32_t* row;
+  uint16_t* cells;
   uint32_t* usage;
   float4* lab;
 };
-__device__ inline WalkerLayout walker_layout(uint8_t* smem, int gw, int p, int R) {
+__device__ inline WalkerLayout walker_layout(uint8_t* smem, int n, int p, int R) {
   WalkerLayout L;
   L.ctrl = reinterpret_cast<uint32_t*>(smem);
   L.rec = reinterpret_cast<CellRecord*>(smem + 16);
   L.seq = reinterpret_cast<uint32_t*>(L.rec + R);
-  L.row = reinterpret_cast<int32_t*>(L.seq + R);
-  L.usage = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(L.row) + align16((size_t)gw * 4));
+  L.cells = reinterpret_cast<uint16_t*>(L.seq + R);
+  L.usage = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(L.cells) + align16((size_t)n * 2));
   L.lab = reinterpret_cast<float4*>(reinterpret_cast<uint8_t*>(L.usage) + align16((size_t)p * 4));
   return L;
 }
 
-// A scout warp (CTA 1): prepares the records of cells s, s + 16, s + 32, ...
+// A scout warp (CTA 1): prepares the records of cells s, s + 32, s + 64, ...
 // Returns false when the walk was aborted.
 __device__ bool scout_cells(int s, const GreedyJob& J, int p, const WalkerLayout& L, ScoutStage& S, int R,
                             uint32_t* err) {
@@ -242,12 +244,11 @@ __device__ bool scout_cells(int s, const GreedyJob& J, int p, const WalkerLayout
   const float inf = __int_as_float(0x7f800000);
   const unsigned lt = (1u << lane) - 1u;
   // the walker CTA's words, in the cluster window
-  const uint32_t r_progress = cluster_map(&L.ctrl[kProgress], 0), r_epoch = cluster_map(&L.ctrl[kEpoch], 0);
-  const uint32_t r_abort = cluster_map(&L.ctrl[kAbort], 0);
-  const uint32_t r_usage = cluster_map(L.usage, 0), r_row = cluster_map(L.row, 0);
+  const uint32_t r_epoch = cluster_map(&L.ctrl[kEpoch], 0), r_abort = cluster_map(&L.ctrl[kAbort], 0);
+  const uint32_t r_usage = cluster_map(L.usage, 0), r_cells = cluster_map(L.cells, 0);
   const uint32_t r_rec = cluster_map(L.rec, 0), r_seq = cluster_map(L.seq, 0);
   for (int c = s; c < n; c += kScouts) {
-    const int x = c % gw, y = c / gw;
+    const int y = c / gw;
     const uint32_t* ci = J.cand_idx + (size_t)c * k;
     const float* cd = J.cand_dist + (size_t)c * k;
     uint32_t t[4];
@@ -262,11 +263,16 @@ __device__ bool scout_cells(int s, const GreedyJob& J, int p, const WalkerLayout
         d[r] = __ldg(cd + j);
       }
     }
+    // The cell above, once placed.  Each cell is written once, by a single
+    // 16-bit store, so a scout that sees a value sees the final one; and the
+    // walker read that cell's record before placing it (the placement depends
+    // on it), so the walker is done with the ring slot this record reuses.
     int up = -1;
     if (y > 0) {
-      const uint32_t need = (uint32_t)(c - gw + 1);
+      const uint32_t a_up = r_cells + 2u * (uint32_t)(c - gw);
       uint32_t polls = 0;
-      while (ld_acquire_cluster(r_progress) < need) {
+      uint32_t v;
+      while ((v = ld_cluster_u16(a_up)) == kUnplaced) {
         if (ld_cluster_u32(r_abort)) return false;
         if (++polls > kScoutPolls) {
           if (lane == 0) {
@@ -277,16 +283,23 @@ __device__ bool scout_cells(int s, const GreedyJob& J, int p, const WalkerLayout
         }
         __nanosleep(64);
       }
-      up = (int)ld_cluster_u32(r_row + 4u * (uint32_t)x);
+      up = (int)v;
     }
     const uint32_t ep0 = ld_acquire_cluster(r_epoch);
+    // every counter the lists may need, in one round trip
+    uint32_t u[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const bool in = r < nr && t[r] < (uint32_t)p && (int)t[r] != up;
+      u[r] = in ? ld_cluster_u32(r_usage + 4u * t[r]) : 0xFFFFFFFFu;
+    }
     int bf = 0, br = 0;
     float af = inf, ar = inf;  // distance of the 33rd entry
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       if (r < nr && (bf <= 32 || br <= 32)) {
         const bool in = t[r] < (uint32_t)p && (int)t[r] != up;
-        const bool okf = in && ld_cluster_u32(r_usage + 4u * t[r]) < max_usage;
+        const bool okf = in && u[r] < max_usage;
         const unsigned mf = __ballot_sync(0xffffffffu, okf), mr = __ballot_sync(0xffffffffu, in);
         const int pf = bf + __popc(mf & lt), pr = br + __popc(mr & lt);
         if (okf && pf < 32) {
@@ -335,13 +348,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gw = J.gw, gh = J.gh, k = J.k, n = gw * gh;
   const int R = ring_size(gw);
-  const WalkerLayout L = walker_layout(smem, gw, p, R);
+  const WalkerLayout L = walker_layout(smem, n, p, R);
   if (rank == 0) {
     for (int i = threadIdx.x; i < p; i += blockDim.x) {
       L.usage[i] = 0;
       if (kLabSmem) L.lab[i] = pal[i];
     }
     for (int i = threadIdx.x; i < R; i += blockDim.x) L.seq[i] = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) L.cells[i] = kUnplaced;
     if (threadIdx.x < 4) L.ctrl[threadIdx.x] = 0;
   }
   cluster_sync_all();  // the walker CTA's state exists before any scout reads it
@@ -412,7 +426,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
   uint32_t* ctrl = L.ctrl;
   CellRecord* rec = L.rec;
   uint32_t* seq = L.seq;
-  int32_t* row = L.row;
+  uint16_t* cells = L.cells;
   uint32_t* usage = L.usage;
   const float4* s_lab = L.lab;
   const uint32_t max_usage = J.max_usage;
@@ -451,10 +465,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
   // software-pipelined around it: the header of cell c + 2 and the counters of
   // cell c + 1 are read while cell c is decided, unconditionally (a record not
   // yet published is read again once it is), and everything uncommon (the
-  // full evaluation, row ends, progress releases, late records) sits behind
-  // one branch.  Progress is released every `rel` cells (a power of two, at
-  // most half a row: a scout waiting for the cell above never waits on the
-  // walker's own wait).
+  // full evaluation, late records and the probes for new ones) sits behind one
+  // branch.  Placements go to the shared-memory grid, which the scouts poll;
+  // the grid reaches global memory once, after the walk.
   struct Head {
     uint32_t ep, kf, kr;
   };
@@ -472,8 +485,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
     r.ui = (r.key != 0xFFFFFFFFu && r.ti < (uint32_t)p) ? usage[r.ti] : 0xFFFFFFFFu;
     return r;
   };
-  int rel = 4;
-  while (rel * 4 <= gw && rel < 32) rel <<= 1;
   Cur cur{0xFFFFFFFFu, 0u, 0xFFFFFFFFu};
   Head h1{0u, 0xFFFFFFFFu, 0xFFFFFFFFu};
   bool h1_ok = false;
@@ -482,12 +493,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
     h1_ok = n > 1 && ready(1, false);
     h1 = load_head(1 < n ? 1 : 0);
   }
-  int next_event = min(n - 1, min(gw - 1, rel - 1));  // the next row end or release point
   for (int c = 0; c < n && !aborted; ++c) {
-    // (a) header of cell c + 2 (waiting here, before this cell's progress
-    // release, could wait on a scout that waits on this cell)
-    const bool h2_ok = c + 2 < n && ready(c + 2, false);
-    const Head h2 = load_head(c + 2);
+    // (a) header of cell c + 2 -- whether it is published is known from the
+    // last probe (probes happen on the uncommon path; waiting here, before
+    // this cell's progress release, could wait on a scout that waits on this
+    // cell)
+    bool h2_ok = c + 2 < ready_until;
+    Head h2 = load_head(c + 2);
     // (b) counters of cell c + 1, read before this cell's commit: the choice
     // made here is that cell's left neighbour (row starts are re-read below)
     Cur nxt = finish(h1);
@@ -498,57 +510,56 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
     const uint32_t best = __reduce_min_sync(0xffffffffu, ok ? cur.key : 0xFFFFFFFFu);
     const bool fast = best != 0xFFFFFFFFu && !(best & 0x10000u);  // found, window clear
     int t = (int)(best & 0xFFFFu);
-    if (fast && lane == (int)(best >> 17)) {
-      usage[cur.ti] = cur.ui + 1u;
-      row[x] = t;
-    }
-    if (!fast || c == next_event || !h1_ok) {
+    const bool mine = fast && lane == (int)(best >> 17);
+    if (mine) usage[cur.ti] = cur.ui + 1u;
+    if (mine) cells[c] = (uint16_t)t;
+    if (!fast || !h1_ok) {
       if (!fast) {
-        const int up = y > 0 ? row[x] : -1;
+        const int up = y > 0 ? (int)cells[c - gw] : -1;
         t = full_cell(lab, J.cand_idx + (size_t)c * k, J.cand_dist + (size_t)c * k, k, p, up, left, usage,
                       max_usage, weight, ctrl, epoch, resets, lane);
-        if (lane == 0) row[x] = t;
+        if (lane == 0) cells[c] = (uint16_t)t;
       }
       __syncwarp();
-      if (c == next_event) {
-        if (x + 1 == gw) {
-          // the finished row goes to global memory in one coalesced pass
-          for (int i = lane; i < gw; i += 32) J.grid[(size_t)y * gw + i] = row[i];
-          __syncwarp();  // ordered before the progress release below
-        }
-        if (lane == 0 && (((c + 1) & (rel - 1)) == 0 || c + 1 == n))
-          st_release_cluster(smem_u32(&ctrl[kProgress]), (uint32_t)(c + 1));
-        // the next row end or release point after this cell
-        next_event = min(n - 1, min(((c + 1) / gw) * gw + gw - 1, (c + 1) | (rel - 1)));
-      }
       if (c + 1 < n) {
         if (!h1_ok) {
           h1_ok = ready(c + 1, true);
           h1 = load_head(c + 1);
         }
-        // the counters moved (a full evaluation), or the next cell starts a row
-        // and may take this cell's choice, or its record came late: read afresh
+        // the counters moved (a full evaluation) or the record came late: read afresh
         nxt = finish(h1);
+        // look ahead for the records of the coming cells (one probe covers 32)
+        if (ready_until < n && ready_until <= c + 32) (void)ready(ready_until, false);
+        if (!h2_ok && c + 2 < ready_until) {
+          h2_ok = true;
+          h2 = load_head(c + 2);
+        }
       }
     } else {
       __syncwarp();
     }
+    // the next cell starts a row and may take this cell's choice: its counter
+    // must include this commit
+    if (x + 1 == gw && nxt.ti == (uint32_t)t && nxt.key != 0xFFFFFFFFu) nxt.ui = usage[nxt.ti];
     last = t;
     cur = nxt;
     h1 = h2;
     h1_ok = h2_ok;
-    if (++x == gw) {
-      x = 0;
-      ++y;
-    }
+    const bool wrap = x + 1 == gw;
+    x = wrap ? 0 : x + 1;
+    y += wrap ? 1 : 0;
   }
   if (aborted) {
     if (lane == 0) {
       atomicOr(err, kErrTimeout);
       *reinterpret_cast<volatile uint32_t*>(&ctrl[kAbort]) = 1u;
     }
-  } else if (lane == 0 && J.n_resets) {
-    *J.n_resets = resets;
+  } else {
+    // the placed grid to global memory, then the completion the scout CTA waits for
+    for (int i = lane; i < n; i += 32) J.grid[i] = (int32_t)cells[i];
+    if (lane == 0 && J.n_resets) *J.n_resets = resets;
+    __syncwarp();
+    if (lane == 0) st_release_cluster(smem_u32(&ctrl[kProgress]), (uint32_t)n);
   }
   cluster_sync_all();  // the scouts are done with this CTA's shared memory
 }
@@ -560,7 +571,7 @@ size_t greedy_shared_bytes(int k, int gw, int p, bool lab_smem, bool usage_smem)
 }
 
 int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_jobs, int k, int max_gw,
-                  uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream) {
+                  int max_cells, uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream) {
   if (n_jobs <= 0) return MG_OK;
   if (k < 1 || k > 100) return fail(MG_ERR_ARG, "candidate count must be in 1..100");
   constexpr size_t kMaxSmem = 220 * 1024;
@@ -578,8 +589,8 @@ int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_job
   // The scouted walk: counters in shared memory, 16-bit palette indices, rows
   // of at least 8 cells.
   if (max_gw >= 8 && p <= 65535) {
-    bool lab_smem = pair_smem_bytes(max_gw, p, true) <= kMaxSmem;
-    const size_t bytes = pair_smem_bytes(max_gw, p, lab_smem);
+    bool lab_smem = pair_smem_bytes(max_gw, max_cells, p, true) <= kMaxSmem;
+    const size_t bytes = pair_smem_bytes(max_gw, max_cells, p, lab_smem);
     if (bytes <= kMaxSmem) {
       if (lab_smem)
         greedy_pair_kernel<true><<<2 * n_jobs, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);

@@ -98,7 +98,7 @@ struct GreedyJob {
 };
 // Candidate arrays must hold ceil(N/16)*16 rows (the walk streams 16 rows per copy).
 int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_jobs, int k, int max_gw,
-                  uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream);
+                  int max_cells, uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream);
 inline size_t padded_cells(int n) { return ((size_t)n + 15) / 16 * 16; }
 
 // (e) annealing chains.

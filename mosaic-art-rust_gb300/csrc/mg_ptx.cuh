@@ -119,6 +119,12 @@ __device__ __forceinline__ uint32_t ld_cluster_u32(uint32_t addr) {
   return v;
 }
 
+__device__ __forceinline__ uint32_t ld_cluster_u16(uint32_t addr) {
+  uint16_t v;
+  asm volatile("ld.shared::cluster.u16 %0, [%1];" : "=h"(v) : "r"(addr) : "memory");
+  return v;
+}
+
 __device__ __forceinline__ void st_cluster_u32(uint32_t addr, uint32_t v) {
   asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
 }
