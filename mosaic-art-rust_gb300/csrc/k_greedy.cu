@@ -10,10 +10,10 @@
 //  - greedy_kernel: one warp walks one mosaic (greedy_walk.cuh).  Used for
 //    palettes whose counters do not fit in shared memory, palettes above 65535
 //    materials and grids narrower than 8 cells.
-//  - greedy_pair_kernel: a cluster of two CTAs per mosaic.  The walk is a chain
-//    of dependent decisions, so its speed is the latency of one decision.  One
-//    warp of CTA 0 (the walker) makes the decisions; 32 scout warps in
-//    CTA 1, on another SM, prepare each cell's decision ahead of the walker
+//  - greedy_pair_kernel: a cluster of three CTAs per mosaic.  The walk is a
+//    chain of dependent decisions, so its speed is the latency of one decision.
+//    One warp of CTA 0 (the walker) makes the decisions; 64 scout warps in
+//    CTAs 1 and 2, on other SMs, prepare each cell's decision ahead of the walker
 //    from a snapshot of the usage counters, reading the walk's state and
 //    writing their records through distributed shared memory:
 //      the first 32 candidates (list order) that differ from the cell above
@@ -51,15 +51,17 @@ __global__ void __launch_bounds__(32) greedy_kernel(const float4* __restrict__ p
 }
 
 // ---- the scouted walk -------------------------------------------------------------------
-// A cluster of two CTAs per mosaic.  CTA 0 walks (warp 0; the state of the
-// walk lives in its shared memory); CTA 1, on another SM, holds the scouts,
-// which read the walk's state and write their records through distributed
-// shared memory, so the walker's SM runs nothing but the walk.
-constexpr int kWarps = 32;   // per CTA
-constexpr int kScouts = 32;  // every warp of CTA 1
+// A cluster of 1 + kScoutCtas CTAs per mosaic.  CTA 0 walks (warp 0; the
+// state of the walk lives in its shared memory); the other CTAs, on other
+// SMs, hold the scouts, which read the walk's state and write their records
+// through distributed shared memory, so the walker's SM runs nothing but the
+// walk.
+constexpr int kWarps = 32;                  // per CTA
+constexpr int kScoutCtas = 2;               // CTAs 1..kScoutCtas of the cluster
+constexpr int kScouts = kWarps * kScoutCtas;  // every warp of the scout CTAs
 constexpr uint32_t kInvalidEpoch = 0xFFFFFFFFu;
 constexpr uint32_t kWalkPolls = 1u << 24;
-constexpr uint32_t kScoutPolls = 1u << 24;
+constexpr uint32_t kScoutPolls = 1u << 21;  // polls of about 1 us each
 constexpr int kCostChunk = 2048;  // cells per pass of the final cost sum
 enum Ctrl { kProgress = 0, kEpoch = 1, kAbort = 2 };
 
@@ -231,7 +233,7 @@ __device__ inline WalkerLayout walker_layout(uint8_t* smem, int n, int p, int R)
   return L;
 }
 
-// A scout warp (CTA 1): prepares the records of cells s, s + 32, s + 64, ...
+// A scout warp: prepares the records of cells s, s + kScouts, s + 2 kScouts, ...
 // Returns false when the walk was aborted.
 __device__ bool scout_cells(int s, const GreedyJob& J, int p, const WalkerLayout& L, ScoutStage& S, int R,
                             uint32_t* err) {
@@ -281,25 +283,19 @@ __device__ bool scout_cells(int s, const GreedyJob& J, int p, const WalkerLayout
           }
           return false;
         }
-        __nanosleep(64);
+        __nanosleep(1000);  // the scouts run far ahead: poll the walker's SM rarely
       }
       up = (int)v;
     }
     const uint32_t ep0 = ld_acquire_cluster(r_epoch);
-    // every counter the lists may need, in one round trip
-    uint32_t u[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const bool in = r < nr && t[r] < (uint32_t)p && (int)t[r] != up;
-      u[r] = in ? ld_cluster_u32(r_usage + 4u * t[r]) : 0xFFFFFFFFu;
-    }
     int bf = 0, br = 0;
     float af = inf, ar = inf;  // distance of the 33rd entry
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       if (r < nr && (bf <= 32 || br <= 32)) {
         const bool in = t[r] < (uint32_t)p && (int)t[r] != up;
-        const bool okf = in && u[r] < max_usage;
+        // counters are read on demand: each one is a load from the walker's SM
+        const bool okf = in && ld_cluster_u32(r_usage + 4u * t[r]) < max_usage;
         const unsigned mf = __ballot_sync(0xffffffffu, okf), mr = __ballot_sync(0xffffffffu, in);
         const int pf = bf + __popc(mf & lt), pr = br + __popc(mr & lt);
         if (okf && pf < 32) {
@@ -329,8 +325,18 @@ __device__ bool scout_cells(int s, const GreedyJob& J, int p, const WalkerLayout
     const bool blocked_r = use_pen && drn < __fadd_rn(dri, two_w);
     const uint32_t slot = (uint32_t)(c & (R - 1));
     const uint32_t rr = r_rec + slot * (uint32_t)sizeof(CellRecord);
-    st_cluster_u32(rr + 4u * lane, lane < cf ? S.kf[lane] | (blocked_f ? 0x10000u : 0u) : 0xFFFFFFFFu);
-    st_cluster_u32(rr + 128u + 4u * lane, lane < cr ? S.kr[lane] | (blocked_r ? 0x10000u : 0u) : 0xFFFFFFFFu);
+    // final keys into the local copy, then 16-byte stores to the walker's SM
+    // (fewer requests on its shared memory)
+    const uint32_t kf_final = lane < cf ? S.kf[lane] | (blocked_f ? 0x10000u : 0u) : 0xFFFFFFFFu;
+    const uint32_t kr_final = lane < cr ? S.kr[lane] | (blocked_r ? 0x10000u : 0u) : 0xFFFFFFFFu;
+    __syncwarp();
+    S.kf[lane] = kf_final;
+    S.kr[lane] = kr_final;
+    __syncwarp();
+    if (lane < 16) {
+      const uint4 v = reinterpret_cast<const uint4*>(lane < 8 ? S.kf : S.kr)[lane & 7];
+      st_cluster_v4(rr + 16u * (uint32_t)lane, v);
+    }
     if (lane == 0) st_cluster_u32(rr + 256u, ep0 == ep1 ? ep0 : kInvalidEpoch);
     fence_cluster();
     __syncwarp();
@@ -340,10 +346,10 @@ __device__ bool scout_cells(int s, const GreedyJob& J, int p, const WalkerLayout
 }
 
 template <bool kLabSmem>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
+__global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps * 32)
     greedy_pair_kernel(const float4* __restrict__ pal, int p, const GreedyJob* __restrict__ jobs, uint32_t* err) {
   extern __shared__ __align__(128) uint8_t smem[];
-  const GreedyJob J = jobs[blockIdx.x >> 1];
+  const GreedyJob J = jobs[blockIdx.x / (1 + kScoutCtas)];
   const uint32_t rank = cluster_ctarank();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gw = J.gw, gh = J.gh, k = J.k, n = gw * gh;
@@ -360,11 +366,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
   }
   cluster_sync_all();  // the walker CTA's state exists before any scout reads it
 
-  if (rank == 1) {
-    // ---- the scouts, then the final cost of the walk
+  if (rank >= 1) {
+    // ---- the scouts, then (CTA 1) the final cost of the walk
     ScoutStage* stage = reinterpret_cast<ScoutStage*>(smem);
     float* terms = reinterpret_cast<float*>(smem + (size_t)kWarps * sizeof(ScoutStage));
-    bool ok = scout_cells(warp, J, p, L, stage[warp], R, err);
+    bool ok = scout_cells((int)(rank - 1) * kWarps + warp, J, p, L, stage[warp], R, err);
+    if (rank > 1) {
+      cluster_sync_all();
+      return;
+    }
     // calculate_total_cost (adjacency.rs:91-130) of the placed grid once the
     // walk is complete: terms in parallel, one sequential FP32 sum in the
     // reference's order (right then down, row-major).
@@ -460,14 +470,23 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
       }
     }
   };
-  // The walk is a chain of dependent decisions; per cell the critical path is
-  // the eligibility test, one warp minimum and a flag test.  Record reads are
-  // software-pipelined around it: the header of cell c + 2 and the counters of
-  // cell c + 1 are read while cell c is decided, unconditionally (a record not
-  // yet published is read again once it is), and everything uncommon (the
-  // full evaluation, late records and the probes for new ones) sits behind one
-  // branch.  Placements go to the shared-memory grid, which the scouts poll;
-  // the grid reaches global memory once, after the walk.
+  // The walk is a chain of dependent decisions.  Per cell, the two lowest
+  // keys among entries under the usage cap -- ignoring the left neighbour --
+  // are found first (two warp minimums that do not depend on the previous
+  // choice); the decision is then one comparison with the previous choice
+  // (the left neighbour): the first key unless its material is that
+  // neighbour's, else the second.  So the chain from one cell's choice to the
+  // next is a compare and a select.  A record's counters are read before the
+  // previous commit; the only counter that commit changed is the left
+  // neighbour's, which the comparison excludes anyway -- except at a row
+  // start (no left neighbour), which takes the uncommon path with that
+  // counter corrected.  Record reads are software-pipelined: the header of
+  // cell c + 2 and the counters of cell c + 1 are read while cell c is
+  // decided, unconditionally (a record not yet published is read again once
+  // it is).  Everything uncommon (row starts, the full evaluation, late
+  // records and the probes for new ones) sits behind one branch.
+  // Placements go to the shared-memory grid, which the scouts poll; the grid
+  // reaches global memory once, after the walk.
   struct Head {
     uint32_t ep, kf, kr;
   };
@@ -486,6 +505,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
     return r;
   };
   Cur cur{0xFFFFFFFFu, 0u, 0xFFFFFFFFu};
+  bool cur_fresh = true;  // cur's counters include the previous commit
   Head h1{0u, 0xFFFFFFFFu, 0xFFFFFFFFu};
   bool h1_ok = false;
   if (n > 0 && ready(0, true)) {
@@ -494,31 +514,48 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
     h1 = load_head(1 < n ? 1 : 0);
   }
   for (int c = 0; c < n && !aborted; ++c) {
-    // (a) header of cell c + 2 -- whether it is published is known from the
+    // (a) the two lowest keys under the cap, left neighbour ignored
+    const bool okn = cur.ui < max_usage;  // absent entries carry ~0
+    const uint32_t b1 = __reduce_min_sync(0xffffffffu, okn ? cur.key : 0xFFFFFFFFu);
+    const uint32_t b2 = __reduce_min_sync(0xffffffffu, (okn && cur.key != b1) ? cur.key : 0xFFFFFFFFu);
+    // (b) header of cell c + 2 -- whether it is published is known from the
     // last probe (probes happen on the uncommon path; waiting here, before
-    // this cell's progress release, could wait on a scout that waits on this
-    // cell)
+    // this cell's commit, could wait on a scout that waits on this cell)
     bool h2_ok = c + 2 < ready_until;
     Head h2 = load_head(c + 2);
-    // (b) counters of cell c + 1, read before this cell's commit: the choice
-    // made here is that cell's left neighbour (row starts are re-read below)
+    // (c) counters of cell c + 1, read before this cell's commit
     Cur nxt = finish(h1);
-    // (c) this cell: the lowest key among entries that pass the counters and
-    // the left neighbour (the lists already exclude the cell above)
-    const int left = x > 0 ? last : -1;
-    const bool ok = cur.ui < max_usage && cur.ti != (uint32_t)left;
-    const uint32_t best = __reduce_min_sync(0xffffffffu, ok ? cur.key : 0xFFFFFFFFu);
-    const bool fast = best != 0xFFFFFFFFu && !(best & 0x10000u);  // found, window clear
-    int t = (int)(best & 0xFFFFu);
-    const bool mine = fast && lane == (int)(best >> 17);
+    bool nxt_fresh = false;
+    // (d) this cell: the first key unless it is the left neighbour's material
+    const bool row_start = x == 0;
+    const uint32_t chosen = (b1 & 0xFFFFu) != (uint32_t)last ? b1 : b2;
+    const bool fast = !row_start && chosen != 0xFFFFFFFFu && !(chosen & 0x10000u);  // found, window clear
+    int t = (int)(chosen & 0xFFFFu);
+    const bool mine = fast && lane == (int)(chosen >> 17);
     if (mine) usage[cur.ti] = cur.ui + 1u;
     if (mine) cells[c] = (uint16_t)t;
     if (!fast || !h1_ok) {
       if (!fast) {
-        const int up = y > 0 ? (int)cells[c - gw] : -1;
-        t = full_cell(lab, J.cand_idx + (size_t)c * k, J.cand_dist + (size_t)c * k, k, p, up, left, usage,
-                      max_usage, weight, ctrl, epoch, resets, lane);
-        if (lane == 0) cells[c] = (uint16_t)t;
+        bool done = false;
+        if (row_start) {
+          // no left neighbour: the previous commit's counter counts
+          const uint32_t ui = cur.ui + ((!cur_fresh && cur.ti == (uint32_t)last && cur.key != 0xFFFFFFFFu) ? 1u : 0u);
+          const uint32_t b = __reduce_min_sync(0xffffffffu, ui < max_usage ? cur.key : 0xFFFFFFFFu);
+          if (b != 0xFFFFFFFFu && !(b & 0x10000u)) {
+            t = (int)(b & 0xFFFFu);
+            if (lane == (int)(b >> 17)) {
+              usage[cur.ti] = ui + 1u;
+              cells[c] = (uint16_t)t;
+            }
+            done = true;
+          }
+        }
+        if (!done) {
+          const int up = y > 0 ? (int)cells[c - gw] : -1;
+          t = full_cell(lab, J.cand_idx + (size_t)c * k, J.cand_dist + (size_t)c * k, k, p, up,
+                        row_start ? -1 : last, usage, max_usage, weight, ctrl, epoch, resets, lane);
+          if (lane == 0) cells[c] = (uint16_t)t;
+        }
       }
       __syncwarp();
       if (c + 1 < n) {
@@ -526,8 +563,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
           h1_ok = ready(c + 1, true);
           h1 = load_head(c + 1);
         }
-        // the counters moved (a full evaluation) or the record came late: read afresh
+        // the counters moved (a full evaluation), or the record came late: read afresh
         nxt = finish(h1);
+        nxt_fresh = true;
         // look ahead for the records of the coming cells (one probe covers 32)
         if (ready_until < n && ready_until <= c + 32) (void)ready(ready_until, false);
         if (!h2_ok && c + 2 < ready_until) {
@@ -538,11 +576,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWarps * 32)
     } else {
       __syncwarp();
     }
-    // the next cell starts a row and may take this cell's choice: its counter
-    // must include this commit
-    if (x + 1 == gw && nxt.ti == (uint32_t)t && nxt.key != 0xFFFFFFFFu) nxt.ui = usage[nxt.ti];
     last = t;
     cur = nxt;
+    cur_fresh = nxt_fresh;
     h1 = h2;
     h1_ok = h2_ok;
     const bool wrap = x + 1 == gw;
@@ -593,9 +629,9 @@ int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_job
     const size_t bytes = pair_smem_bytes(max_gw, max_cells, p, lab_smem);
     if (bytes <= kMaxSmem) {
       if (lab_smem)
-        greedy_pair_kernel<true><<<2 * n_jobs, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
+        greedy_pair_kernel<true><<<(1 + kScoutCtas) * n_jobs, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
       else
-        greedy_pair_kernel<false><<<2 * n_jobs, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
+        greedy_pair_kernel<false><<<(1 + kScoutCtas) * n_jobs, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
       g_launches += 1;
       MG_CUDA(cudaGetLastError());
       return MG_OK;
