@@ -148,8 +148,13 @@ def algorithmic(inp, palette_size: int, sel_px: int):
 
 STAGES = ["palette_lab", "similarity", "cell_lab", "nearest", "greedy", "anneal", "composite"]
 KERNEL_OF_STAGE = {"palette_lab": "region_stats_kernel", "similarity": "similarity_full_kernel",
-                   "cell_lab": "region_stats_kernel", "nearest": "nearest_kernel", "greedy": "greedy_kernel",
-                   "anneal": "anneal_kernel", "composite": "composite_kernel"}
+                   "cell_lab": "region_stats_kernel", "nearest": "nearest_kernel", "greedy": "greedy_pair_kernel",
+                   "anneal": "anneal_cta_kernel", "composite": "composite_kernel"}
+# Stages that are chains of dependent decisions (their bytes are a lower bound;
+# the limit is the latency of one decision), and the data-parallel ones.
+SEQUENTIAL = {"greedy": "latency of one placement decision (row-major walk, sequential by definition)",
+              "anneal": "latency of one round of 16 proposals per chain (32 chains, sequential within a chain)"}
+DATA_PARALLEL = ["palette_lab", "cell_lab", "nearest", "similarity", "composite"]
 
 
 def traffic_from_profiles(kernel: str):
@@ -330,7 +335,16 @@ def run_ours(args, rank, world, local):
                      "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / peaks["hbm_gbs"], 6), "peak_source": peak_kind,
                      "traffic": traffic_from_profiles(KERNEL_OF_STAGE[dom_name]),
-                     "algorithmic_bytes": alg[dom_name]},
+                     "algorithmic_bytes": alg[dom_name],
+                     "limit": SEQUENTIAL.get(dom_name, "HBM bandwidth"),
+                     "us_per_unit": round(1000.0 * mean_stage[dom] / N, 4) if dom_name == "greedy" else None},
+        "roofline_data_parallel": (lambda d: {
+            "bound": "hbm", "kernel": KERNEL_OF_STAGE[d], "stage": d,
+            "achieved": round(alg[d] / (mean_stage[STAGES.index(d)] / 1000.0) / 1e9, 2), "peak": peaks["hbm_gbs"],
+            "unit": "GB/s",
+            "frac": round(alg[d] / (mean_stage[STAGES.index(d)] / 1000.0) / 1e9 / peaks["hbm_gbs"], 4),
+            "traffic": traffic_from_profiles(KERNEL_OF_STAGE[d]), "algorithmic_bytes": alg[d]})(
+            max(DATA_PARALLEL, key=lambda d: mean_stage[STAGES.index(d)])),
         "stages": stages,
         "clocks": clk,
         "wall_s_timed": round(wall, 3),
@@ -349,6 +363,8 @@ def run_batched(args, rank, world, local):
     """256 uneven mosaics over one resident 10 000-material palette: the batched
     pipeline (one persistent walk/chain launch, graph replay) against the same
     mosaics run one single-mosaic batch after another (the plain path)."""
+    import ctypes as C
+
     import numpy as np
     import torch
 
@@ -358,7 +374,7 @@ def run_batched(args, rank, world, local):
     lib = capi.load()
     ctx = capi.Context(local)
     t0 = time.perf_counter()
-    specs, mats, thumbs = job.batched_workload(seed=20251203 + 7919 * rank)
+    specs, mats, thumbs = job.batched_workload(seed=20251203 + 7919 * rank, allocator=lib.mg_host_alloc)
     gen_s = time.perf_counter() - t0
     pal = job.Palette(ctx, mats, thumbs, 32, 32, target_aspect=4 / 3, build_similarity=True)
     reqs = job.batched_requests(specs)
@@ -414,14 +430,22 @@ def run_batched(args, rank, world, local):
                for i in range(0, n, 17))
     for b in singles:
         b.close()
-    # end to end from host buffers (one mg_generate_batch call)
-    e2e = []
-    for _ in range(2):
-        t1 = time.perf_counter()
-        job.generate_batch(ctx, pal, reqs)
-        e2e.append(time.perf_counter() - t1)
-    e2e_s = float(np.mean(e2e))
+    # end to end from pinned host buffers to pinned host buffers (one
+    # mg_generate_batch call; the targets are read in place)
     tw = 32
+    outs = []
+    for s in specs:
+        g = np.ctypeslib.as_array(C.cast(lib.mg_host_alloc(4 * s.gw * s.gh), C.POINTER(C.c_int32)), shape=(s.gw * s.gh,))
+        im = np.ctypeslib.as_array(C.cast(lib.mg_host_alloc(3 * s.gw * s.gh * tw * tw), C.POINTER(C.c_uint8)),
+                                   shape=(s.gh * tw, s.gw * tw, 3))
+        outs.append((g, im))
+    e2e = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        job.generate_batch(ctx, pal, reqs, outputs=outs)
+        e2e.append(time.perf_counter() - t1)
+    e2e = e2e[1:]
+    e2e_s = float(np.mean(e2e))
     h2d = int(sum(s.target.nbytes for s in specs))
     d2h = int(sum(s.gw * s.gh * tw * tw * 3 + s.gw * s.gh * 4 for s in specs))
     line = {"metric": "mosaics/sec (batched)", "value": n / (step_ms / 1000.0), "unit": "mosaics/s", "n_gpus": world,

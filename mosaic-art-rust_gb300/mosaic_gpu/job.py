@@ -298,15 +298,20 @@ class Batch:
             pass
 
 
-def generate_batch(ctx: capi.Context, palette: Palette, mosaics: list):
+def generate_batch(ctx: capi.Context, palette: Palette, mosaics: list, outputs=None):
+    """One mg_generate_batch call.  outputs: optional [(grid, image)] to write
+    into (e.g. pinned buffers); fresh numpy arrays otherwise."""
     n = len(mosaics)
     arr = (capi.Mosaic * max(n, 1))(*mosaics)
     tw, th = palette.tile
     grids, images = [], []
     results = (capi.Result * max(n, 1))()
     for i, m in enumerate(mosaics):
-        g = np.zeros(m.grid_w * m.grid_h, np.int32)
-        im = np.zeros((m.grid_h * th, m.grid_w * tw, 3), np.uint8)
+        if outputs is not None:
+            g, im = outputs[i]
+        else:
+            g = np.zeros(m.grid_w * m.grid_h, np.int32)
+            im = np.zeros((m.grid_h * th, m.grid_w * tw, 3), np.uint8)
         results[i].grid = capi.ptr(g, C.c_int32)
         results[i].image = capi.ptr(im, C.c_uint8)
         grids.append(g.reshape(m.grid_h, m.grid_w))
