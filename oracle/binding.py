@@ -238,8 +238,8 @@ def composite(grid, thumbs, cell_rgb, thumb_rgb, strength):
     return out
 
 
-def generate(inp, threads: int = 1, want_image: bool = True):
-    """Run the whole job on the CPU from mosaic_gpu.job.Inputs."""
+def generate(inp, threads: int = 1, want_image: bool = True, stream: int = 0):
+    """Run the whole job on the CPU from mosaic_gpu.job.Inputs (Philox stream id `stream`)."""
     cfg = inp.cfg
     tw, th = inp.tile
     n = len(inp.mats)
@@ -260,7 +260,7 @@ def generate(inp, threads: int = 1, want_image: bool = True):
     job.max_usage, job.weight, job.color_strength = cfg.max_usage, cfg.weight, cfg.color_strength
     job.enable_opt = 1 if cfg.enable_optimization else 0
     job.iters, job.t0, job.decay = cfg.iterations, 100.0, 0.99995
-    job.chains, job.seed, job.stream, job.threads = cfg.chains, cfg.seed, 0, threads
+    job.chains, job.seed, job.stream, job.threads = cfg.chains, cfg.seed, stream, threads
     N = cfg.grid_w * cfg.grid_h
     grid = np.zeros(N, np.int32)
     image = np.zeros((cfg.grid_h * th, cfg.grid_w * tw, 3), np.uint8) if want_image else None
