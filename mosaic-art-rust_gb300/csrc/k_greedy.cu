@@ -513,68 +513,95 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
     h1_ok = n > 1 && ready(1, false);
     h1 = load_head(1 < n ? 1 : 0);
   }
-  for (int c = 0; c < n && !aborted; ++c) {
-    // (a) the two lowest keys under the cap, left neighbour ignored
-    const bool okn = cur.ui < max_usage;  // absent entries carry ~0
-    const uint32_t b1 = __reduce_min_sync(0xffffffffu, okn ? cur.key : 0xFFFFFFFFu);
-    const uint32_t b2 = __reduce_min_sync(0xffffffffu, (okn && cur.key != b1) ? cur.key : 0xFFFFFFFFu);
-    // (b) header of cell c + 2 -- whether it is published is known from the
-    // last probe (probes happen on the uncommon path; waiting here, before
-    // this cell's commit, could wait on a scout that waits on this cell)
-    bool h2_ok = c + 2 < ready_until;
-    Head h2 = load_head(c + 2);
-    // (c) counters of cell c + 1, read before this cell's commit
-    Cur nxt = finish(h1);
-    bool nxt_fresh = false;
-    // (d) this cell: the first key unless it is the left neighbour's material
-    const bool row_start = x == 0;
-    const uint32_t chosen = (b1 & 0xFFFFu) != (uint32_t)last ? b1 : b2;
-    const bool fast = !row_start && chosen != 0xFFFFFFFFu && !(chosen & 0x10000u);  // found, window clear
-    int t = (int)(chosen & 0xFFFFu);
-    const bool mine = fast && lane == (int)(chosen >> 17);
-    if (mine) usage[cur.ti] = cur.ui + 1u;
-    if (mine) cells[c] = (uint16_t)t;
-    if (!fast || !h1_ok) {
-      if (!fast) {
-        bool done = false;
-        if (row_start) {
-          // no left neighbour: the previous commit's counter counts
-          const uint32_t ui = cur.ui + ((!cur_fresh && cur.ti == (uint32_t)last && cur.key != 0xFFFFFFFFu) ? 1u : 0u);
-          const uint32_t b = __reduce_min_sync(0xffffffffu, ui < max_usage ? cur.key : 0xFFFFFFFFu);
-          if (b != 0xFFFFFFFFu && !(b & 0x10000u)) {
-            t = (int)(b & 0xFFFFu);
-            if (lane == (int)(b >> 17)) {
-              usage[cur.ti] = ui + 1u;
-              cells[c] = (uint16_t)t;
-            }
-            done = true;
-          }
-        }
-        if (!done) {
-          const int up = y > 0 ? (int)cells[c - gw] : -1;
-          t = full_cell(lab, J.cand_idx + (size_t)c * k, J.cand_dist + (size_t)c * k, k, p, up,
-                        row_start ? -1 : last, usage, max_usage, weight, ctrl, epoch, resets, lane);
-          if (lane == 0) cells[c] = (uint16_t)t;
-        }
+  // The common case runs in a tight inner loop of its own; a cell that needs
+  // anything else leaves it, is finished below, and the inner loop resumes.
+  int c = 0;
+  while (c < n && !aborted) {
+    Head h2{};
+    bool h2_ok = false;
+    Cur nxt = cur;
+    uint32_t chosen = 0xFFFFFFFFu;
+    bool fast = false;
+    for (;;) {
+      // (a) the two lowest keys under the cap, left neighbour ignored
+      const bool okn = cur.ui < max_usage;  // absent entries carry ~0
+      const uint32_t b1 = __reduce_min_sync(0xffffffffu, okn ? cur.key : 0xFFFFFFFFu);
+      const uint32_t b2 = __reduce_min_sync(0xffffffffu, (okn && cur.key != b1) ? cur.key : 0xFFFFFFFFu);
+      // (b) header of cell c + 2 -- whether it is published is known from the
+      // last probe (probes happen on the uncommon path; waiting here, before
+      // this cell's commit, could wait on a scout that waits on this cell)
+      h2_ok = c + 2 < ready_until;
+      h2 = load_head(c + 2);
+      // (c) counters of cell c + 1, read before this cell's commit
+      nxt = finish(h1);
+      // (d) this cell: the first key unless it is the left neighbour's material
+      chosen = (b1 & 0xFFFFu) != (uint32_t)last ? b1 : b2;
+      fast = x != 0 && chosen != 0xFFFFFFFFu && !(chosen & 0x10000u);  // not a row start, found, window clear
+      if (!fast || !h1_ok) break;
+      const int t = (int)(chosen & 0xFFFFu);
+      if (lane == (int)(chosen >> 17)) {
+        usage[cur.ti] = cur.ui + 1u;
+        cells[c] = (uint16_t)t;
       }
       __syncwarp();
-      if (c + 1 < n) {
-        if (!h1_ok) {
-          h1_ok = ready(c + 1, true);
-          h1 = load_head(c + 1);
-        }
-        // the counters moved (a full evaluation), or the record came late: read afresh
-        nxt = finish(h1);
-        nxt_fresh = true;
-        // look ahead for the records of the coming cells (one probe covers 32)
-        if (ready_until < n && ready_until <= c + 32) (void)ready(ready_until, false);
-        if (!h2_ok && c + 2 < ready_until) {
-          h2_ok = true;
-          h2 = load_head(c + 2);
-        }
+      last = t;
+      cur = nxt;
+      cur_fresh = false;
+      h1 = h2;
+      h1_ok = h2_ok;
+      const bool wrap = x + 1 == gw;
+      x = wrap ? 0 : x + 1;
+      y += wrap ? 1 : 0;
+      if (++c == n) break;
+    }
+    if (c == n) break;
+    // ---- the uncommon path for cell c
+    int t = (int)(chosen & 0xFFFFu);
+    if (fast) {
+      // only the next record was late
+      if (lane == (int)(chosen >> 17)) {
+        usage[cur.ti] = cur.ui + 1u;
+        cells[c] = (uint16_t)t;
       }
     } else {
-      __syncwarp();
+      const bool row_start = x == 0;
+      bool done = false;
+      if (row_start) {
+        // no left neighbour: the previous commit's counter counts
+        const uint32_t ui = cur.ui + ((!cur_fresh && cur.ti == (uint32_t)last && cur.key != 0xFFFFFFFFu) ? 1u : 0u);
+        const uint32_t b = __reduce_min_sync(0xffffffffu, ui < max_usage ? cur.key : 0xFFFFFFFFu);
+        if (b != 0xFFFFFFFFu && !(b & 0x10000u)) {
+          t = (int)(b & 0xFFFFu);
+          if (lane == (int)(b >> 17)) {
+            usage[cur.ti] = ui + 1u;
+            cells[c] = (uint16_t)t;
+          }
+          done = true;
+        }
+      }
+      if (!done) {
+        const int up = y > 0 ? (int)cells[c - gw] : -1;
+        t = full_cell(lab, J.cand_idx + (size_t)c * k, J.cand_dist + (size_t)c * k, k, p, up,
+                      row_start ? -1 : last, usage, max_usage, weight, ctrl, epoch, resets, lane);
+        if (lane == 0) cells[c] = (uint16_t)t;
+      }
+    }
+    __syncwarp();
+    bool nxt_fresh = false;
+    if (c + 1 < n) {
+      if (!h1_ok) {
+        h1_ok = ready(c + 1, true);
+        h1 = load_head(c + 1);
+      }
+      // the counters moved (a full evaluation), or the record came late: read afresh
+      nxt = finish(h1);
+      nxt_fresh = true;
+      // look ahead for the records of the coming cells (one probe covers 32)
+      if (ready_until < n && ready_until <= c + 32) (void)ready(ready_until, false);
+      if (!h2_ok && c + 2 < ready_until) {
+        h2_ok = true;
+        h2 = load_head(c + 2);
+      }
     }
     last = t;
     cur = nxt;
@@ -584,6 +611,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
     const bool wrap = x + 1 == gw;
     x = wrap ? 0 : x + 1;
     y += wrap ? 1 : 0;
+    ++c;
   }
   if (aborted) {
     if (lane == 0) {
