@@ -235,10 +235,14 @@ __device__ inline WalkerLayout walker_layout(uint8_t* smem, int n, int p, int R)
 
 // A scout warp: prepares the records of cells s, s + kScouts, s + 2 kScouts, ...
 // Returns false when the walk was aborted.
-__device__ bool scout_cells(int s, const GreedyJob& J, int p, const WalkerLayout& L, ScoutStage& S, int R,
+// (The layout is recomputed here rather than passed by reference: a struct
+// whose address escapes would turn the walker's shared-memory pointers into
+// generic ones.)
+__device__ bool scout_cells(int s, const GreedyJob& J, int p, uint8_t* smem, ScoutStage& S, int R,
                             uint32_t* err) {
   const int lane = threadIdx.x & 31;
   const int gw = J.gw, k = J.k, n = gw * J.gh;
+  const WalkerLayout L = walker_layout(smem, n, p, R);
   const uint32_t max_usage = J.max_usage;
   const bool use_pen = J.weight > 0.0f;
   const float two_w = __fmul_rn(2.0f, J.weight);
@@ -370,7 +374,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
     // ---- the scouts, then (CTA 1) the final cost of the walk
     ScoutStage* stage = reinterpret_cast<ScoutStage*>(smem);
     float* terms = reinterpret_cast<float*>(smem + (size_t)kWarps * sizeof(ScoutStage));
-    bool ok = scout_cells((int)(rank - 1) * kWarps + warp, J, p, L, stage[warp], R, err);
+    bool ok = scout_cells((int)(rank - 1) * kWarps + warp, J, p, smem, stage[warp], R, err);
     if (rank > 1) {
       cluster_sync_all();
       return;
