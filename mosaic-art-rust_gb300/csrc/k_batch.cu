@@ -19,6 +19,7 @@
 // anneal_chain.cuh), so batched results equal the one-mosaic-per-launch
 // results bit for bit.
 #include "anneal_chain.cuh"
+#include "composite.cuh"
 #include "greedy_walk.cuh"
 
 namespace mg {
@@ -229,7 +230,8 @@ __global__ void batch_adjust_kernel(const BatchMosaic* __restrict__ mos, int nm,
   adj[cell] = r;
 }
 
-// blockIdx.y = mosaic; a grid-stride loop over its output pixels.
+// blockIdx.y = mosaic; a grid-stride loop over its output pixels, four per
+// thread when the tile width allows (composite.cuh).
 __global__ void __launch_bounds__(256) batch_composite_kernel(const BatchMosaic* __restrict__ mos,
                                                               const uint8_t* __restrict__ thumbs, int tw, int th,
                                                               const float4* __restrict__ adj) {
@@ -237,9 +239,32 @@ __global__ void __launch_bounds__(256) batch_composite_kernel(const BatchMosaic*
   s_unit[threadIdx.x] = u8_unit(threadIdx.x);
   __syncthreads();
   const BatchMosaic& M = mos[blockIdx.y];
-  const int ow = M.gw * tw;
-  const int64_t total = (int64_t)ow * M.gh * th;
+  const int ow = M.gw * tw, oh = M.gh * th;
   const bool do_adj = M.strength > 0.0f;
+  if ((tw & 3) == 0) {
+    const int gpr = ow >> 2, total = gpr * oh;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+      const int oy = q / gpr, ox = (q - oy * gpr) << 2;
+      const int cy = oy / th, cx = ox / tw;
+      const int local = cy * M.gw + cx;
+      const int g = M.final_grid[local];
+      uint8_t* d = M.out + ((size_t)oy * ow + ox) * 3;
+      if (g < 0) {
+        uint32_t* dw = reinterpret_cast<uint32_t*>(d);
+        dw[0] = dw[1] = dw[2] = 0u;
+        continue;
+      }
+      const uint8_t* src = thumbs + (((size_t)g * th + (oy - cy * th)) * tw + (ox - cx * tw)) * 3;
+      Adjust a{0.0f, 1.0f, 0.0f, 1.0f};
+      if (do_adj) {
+        const float4 a4 = adj[M.cell_base + local];
+        a = Adjust{a4.x, a4.y, a4.z, a4.w};
+      }
+      composite_group4(src, d, do_adj, a, s_unit);
+    }
+    return;
+  }
+  const int64_t total = (int64_t)ow * oh;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int oy = (int)(t / ow), ox = (int)(t - (int64_t)oy * ow);
     const int cy = oy / th, cx = ox / tw;
@@ -339,7 +364,7 @@ int launch_batch_finish(const BatchMosaic* mos, int nm, int total_cells, const u
                         cudaStream_t stream) {
   if (nm <= 0) return MG_OK;
   batch_adjust_kernel<<<(total_cells + 255) / 256, 256, 0, stream>>>(mos, nm, total_cells, thumb_rgb, cell_rgb, adj);
-  const int bx = std::max(1, std::min((max_out_px + 255) / 256, 256));
+  const int bx = std::max(1, std::min(((tw & 3) == 0 ? max_out_px / 4 : max_out_px) / 256 + 1, 256));
   batch_composite_kernel<<<dim3(bx, nm), 256, 0, stream>>>(mos, thumbs, tw, th, adj);
   g_launches += 2;
   MG_CUDA(cudaGetLastError());

@@ -195,7 +195,9 @@ MG_HD void lab_pixel(const float* lut, const float* ms, float eps, float k1, flo
 
 MG_HD long long lab_quant(float v) {
 #if defined(__CUDA_ARCH__)
-  return __float2ll_rn(__fmul_rn(v, kLabQ));
+  // |v| <= 128, so v * 2^20 fits a 32-bit integer: the 32-bit conversion
+  // (round to nearest even, as llrint) is exact and cheaper than the 64-bit one.
+  return (long long)__float2int_rn(__fmul_rn(v, kLabQ));
 #else
   return (long long)std::llrintf(v * kLabQ);
 #endif
