@@ -111,6 +111,18 @@ float mg_lab_distance(const float a[3], const float b[3]);
 int mg_nearest_n(mg_ctx* ctx, const float* palette_lab, int p, const float* query_lab, int nq, int k,
                  uint32_t* idx_out, float* dist_out);
 
+/* How this context searches: MG_NEAREST_SCAN compares every query with every
+ * palette colour; MG_NEAREST_GRID first sorts the palette into a bucket grid
+ * over its Lab bounding box and compares each query only with the buckets
+ * that can hold its k nearest; MG_NEAREST_AUTO (the default) takes the grid
+ * for palettes of at least 2048 colours and 16k.  Results are identical.
+ * Applies to mg_nearest_n, mg_place_greedy, mg_generate and to palettes
+ * created afterwards (mg_palette_create builds the grid once). */
+#define MG_NEAREST_AUTO 0
+#define MG_NEAREST_SCAN 1
+#define MG_NEAREST_GRID 2
+int mg_ctx_set_nearest_method(mg_ctx* ctx, int method);
+
 /* ---- adjacency ------------------------------------------------------------------ */
 /* adjacency.rs:63-88 calculate_penalty for n (candidate, x, y) triples
  * (cxy: n*3 ints) against one grid; out: n floats (weighted). */
@@ -300,7 +312,8 @@ int mg_batch_read(mg_batch* batch, int i, mg_result* res);
 /* [0] cell statistics, [1] k-nearest, [2] walks + chains, [3] adjust +
  * composite, [4] total; ms of the last run. */
 int mg_batch_stage_ms(mg_batch* batch, float* ms, int cap);
-/* The launch shapes the autotuner picked. */
+/* The launch shapes the autotuner picked (nearest_chunk 0: the palette's
+ * bucket grid serves the k-nearest search, which has no chunk size). */
 int mg_batch_tuning(mg_batch* batch, int* cells_per_cta, int* nearest_chunk, int* workers_per_cta);
 int mg_batch_launches(mg_batch* batch);
 int mg_batch_destroy(mg_batch* batch);

@@ -69,6 +69,7 @@ struct mg_plan {
   DevBuf target, mats, regions, thumb_regions, thumbs, pal_lab, thumb_rgb, sim, cell_lab, cell_rgb, cand_idx,
       cand_dist, grid_greedy, resets, init_cost, greedy_job, chain_grids, chain_res, anneal_job, final_grid,
       finals_ptr, best_chain, adj, out, sums, err, usage, gather_src;
+  LabIndex index;  // bucket grid over pal_lab for the k-nearest search (when large)
   // Where the kernels read the target (a device copy, or pinned host memory in place).
   bool zero_copy = false;
   const uint8_t* target_ptr = nullptr;
@@ -204,6 +205,7 @@ int mg_ctx_destroy(mg_ctx* ctx) {
   for (DevBuf* b : {&ctx->in0, &ctx->in1, &ctx->in2, &ctx->out0, &ctx->out1, &ctx->out2, &ctx->sums, &ctx->regions,
                     &ctx->err, &ctx->lab_consts})
     b->release();
+  ctx->nn_index.release();
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return MG_OK;
@@ -215,6 +217,14 @@ int mg_ctx_sync(mg_ctx* ctx) {
 }
 
 void* mg_ctx_stream(mg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int mg_ctx_set_nearest_method(mg_ctx* ctx, int method) {
+  if (!ctx) return fail(MG_ERR_ARG, "null context");
+  if (method != MG_NEAREST_AUTO && method != MG_NEAREST_SCAN && method != MG_NEAREST_GRID)
+    return fail(MG_ERR_ARG, "unknown nearest method");
+  ctx->nearest_method = method;
+  return MG_OK;
+}
 
 void* mg_host_alloc(size_t bytes) {
   void* p = nullptr;
@@ -381,8 +391,9 @@ int mg_nearest_n(mg_ctx* ctx, const float* palette_lab, int p, const float* quer
   MG_CHECK(upload(ctx, ctx->in2, q.data(), sizeof(float4) * nq));
   MG_CHECK(ctx->out0.ensure(sizeof(uint32_t) * (size_t)nq * k));
   MG_CHECK(ctx->out1.ensure(sizeof(float) * (size_t)nq * k));
+  MG_CHECK(ctx->nn_index.build(ctx->in1.as<float4>(), p, ctx->nearest_method, k, ctx->stream));
   MG_CHECK(launch_nearest(ctx->in1.as<float4>(), p, ctx->in2.as<float4>(), nq, k, ctx->out0.as<uint32_t>(),
-                          ctx->out1.as<float>(), ctx->err.as<uint32_t>(), ctx->stream));
+                          ctx->out1.as<float>(), ctx->err.as<uint32_t>(), ctx->stream, 2048, &ctx->nn_index));
   if (p == 0) {
     MG_CHECK(finish(ctx));
     for (size_t i = 0; i < (size_t)nq * k; ++i) {
@@ -489,8 +500,9 @@ int mg_place_greedy(mg_ctx* ctx, const float* palette_lab, int p, const float* c
   MG_CHECK(ctx->out1.ensure(sizeof(float) * padded_cells(n) * k));
   MG_CHECK(ctx->out2.ensure(sizeof(int32_t) * n + 64));
   MG_CHECK(ctx->sums.ensure(sizeof(uint32_t) * p));
+  MG_CHECK(ctx->nn_index.build(ctx->in0.as<float4>(), p, ctx->nearest_method, k, ctx->stream));
   MG_CHECK(launch_nearest(ctx->in0.as<float4>(), p, ctx->in1.as<float4>(), n, k, ctx->out0.as<uint32_t>(),
-                          ctx->out1.as<float>(), ctx->err.as<uint32_t>(), ctx->stream));
+                          ctx->out1.as<float>(), ctx->err.as<uint32_t>(), ctx->stream, 2048, &ctx->nn_index));
   int32_t* d_grid = ctx->out2.as<int32_t>();
   int* d_resets = reinterpret_cast<int*>(d_grid + n);
   GreedyJob job{ctx->out0.as<uint32_t>(), ctx->out1.as<float>(), d_grid, gw, gh, k,
@@ -700,6 +712,7 @@ void plan_release(mg_plan* pl) {
                     &pl->anneal_job, &pl->final_grid, &pl->finals_ptr, &pl->best_chain, &pl->adj, &pl->out, &pl->sums, &pl->usage, &pl->gather_src,
                     &pl->err})
     b->release();
+  pl->index.release();
   if (pl->events)
     for (auto& e : pl->ev) cudaEventDestroy(e);
   pl->events = false;
@@ -916,9 +929,11 @@ int plan_run(mg_plan* pl) {
                                pl->cell_lab.as<float4>(), pl->cell_rgb.as<uchar4>(), pl->sums.as<RegionSums>(), 1, s));
   MG_CUDA(cudaEventRecord(pl->ev[3], s));
   // [3] k nearest per cell
-  if (P > 0)
+  if (P > 0) {
+    MG_CHECK(pl->index.build(pl->pal_lab.as<float4>(), P, ctx->nearest_method, pl->k, s));
     MG_CHECK(launch_nearest(pl->pal_lab.as<float4>(), P, pl->cell_lab.as<float4>(), N, pl->k, pl->cand_idx.as<uint32_t>(),
-                            pl->cand_dist.as<float>(), pl->err.as<uint32_t>(), s));
+                            pl->cand_dist.as<float>(), pl->err.as<uint32_t>(), s, 2048, &pl->index));
+  }
   MG_CUDA(cudaEventRecord(pl->ev[4], s));
   // [4] greedy placement
   if (P > 0) {

@@ -28,6 +28,7 @@ struct mg_palette {
   std::vector<int> selected;
   std::vector<Region> h_regions;
   DevBuf mats, regions, thumbs, thumb_regions, pal_lab, thumb_rgb, sim, sums;
+  LabIndex index;  // bucket grid over pal_lab for the k-nearest search (when large)
   bool has_sim = false;
   size_t device_bytes = 0;
 };
@@ -125,9 +126,11 @@ int palette_setup(mg_palette* pl, mg_ctx* ctx, const mg_palette_desc* d) {
       MG_CHECK(launch_similarity(pl->pal_lab.as<float4>(), P, 0, pl->sim.as<float>(), s));
       pl->has_sim = true;
     }
+    MG_CHECK(pl->index.build(pl->pal_lab.as<float4>(), P, ctx->nearest_method, std::min(P, 100), s));
   }
   MG_CHECK(finish(ctx));
-  pl->device_bytes = pl->mats.cap + pl->thumbs.cap + pl->pal_lab.cap + pl->thumb_rgb.cap + pl->sim.cap;
+  pl->device_bytes = pl->mats.cap + pl->thumbs.cap + pl->pal_lab.cap + pl->thumb_rgb.cap + pl->sim.cap +
+                     pl->index.hdr.cap + pl->index.sorted.cap + pl->index.start.cap;
   return MG_OK;
 }
 
@@ -310,7 +313,8 @@ int batch_enqueue(mg_batch* b, bool with_events) {
   if (with_events) MG_CUDA(record(b, b->ev[1], s));
   if (P > 0)
     MG_CHECK(launch_nearest(pal->pal_lab.as<float4>(), P, b->cell_lab.as<float4>(), b->total_cells, k,
-                            b->cand_idx.as<uint32_t>(), b->cand_dist.as<float>(), b->err.as<uint32_t>(), s, b->nn_chunk));
+                            b->cand_idx.as<uint32_t>(), b->cand_dist.as<float>(), b->err.as<uint32_t>(), s, b->nn_chunk,
+                            &pal->index));
   if (with_events) MG_CUDA(record(b, b->ev[2], s));
   if (P > 0) {
     // reset the queue: walk slots published, chain slots empty, counters
@@ -361,6 +365,7 @@ int batch_tune(mg_batch* b) {
   best = 1e30f;
   int best_nn = 2048;
   for (int ch : {1024, 2048, 4096}) {
+    if (b->pal->index.g > 0) break;  // the grid search has no chunk size
     b->nn_chunk = ch;
     MG_CHECK(batch_enqueue(b, true));
     MG_CUDA(cudaStreamSynchronize(s));
@@ -519,6 +524,7 @@ int mg_palette_destroy(mg_palette* pal) {
   cudaDeviceSynchronize();
   release({&pal->mats, &pal->regions, &pal->thumbs, &pal->thumb_regions, &pal->pal_lab, &pal->thumb_rgb, &pal->sim,
            &pal->sums});
+  pal->index.release();
   delete pal;
   return MG_OK;
 }
@@ -581,7 +587,7 @@ int mg_batch_stage_ms(mg_batch* b, float* ms, int cap) {
 int mg_batch_tuning(mg_batch* b, int* cells_per_cta, int* nearest_chunk, int* workers_per_cta) {
   if (!b) return fail(MG_ERR_ARG, "null batch");
   if (cells_per_cta) *cells_per_cta = b->cells_warps;
-  if (nearest_chunk) *nearest_chunk = b->nn_chunk;
+  if (nearest_chunk) *nearest_chunk = b->pal->index.g > 0 ? 0 : b->nn_chunk;
   if (workers_per_cta) *workers_per_cta = b->workers;
   return b->tuned ? MG_OK : fail(MG_ERR_STATE, "batch has not run");
 }

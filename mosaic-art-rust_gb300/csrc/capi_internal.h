@@ -10,6 +10,8 @@ struct mg_ctx {
   cudaStream_t stream = nullptr;
   mg::DevBuf in0, in1, in2, out0, out1, out2, sums, regions, err, lab_consts;
   mg_plan* gen_plan = nullptr;
+  int nearest_method = mg::kNearestAuto;  // MG_NEAREST_*
+  mg::LabIndex nn_index;                  // grid of the last single-call palette
 };
 
 namespace mg {

@@ -15,79 +15,16 @@
 //    bitonic-sorted and merged into the sorted top-k list (merge-path ranks).
 #include "mg_internal.h"
 #include "mg_ptx.cuh"
+#include "topk_warp.cuh"
 
 namespace mg {
 namespace {
 
 constexpr int kWarps = 16;
 constexpr int kThreads = kWarps * 32;
-constexpr int kListCap = 128;  // k <= 100
-constexpr int kBufCap = 128;   // candidate buffer; merged when it could overflow
-constexpr unsigned long long kMaxKey = ~0ull;
-
-struct WarpLists {
-  unsigned long long list[kListCap];
-  unsigned long long tmp[kListCap];
-  unsigned long long buf[kBufCap];
-};
 
 template <int kChunk>
 constexpr size_t smem_bytes() { return 2 * kChunk * sizeof(float4) + 16 + kWarps * sizeof(WarpLists); }
-
-__device__ __forceinline__ int lower_bound_u64(const unsigned long long* a, int n, unsigned long long key) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (a[mid] < key) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-
-// Sort buf[0..m) ascending (m a power of two, <= kBufCap) with a bitonic network.
-__device__ void warp_bitonic_sort(unsigned long long* buf, int m, int lane) {
-  for (int size = 2; size <= m; size <<= 1) {
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      for (int t = lane; t < (m >> 1); t += 32) {
-        int i = 2 * t - (t & (stride - 1));
-        int j = i + stride;
-        bool asc = (i & size) == 0;
-        unsigned long long a = buf[i], b = buf[j];
-        if ((a > b) == asc) {
-          buf[i] = b;
-          buf[j] = a;
-        }
-      }
-      __syncwarp();
-    }
-  }
-}
-
-// Merge the nbuf buffered keys into the sorted list (first k kept).
-__device__ void warp_merge(WarpLists& W, int& len, int& nbuf, unsigned long long& thr, int k, int lane) {
-  if (nbuf == 0) return;
-  int m = 1;
-  while (m < nbuf) m <<= 1;
-  for (int i = nbuf + lane; i < m; i += 32) W.buf[i] = kMaxKey;
-  __syncwarp();
-  warp_bitonic_sort(W.buf, m, lane);
-  for (int i = lane; i < len; i += 32) {
-    unsigned long long key = W.list[i];
-    int r = i + lower_bound_u64(W.buf, nbuf, key);
-    if (r < k) W.tmp[r] = key;
-  }
-  for (int j = lane; j < nbuf; j += 32) {
-    unsigned long long key = W.buf[j];
-    int r = j + lower_bound_u64(W.list, len, key);
-    if (r < k) W.tmp[r] = key;
-  }
-  __syncwarp();
-  len = min(k, len + nbuf);
-  for (int i = lane; i < len; i += 32) W.list[i] = W.tmp[i];
-  __syncwarp();
-  nbuf = 0;
-  thr = (len == k) ? W.list[k - 1] : kMaxKey;
-}
 
 template <int kChunk>  // palette entries per shared-memory stage
 __global__ void __launch_bounds__(kThreads) nearest_kernel(const float4* __restrict__ pal, int p,
@@ -245,7 +182,7 @@ int launch_nearest_t(const float4* pal, int p, const float4* queries, int nq, in
 }  // namespace
 
 int launch_nearest(const float4* pal, int p, const float4* queries, int nq, int k, uint32_t* idx, float* dist,
-                   uint32_t* err, cudaStream_t stream, int chunk) {
+                   uint32_t* err, cudaStream_t stream, int chunk, const LabIndex* index) {
   if (nq <= 0) return MG_OK;
   if (k <= 0 || k > 100) return fail(MG_ERR_ARG, "k must be in 1..100");
   const int keff = min(k, p);
@@ -253,6 +190,7 @@ int launch_nearest(const float4* pal, int p, const float4* queries, int nq, int 
     MG_CUDA(cudaMemsetAsync(idx, 0xFF, sizeof(uint32_t) * (size_t)nq * k, stream));
     return MG_OK;
   }
+  if (index && index->g > 0) return launch_nearest_grid(*index, queries, nq, keff, k, idx, dist, stream);
   if (chunk == 4096) return launch_nearest_t<4096>(pal, p, queries, nq, keff, k, idx, dist, err, stream);
   if (chunk == 1024) return launch_nearest_t<1024>(pal, p, queries, nq, keff, k, idx, dist, err, stream);
   return launch_nearest_t<2048>(pal, p, queries, nq, keff, k, idx, dist, err, stream);

@@ -79,8 +79,30 @@ int launch_thumbnails(const uint8_t* base, const Region* regions, int n, int tw,
 
 // (b) k nearest palette entries for every query (ties -> lowest index).
 // chunk: palette entries per shared-memory stage (1024, 2048 or 4096).
+// index: a grid built over `pal` (LabIndex::build); when it has buckets the
+// grid search runs instead of the scan.
+struct LabIndex;
 int launch_nearest(const float4* pal, int p, const float4* queries, int nq, int k, uint32_t* idx,
-                   float* dist, uint32_t* err, cudaStream_t stream, int chunk = 2048);
+                   float* dist, uint32_t* err, cudaStream_t stream, int chunk = 2048,
+                   const LabIndex* index = nullptr);
+
+// (b) the same search through a bucket grid over the palette's Lab colours
+// (k_nearest_grid.cu): identical results, far fewer distances for P >> k.
+enum NearestMethod { kNearestAuto = 0, kNearestScan = 1, kNearestGrid = 2 };
+struct LabGrid {
+  float lo[3], inv[3];  // bucket of v on axis c: floor((v - lo[c]) * inv[c]), clamped to [0, g)
+  int g, p;
+};
+struct LabIndex {
+  DevBuf hdr, sorted, start;  // LabGrid; P float4 (L, a, b, index bits) by bucket; g^3 + 1 ints
+  int g = 0;                  // buckets per axis; 0: no index (the scan runs)
+  int build(const float4* pal, int p, int method, int k, cudaStream_t s);
+  void release();
+};
+// Buckets per axis the method picks for a palette of p entries (0: scan).
+int lab_grid_dim(int method, int p, int k);
+int launch_nearest_grid(const LabIndex& index, const float4* queries, int nq, int keff, int k, uint32_t* idx,
+                        float* dist, cudaStream_t stream);
 
 // (c) similarity matrix, full (P x P) or strict upper triangle.
 int launch_similarity(const float4* pal, int p, int triangular, float* out, cudaStream_t stream);

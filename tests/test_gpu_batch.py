@@ -73,7 +73,7 @@ def test_batch_equals_single_mosaic_path(ctx):
             assert r.best_chain == res.best_chain and np.float32(r.final_cost) == np.float32(res.final_cost)
             assert r.n_resets == res.n_resets and r.palette_size == res.palette_size
     tune = batch.tuning()
-    assert tune["cells_per_cta"] in (4, 8) and tune["nearest_chunk"] in (1024, 2048, 4096)
+    assert tune["cells_per_cta"] in (4, 8) and tune["nearest_chunk"] in (0, 1024, 2048, 4096)
     assert tune["workers_per_cta"] in (1, 2, 4)
     assert len(batch.stage_ms()) == 5 and batch.launches() > 0
     # one-shot batch from host buffers
