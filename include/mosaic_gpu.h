@@ -313,7 +313,8 @@ int mg_batch_read(mg_batch* batch, int i, mg_result* res);
  * composite, [4] total; ms of the last run. */
 int mg_batch_stage_ms(mg_batch* batch, float* ms, int cap);
 /* The launch shapes the autotuner picked (nearest_chunk 0: the palette's
- * bucket grid serves the k-nearest search, which has no chunk size). */
+ * bucket grid serves the k-nearest search, which has no chunk size;
+ * workers_per_cta is 0: every chain runs as one CTA of the chain kernel). */
 int mg_batch_tuning(mg_batch* batch, int* cells_per_cta, int* nearest_chunk, int* workers_per_cta);
 int mg_batch_launches(mg_batch* batch);
 int mg_batch_destroy(mg_batch* batch);

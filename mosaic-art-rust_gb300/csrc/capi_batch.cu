@@ -7,10 +7,11 @@
 // mean RGB; here it stays in device memory and serves any number of mosaics.
 // A batch runs many mosaics over one palette through the batched pipeline of
 // k_batch.cu; after its first run the batch's launches are captured in a CUDA
-// graph and replayed.  The first run also autotunes three launch shapes by
+// graph and replayed.  The first run also autotunes two launch shapes by
 // timing each candidate on the batch itself: cells per CTA of the cell
-// statistics (4 or 8), palette chunk of the k-nearest scan (2048 or 4096
-// entries per shared-memory stage) and walk/chain workers per CTA (1, 2, 4).
+// statistics (4 or 8) and the palette chunk of the k-nearest scan (1024, 2048
+// or 4096 entries per shared-memory stage; none when the palette's bucket grid
+// serves the search).
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -37,17 +38,17 @@ struct mg_batch {
   mg_ctx* ctx = nullptr;
   int device = 0;  // destroy must not touch ctx, which may already be gone
   mg_palette* pal = nullptr;
-  int n = 0, total_cells = 0, max_gw = 0, max_cells = 0, max_out_px = 0;
-  unsigned total_items = 0;
+  int n = 0, total_cells = 0, max_gw = 0, max_cells = 0, max_sa_cells = 0, max_out_px = 0;
+  int total_chains = 0;
   std::vector<BatchMosaic> h_mos;
   std::vector<int> cells, out_w, out_h, chains;
   std::vector<size_t> out_off;
-  std::vector<unsigned long long> h_items0;  // the walk items, largest mosaic first
-  std::vector<unsigned> h_chains_left;
   DevBuf targets, mos, cell_lab, cell_rgb, cand_idx, cand_dist, grids, finals, chain_grids, results, resets,
-      init_cost, best, adj, out, q_items, q_ready, q_ctr, q_left, q_left0, err;
+      init_cost, best, adj, out, err, gjobs, usage, ajobs, chain_job, chain_id, finals_ptr;
+  // walk jobs (gjobs): the n_wide mosaics with rows of >= 8 cells first, then the rest
+  int n_wide = 0, wide_gw = 0, wide_cells = 0, narrow_gw = 0, narrow_cells = 0;
   // tuned launch shapes
-  int cells_warps = 8, nn_chunk = 2048, workers = 1;
+  int cells_warps = 8, nn_chunk = 2048;
   bool tuned = false;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -146,8 +147,8 @@ void batch_release(mg_batch* b) {
   for (auto& e : b->ev)
     if (e) cudaEventDestroy(e);
   release({&b->targets, &b->mos, &b->cell_lab, &b->cell_rgb, &b->cand_idx, &b->cand_dist, &b->grids, &b->finals,
-           &b->chain_grids, &b->results, &b->resets, &b->init_cost, &b->best, &b->adj, &b->out, &b->q_items,
-           &b->q_ready, &b->q_ctr, &b->q_left, &b->q_left0, &b->err});
+           &b->chain_grids, &b->results, &b->resets, &b->init_cost, &b->best, &b->adj, &b->out, &b->err,
+           &b->gjobs, &b->usage, &b->ajobs, &b->chain_job, &b->chain_id, &b->finals_ptr});
 }
 
 int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, int n, bool zero_copy) {
@@ -168,8 +169,8 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
   int64_t tgt_bytes = 0;
   size_t out_bytes = 0, chain_cells = 0, n_results = 0;
   int cell_base = 0, grid_base = 0;
-  b->total_items = (unsigned)n;
-  b->max_gw = b->max_cells = b->max_out_px = 0;
+  b->total_chains = 0;
+  b->max_gw = b->max_cells = b->max_sa_cells = b->max_out_px = 0;
   for (int i = 0; i < n; ++i) {
     const mg_mosaic& r = ms[i];
     const int64_t st = r.target_stride ? r.target_stride : 3ll * r.target_w;
@@ -218,9 +219,10 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
     n_results += M.chains;
     cell_base += (int)padded_cells(N);
     grid_base += N;
-    b->total_items += (unsigned)M.chains;
+    b->total_chains += M.chains;
     b->max_gw = std::max(b->max_gw, r.grid_w);
     b->max_cells = std::max(b->max_cells, N);
+    if (run_sa) b->max_sa_cells = std::max(b->max_sa_cells, N);
     b->max_out_px = std::max(b->max_out_px, b->out_w[i] * b->out_h[i]);
     if (run_sa && (size_t)N * 2 > 180 * 1024) return fail(MG_ERR_ARG, "mosaic too large for the annealer");
   }
@@ -240,11 +242,6 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
   MG_CHECK(b->best.ensure(sizeof(int) * std::max(n, 1)));
   MG_CHECK(b->adj.ensure(sizeof(float4) * std::max(cell_base, 1)));
   MG_CHECK(b->out.ensure(std::max<size_t>(out_bytes, 16)));
-  MG_CHECK(b->q_items.ensure(sizeof(unsigned long long) * std::max(b->total_items, 1u)));
-  MG_CHECK(b->q_ready.ensure(sizeof(unsigned) * std::max(b->total_items, 1u)));
-  MG_CHECK(b->q_ctr.ensure(16));
-  MG_CHECK(b->q_left.ensure(sizeof(unsigned) * std::max(n, 1)));
-  MG_CHECK(b->q_left0.ensure(sizeof(unsigned) * std::max(n, 1)));
   MG_CHECK(b->err.ensure(16));
   MG_CUDA(cudaMemsetAsync(b->err.p, 0, 16, s));
   // targets that are not read in place
@@ -274,18 +271,72 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
     rpos += M.chains;
   }
   MG_CHECK(upload(ctx, b->mos, b->h_mos.data(), sizeof(BatchMosaic) * std::max(n, 1)));
-  // queue: walk items largest mosaic first, published; chain slots empty
+  // largest mosaic first: walks, then chains
   std::vector<int> order(n);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return b->cells[a] > b->cells[c]; });
-  b->h_items0.assign(std::max(n, 1), 0ull);
-  for (int i = 0; i < n; ++i) b->h_items0[i] = (unsigned long long)order[i];  // type 0, chain 0, mosaic
-  b->h_chains_left.assign(std::max(n, 1), 0u);
-  for (int i = 0; i < n; ++i) b->h_chains_left[i] = (unsigned)b->chains[i];
-  MG_CUDA(cudaMemcpyAsync(b->q_left0.p, b->h_chains_left.data(), sizeof(unsigned) * std::max(n, 1),
-                          cudaMemcpyHostToDevice, s));
-  MG_CUDA(cudaMemcpyAsync(b->q_items.p, b->h_items0.data(), sizeof(unsigned long long) * std::max(n, 1),
-                          cudaMemcpyHostToDevice, s));
+  // walk jobs, wide rows first
+  std::vector<GreedyJob> jobs;
+  jobs.reserve(std::max(n, 1));
+  b->n_wide = b->wide_gw = b->wide_cells = b->narrow_gw = b->narrow_cells = 0;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int i : order) {
+      const BatchMosaic& M = b->h_mos[i];
+      if ((M.gw >= 8) != (pass == 0)) continue;
+      jobs.push_back(GreedyJob{b->cand_idx.as<uint32_t>() + (size_t)M.cell_base * k,
+                               b->cand_dist.as<float>() + (size_t)M.cell_base * k, M.grid, M.gw, M.gh, k, M.max_usage,
+                               M.weight, M.n_resets, M.init_cost});
+      if (pass == 0) {
+        ++b->n_wide;
+        b->wide_gw = std::max(b->wide_gw, M.gw);
+        b->wide_cells = std::max(b->wide_cells, M.n);
+      } else {
+        b->narrow_gw = std::max(b->narrow_gw, M.gw);
+        b->narrow_cells = std::max(b->narrow_cells, M.n);
+      }
+    }
+  }
+  MG_CHECK(upload(ctx, b->gjobs, jobs.data(), sizeof(GreedyJob) * std::max<size_t>(jobs.size(), 1)));
+  // counters in global memory for the one-warp walk when a palette's do not fit in shared memory
+  if (pal->P > 32768) MG_CHECK(b->usage.ensure(sizeof(uint32_t) * (size_t)n * pal->P));
+  // chain jobs (one per mosaic, in mosaic order: the selection writes best_chain[i]),
+  // the chains largest mosaic first, and the final-grid pointers
+  std::vector<AnnealJob> ajobs(std::max(n, 1));
+  std::vector<int32_t*> finals(std::max(n, 1), nullptr);
+  std::vector<int> cjob, cid;
+  cjob.reserve(std::max(b->total_chains, 1));
+  cid.reserve(std::max(b->total_chains, 1));
+  for (int i = 0; i < n; ++i) {
+    const BatchMosaic& M = b->h_mos[i];
+    AnnealJob& A = ajobs[i];
+    A = AnnealJob{};
+    A.grid_in = M.grid;
+    A.chain_grids = M.chain_grids;
+    A.results = M.results;
+    A.initial_cost = M.init_cost;
+    A.gw = M.gw;
+    A.gh = M.gh;
+    A.chains = M.chains;
+    A.iters = M.iters;
+    A.t0 = M.t0;
+    A.decay = M.decay;
+    A.key0 = M.key0;
+    A.key1 = M.key1;
+    A.stream = M.stream;
+    A.greedy_only = 0;
+    finals[i] = M.final_grid;
+  }
+  for (int i : order)
+    for (int c = 0; c < b->h_mos[i].chains; ++c) {
+      cjob.push_back(i);
+      cid.push_back(c);
+    }
+  cjob.resize(std::max<size_t>(cjob.size(), 1));
+  cid.resize(std::max<size_t>(cid.size(), 1));
+  MG_CHECK(upload(ctx, b->ajobs, ajobs.data(), sizeof(AnnealJob) * ajobs.size()));
+  MG_CHECK(upload(ctx, b->finals_ptr, finals.data(), sizeof(int32_t*) * finals.size()));
+  MG_CHECK(upload(ctx, b->chain_job, cjob.data(), sizeof(int) * cjob.size()));
+  MG_CHECK(upload(ctx, b->chain_id, cid.data(), sizeof(int) * cid.size()));
   for (auto& e : b->ev)
     if (!e) MG_CUDA(cudaEventCreate(&e));
   MG_CUDA(cudaStreamSynchronize(s));
@@ -317,17 +368,21 @@ int batch_enqueue(mg_batch* b, bool with_events) {
                             &pal->index));
   if (with_events) MG_CUDA(record(b, b->ev[2], s));
   if (P > 0) {
-    // reset the queue: walk slots published, chain slots empty, counters
-    MG_CUDA(cudaMemsetAsync(b->q_ready.p, 0, sizeof(unsigned) * b->total_items, s));
-    MG_CHECK(launch_fill_u32(b->q_ready.as<unsigned>(), (unsigned)n, 1u, s));
-    MG_CHECK(launch_fill_u32(b->q_ctr.as<unsigned>(), 1u, 0u, s));                 // head
-    MG_CHECK(launch_fill_u32(b->q_ctr.as<unsigned>() + 1, 1u, (unsigned)n, s));    // tail
-    MG_CUDA(cudaMemcpyAsync(b->q_left.p, b->q_left0.p, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, s));
-    BatchQueue q{b->q_items.as<unsigned long long>(), b->q_ready.as<unsigned>(), b->q_ctr.as<unsigned>(),
-                 b->q_ctr.as<unsigned>() + 1, b->q_left.as<unsigned>(), b->total_items, b->cand_idx.as<uint32_t>(),
-                 b->cand_dist.as<float>()};
-    MG_CHECK(launch_batch_place(pal->pal_lab.as<float4>(), P, b->mos.as<BatchMosaic>(), q, k, b->max_gw, b->max_cells,
-                                b->workers, b->err.as<uint32_t>(), s));
+    // every greedy walk: rows of >= 8 cells by the scouted walk, the rest one
+    // warp each (k_greedy.cu), largest mosaic first
+    uint32_t* usage = b->usage.cap ? b->usage.as<uint32_t>() : nullptr;
+    if (b->n_wide > 0)
+      MG_CHECK(launch_greedy(pal->pal_lab.as<float4>(), P, b->gjobs.as<GreedyJob>(), b->n_wide, k, b->wide_gw,
+                             b->wide_cells, usage, b->err.as<uint32_t>(), s));
+    if (b->n - b->n_wide > 0)
+      MG_CHECK(launch_greedy(pal->pal_lab.as<float4>(), P, b->gjobs.as<GreedyJob>() + b->n_wide, b->n - b->n_wide, k,
+                             b->narrow_gw, b->narrow_cells, usage ? usage + (size_t)b->n_wide * P : nullptr,
+                             b->err.as<uint32_t>(), s));
+    // every annealing chain of every mosaic (k_anneal.cu), then per mosaic the
+    // best chain -- or the greedy grid when it is not optimised -- as its final grid
+    MG_CHECK(launch_anneal(pal->pal_lab.as<float4>(), P, b->ajobs.as<AnnealJob>(), b->chain_job.as<int>(),
+                           b->chain_id.as<int>(), b->total_chains, b->max_sa_cells, s));
+    MG_CHECK(launch_select_best(b->ajobs.as<AnnealJob>(), n, b->finals_ptr.as<int32_t*>(), b->best.as<int>(), s));
   } else {
     MG_CUDA(cudaMemsetAsync(b->finals.p, 0xFF, b->finals.cap, s));
   }
@@ -376,19 +431,6 @@ int batch_tune(mg_batch* b) {
     }
   }
   b->nn_chunk = best_nn;
-  best = 1e30f;
-  int best_w = 1;
-  for (int w : {1, 2, 4}) {
-    b->workers = w;
-    MG_CHECK(batch_enqueue(b, true));
-    MG_CUDA(cudaStreamSynchronize(s));
-    const float t = elapsed(b->ev[2], b->ev[3]);
-    if (t < best) {
-      best = t;
-      best_w = w;
-    }
-  }
-  b->workers = best_w;
   b->tuned = true;
   return MG_OK;
 }
@@ -588,7 +630,7 @@ int mg_batch_tuning(mg_batch* b, int* cells_per_cta, int* nearest_chunk, int* wo
   if (!b) return fail(MG_ERR_ARG, "null batch");
   if (cells_per_cta) *cells_per_cta = b->cells_warps;
   if (nearest_chunk) *nearest_chunk = b->pal->index.g > 0 ? 0 : b->nn_chunk;
-  if (workers_per_cta) *workers_per_cta = b->workers;
+  if (workers_per_cta) *workers_per_cta = 0;  // chains run one CTA each, no persistent workers
   return b->tuned ? MG_OK : fail(MG_ERR_STATE, "batch has not run");
 }
 
@@ -659,8 +701,9 @@ int64_t server_request_bytes(const mg_palette* pal, const mg_mosaic* m) {
   const int64_t k = std::max(pal->k, 1);
   const int64_t chains = m->enable_optimization ? std::max(m->chains, 1) : 0;
   int64_t bytes = padded * (16 + 4 + 8 * k + 16) + N * 8 + chains * (N * 4 + 32) +
-                  N * pal->tw * pal->th * 3 + 4096;
+                  N * pal->tw * pal->th * 3 + 4096 + (int64_t)sizeof(GreedyJob);
   if (!device_view_or_device(m->target)) bytes += 3ll * m->target_w * m->target_h;
+  if (pal->P > 32768) bytes += 4ll * pal->P;  // the walk's counters in global memory
   return bytes;
 }
 

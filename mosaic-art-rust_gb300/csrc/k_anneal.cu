@@ -38,7 +38,7 @@ __global__ void select_best_kernel(const AnnealJob* __restrict__ jobs, int32_t* 
   __shared__ int s_best;
   const AnnealJob J = jobs[blockIdx.x];
   if (threadIdx.x == 0) {
-    int b = 0;
+    int b = J.chains > 0 ? 0 : -1;
     for (int c = 1; c < J.chains; ++c)
       if (J.results[c].final_cost < J.results[b].final_cost) b = c;
     s_best = b;
@@ -46,7 +46,7 @@ __global__ void select_best_kernel(const AnnealJob* __restrict__ jobs, int32_t* 
   }
   __syncthreads();
   const int n = J.gw * J.gh;
-  const int32_t* src = J.chain_grids + (size_t)s_best * n;
+  const int32_t* src = s_best < 0 ? J.grid_in : J.chain_grids + (size_t)s_best * n;
   int32_t* dst = finals[blockIdx.x];
   for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
 }

@@ -3,24 +3,15 @@
 // The per-mosaic path (main.rs:477-685 once per target) is sequential inside a
 // mosaic -- the greedy walk and each annealing chain -- so a single mosaic
 // cannot fill the GPU.  The batch runs the data-parallel stages once over the
-// cells of every mosaic (cell statistics, k-nearest, adjustment, composite) and
-// runs the sequential stages in one persistent launch whose warps pull work
-// items from a device queue:
-//   item (walk, m)      the greedy walk of mosaic m; on completion it publishes
-//                       the mosaic's K chain items (or its final grid when the
-//                       optimiser is off);
-//   item (chain, m, c)  annealing chain c of mosaic m; the last chain of a
-//                       mosaic to finish picks the lowest final cost (ties: the
-//                       lowest chain) and writes the final grid.
-// Walk items are queued largest mosaic first, so the longest walks start
-// first and short mosaics' chains fill the SMs while they run.  Every wait on
-// the queue is bounded (it sets an error word and the warp leaves).  Each item
-// is the same code as the single-mosaic kernels (greedy_walk.cuh,
-// anneal_chain.cuh), so batched results equal the one-mosaic-per-launch
-// results bit for bit.
-#include "anneal_chain.cuh"
+// cells of every mosaic (cell statistics and k-nearest here and in k_scan.cu /
+// k_nearest_grid.cu, adjustment and composite here), every greedy walk in one
+// launch of the walk kernels (k_greedy.cu: one three-CTA cluster per mosaic,
+// largest mosaic first), every annealing chain of every mosaic in one launch
+// of the chain kernel (k_anneal.cu: one CTA per chain) and one best-chain
+// selection per mosaic.  Each walk and chain is the single-mosaic code, so
+// batched results equal the one-mosaic-per-launch results bit for bit.
+#include "mg_internal.h"
 #include "composite.cuh"
-#include "greedy_walk.cuh"
 
 namespace mg {
 namespace {
@@ -98,114 +89,6 @@ __global__ void __launch_bounds__(32 * kWarps) batch_cells_kernel(const BatchMos
       lab_out[cell] = make_float4(lab_mean(aL, npx), lab_mean(aA, npx), lab_mean(aB, npx), 0.0f);
       rgb_out[cell] = make_uchar4((unsigned char)(sr / (unsigned)npx), (unsigned char)(sg / (unsigned)npx),
                                   (unsigned char)(sb / (unsigned)npx), 0);
-    }
-  }
-}
-
-__device__ __forceinline__ unsigned long long make_item(unsigned type, unsigned chain, unsigned m) {
-  return ((unsigned long long)type << 48) | ((unsigned long long)chain << 32) | m;
-}
-
-constexpr unsigned kMaxQueueSpins = 20u * 1000u * 1000u;  // with <= 1 us naps: ~20 s at most
-
-// Persistent walk + chain workers, kWorkers warps per CTA, each with its own
-// shared-memory slice of worker_smem bytes.
-template <bool kLabSmem, int kWorkers>
-__global__ void __launch_bounds__(32 * kWorkers) batch_place_kernel(const float4* __restrict__ pal, int p,
-                                                                    const BatchMosaic* __restrict__ mos, BatchQueue q,
-                                                                    int k, size_t worker_smem, uint32_t* err) {
-  extern __shared__ __align__(128) uint8_t smem[];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  uint8_t* my = smem + (size_t)w * worker_smem;
-  for (;;) {
-    unsigned slot = 0;
-    if (lane == 0) slot = atomicAdd(q.head, 1u);
-    slot = __shfl_sync(0xffffffffu, slot, 0);
-    if (slot >= q.total) break;
-    unsigned long long item = 0;
-    int ok = 1;
-    if (lane == 0) {
-      unsigned spins = 0, nap = 32;
-      while (((volatile unsigned*)q.ready)[slot] == 0u) {
-        __nanosleep(nap);
-        nap = nap < 1024 ? nap * 2 : 1024;
-        if (++spins > kMaxQueueSpins) {
-          ok = 0;
-          break;
-        }
-      }
-      __threadfence();
-      item = ((volatile unsigned long long*)q.items)[slot];
-    }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    if (!ok) {
-      if (lane == 0) atomicOr(err, kErrTimeout);
-      break;
-    }
-    item = __shfl_sync(0xffffffffu, item, 0);
-    const unsigned type = (unsigned)(item >> 48);
-    const int chain = (int)((item >> 32) & 0xFFFFu);
-    const int m = (int)(item & 0xFFFFFFFFu);
-    const BatchMosaic& M = mos[m];
-    if (type == 0) {
-      GreedyJob J{q.cand_idx + (size_t)M.cell_base * k, q.cand_dist + (size_t)M.cell_base * k, M.grid, M.gw, M.gh, k,
-                  M.max_usage, M.weight, M.n_resets, M.init_cost};
-      greedy_detail::greedy_walk<kLabSmem, true>(pal, p, J, my, nullptr, err);
-      __syncwarp();
-      if (M.run_sa && M.chains > 0) {
-        if (lane == 0) {
-          __threadfence();  // the grid and initial cost before the chain items
-          const unsigned base = atomicAdd(q.tail, (unsigned)M.chains);
-          for (int c = 0; c < M.chains; ++c) q.items[base + c] = make_item(1u, (unsigned)c, (unsigned)m);
-          __threadfence();
-          for (int c = 0; c < M.chains; ++c) atomicExch(q.ready + base + c, 1u);
-        }
-      } else {
-        for (int i = lane; i < M.n; i += 32) M.final_grid[i] = M.grid[i];
-        if (lane == 0) *M.best_chain = -1;
-      }
-    } else {
-      AnnealJob J{};
-      J.grid_in = M.grid;
-      J.chain_grids = M.chain_grids;
-      J.results = M.results;
-      J.initial_cost = M.init_cost;
-      J.gw = M.gw;
-      J.gh = M.gh;
-      J.chains = M.chains;
-      J.iters = M.iters;
-      J.t0 = M.t0;
-      J.decay = M.decay;
-      J.key0 = M.key0;
-      J.key1 = M.key1;
-      J.stream = M.stream;
-      J.greedy_only = 0;
-      anneal_detail::anneal_chain<kLabSmem>(pal, p, J, chain, my);
-      __syncwarp();
-      unsigned left = 0;
-      if (lane == 0) {
-        __threadfence();
-        left = atomicSub(q.chains_left + m, 1u);
-      }
-      left = __shfl_sync(0xffffffffu, left, 0);
-      if (left == 1u) {  // last chain of the mosaic: pick the best
-        __threadfence();
-        int b = 0;
-        if (lane == 0) {
-          float bf = __ldcg(&M.results[0].final_cost);
-          for (int c = 1; c < M.chains; ++c) {
-            const float f = __ldcg(&M.results[c].final_cost);
-            if (f < bf) {
-              bf = f;
-              b = c;
-            }
-          }
-          *M.best_chain = b;
-        }
-        b = __shfl_sync(0xffffffffu, b, 0);
-        const int32_t* src = M.chain_grids + (size_t)b * M.n;
-        for (int i = lane; i < M.n; i += 32) M.final_grid[i] = __ldcg(src + i);
-      }
     }
   }
 }
@@ -291,20 +174,6 @@ __global__ void __launch_bounds__(256) batch_composite_kernel(const BatchMosaic*
 
 }  // namespace
 
-namespace {
-__global__ void fill_u32_kernel(unsigned* p, unsigned n, unsigned v) {
-  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
-}
-}  // namespace
-
-int launch_fill_u32(unsigned* p, unsigned n, unsigned v, cudaStream_t stream) {
-  if (n == 0) return MG_OK;
-  fill_u32_kernel<<<std::min((n + 255) / 256, 1024u), 256, 0, stream>>>(p, n, v);
-  g_launches += 1;
-  MG_CUDA(cudaGetLastError());
-  return MG_OK;
-}
-
 int launch_batch_cells(const BatchMosaic* mos, int nm, int total_cells, const LabConsts* consts, float4* lab,
                        uchar4* rgb, int warps, cudaStream_t stream) {
   if (total_cells <= 0) return MG_OK;
@@ -316,47 +185,6 @@ int launch_batch_cells(const BatchMosaic* mos, int nm, int total_cells, const La
   g_launches += 1;
   MG_CUDA(cudaGetLastError());
   return MG_OK;
-}
-
-size_t batch_worker_smem(int k, int max_gw, int max_cells, int p, bool lab_smem) {
-  const size_t g = greedy_detail::greedy_smem_bytes(k, max_gw, p, lab_smem, true);
-  const size_t a = anneal_detail::anneal_smem_bytes(max_cells, p, lab_smem);
-  return ((g > a ? g : a) + 127) & ~(size_t)127;
-}
-
-int launch_batch_place(const float4* pal, int p, const BatchMosaic* mos, const BatchQueue& q, int k, int max_gw,
-                       int max_cells, int workers, uint32_t* err, cudaStream_t stream) {
-  constexpr size_t kMaxSmem = 227 * 1024;
-  bool lab_smem = true;
-  size_t ws = batch_worker_smem(k, max_gw, max_cells, p, true);
-  if (ws * workers > kMaxSmem) {
-    lab_smem = false;
-    ws = batch_worker_smem(k, max_gw, max_cells, p, false);
-  }
-  while (workers > 1 && ws * workers > kMaxSmem) workers >>= 1;
-  if (ws * workers > kMaxSmem) return fail(MG_ERR_ARG, "a mosaic of this batch is too large for one worker");
-  const size_t bytes = ws * workers;
-  int dev = 0, sms = 0, per_sm = 0;
-  MG_CUDA(cudaGetDevice(&dev));
-  MG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  auto go = [&](auto kernel) -> int {
-    MG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * workers, bytes));
-    if (per_sm < 1) return fail(MG_ERR_ARG, "batch worker does not fit on an SM");
-    const int grid = (int)std::min<long long>((long long)sms * per_sm, ((long long)q.total + workers - 1) / workers);
-    kernel<<<std::max(grid, 1), 32 * workers, bytes, stream>>>(pal, p, mos, q, k, ws, err);
-    g_launches += 1;
-    MG_CUDA(cudaGetLastError());
-    return MG_OK;
-  };
-  if (lab_smem) {
-    if (workers == 4) return go(batch_place_kernel<true, 4>);
-    if (workers == 2) return go(batch_place_kernel<true, 2>);
-    return go(batch_place_kernel<true, 1>);
-  }
-  if (workers == 4) return go(batch_place_kernel<false, 4>);
-  if (workers == 2) return go(batch_place_kernel<false, 2>);
-  return go(batch_place_kernel<false, 1>);
 }
 
 int launch_batch_finish(const BatchMosaic* mos, int nm, int total_cells, const uchar4* thumb_rgb,

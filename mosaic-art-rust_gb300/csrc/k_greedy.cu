@@ -61,7 +61,8 @@ constexpr int kScoutCtas = 2;               // CTAs 1..kScoutCtas of the cluster
 constexpr int kScouts = kWarps * kScoutCtas;  // every warp of the scout CTAs
 constexpr uint32_t kInvalidEpoch = 0xFFFFFFFFu;
 constexpr uint32_t kWalkPolls = 1u << 24;
-constexpr uint32_t kScoutPolls = 1u << 21;  // polls of about 1 us each
+constexpr uint32_t kScoutPolls = 1u << 22;  // polls of about 1 us each
+constexpr int kScoutLead = 80;             // records built at most this many cells ahead
 constexpr int kCostChunk = 2048;  // cells per pass of the final cost sum
 enum Ctrl { kProgress = 0, kEpoch = 1, kAbort = 2 };
 
@@ -212,6 +213,114 @@ __device__ int full_cell(LabFn lab, const uint32_t* __restrict__ ci, const float
   return t;
 }
 
+// full_cell with the whole candidate row (k <= 100: four entries per lane)
+// and the neighbours' Lab read at once, then the Lab of the candidates inside
+// the penalty window: two dependent memory round trips whatever the depth of
+// the first eligible entry.  Taken when the palette's Lab is read from global
+// memory, where a round trip costs most; the same decision as full_cell.
+template <class LabFn>
+__device__ int full_cell_rows(LabFn lab, const uint32_t* __restrict__ ci, const float* __restrict__ cd, int k, int p,
+                              int up, int left, uint32_t* usage, uint32_t max_usage, float weight, uint32_t* ctrl,
+                              uint32_t& epoch, int& resets, int lane) {
+  constexpr int kRounds = 4;  // ceil(100 / 32)
+  const bool use_pen = weight > 0.0f;
+  const float two_w = __fmul_rn(2.0f, weight);
+  const float kInf = __int_as_float(0x7f800000);
+  uint32_t tr[kRounds];
+  float dr[kRounds];
+#pragma unroll
+  for (int r = 0; r < kRounds; ++r) {
+    const int j = r * 32 + lane;
+    tr[r] = j < k ? __ldg(ci + j) : kNoCand;
+    dr[r] = j < k ? __ldg(cd + j) : kInf;
+  }
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 lab_up = use_pen && up >= 0 ? lab(up) : zero;
+  const float4 lab_left = use_pen && left >= 0 ? lab(left) : zero;
+  auto okf = [&](uint32_t t) { return t < (uint32_t)p && (int)t != up && (int)t != left && usage[t] < max_usage; };
+  int r0 = -1;
+  unsigned m = 0;
+#pragma unroll
+  for (int r = 0; r < kRounds; ++r) {
+    const unsigned mr = __ballot_sync(0xffffffffu, okf(tr[r]));
+    if (r0 < 0 && mr) {
+      r0 = r;
+      m = mr;
+    }
+  }
+  int t;
+  if (r0 >= 0) {
+    const int e0l = __ffs(m) - 1;
+    int win = r0 * 32 + e0l;
+    uint32_t t_win = 0;
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r)
+      if (r == r0) t_win = __shfl_sync(0xffffffffu, tr[r], e0l);
+    if (use_pen) {
+      float d0 = 0.0f;
+#pragma unroll
+      for (int r = 0; r < kRounds; ++r)
+        if (r == r0) d0 = __shfl_sync(0xffffffffu, dr[r], e0l);
+      const float b0 = __fadd_rn(d0, two_w);
+      // another eligible entry after e0 inside [d0, d0 + 2w): penalties decide
+      bool any_in = false;
+#pragma unroll
+      for (int r = 0; r < kRounds; ++r) any_in |= r * 32 + lane > win && dr[r] < b0 && okf(tr[r]);
+      if (__any_sync(0xffffffffu, any_in)) {
+        float4 lt[kRounds];
+        bool in[kRounds];
+#pragma unroll
+        for (int r = 0; r < kRounds; ++r) {
+          in[r] = r * 32 + lane >= win && dr[r] < b0 && okf(tr[r]);
+          lt[r] = in[r] ? lab((int)tr[r]) : zero;
+        }
+        uint32_t best_s = 0xFFFFFFFFu;
+#pragma unroll
+        for (int r = 0; r < kRounds; ++r) {
+          uint32_t sb = 0xFFFFFFFFu;
+          if (in[r]) {
+            float pen = 0.0f;
+            if (up >= 0) pen = __fadd_rn(pen, wgt(lt[r], lab_up));
+            if (left >= 0) pen = __fadd_rn(pen, wgt(lt[r], lab_left));
+            sb = __float_as_uint(__fadd_rn(dr[r], __fmul_rn(pen, weight)));
+          }
+          const uint32_t mn = __reduce_min_sync(0xffffffffu, sb);
+          if (mn < best_s) {  // strict: the earliest entry keeps a tie
+            best_s = mn;
+            const int l = __ffs(__ballot_sync(0xffffffffu, sb == mn)) - 1;
+            win = r * 32 + l;
+            t_win = __shfl_sync(0xffffffffu, tr[r], l);
+          }
+        }
+      }
+    }
+    t = (int)t_win;
+    __syncwarp();
+    if (lane == 0) usage[t] += 1u;
+  } else {
+    // main.rs:420-475: global reset, first candidate passing can_place, else nearest.
+    ++resets;
+    __syncwarp();
+    for (int i = lane; i < p; i += 32) usage[i] = 0;
+    t = -1;
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+      const int tj = (int)tr[r];
+      const unsigned mask = __ballot_sync(0xffffffffu, tr[r] != kNoCand && tj >= 0 && tj < p && tj != up && tj != left);
+      if (t < 0 && mask) t = __shfl_sync(0xffffffffu, tj, __ffs(mask) - 1);
+    }
+    if (t < 0) t = (int)__shfl_sync(0xffffffffu, tr[0], 0);
+    fence_cluster();
+    __syncwarp();
+    ++epoch;
+    if (lane == 0) {
+      usage[t] = 1u;
+      st_release_cluster(smem_u32(&ctrl[kEpoch]), epoch);
+    }
+  }
+  return t;
+}
+
 // The walker CTA's shared-memory layout (both CTAs compute it; the scouts map
 // it into the walker CTA's window).
 struct WalkerLayout {
@@ -269,16 +378,21 @@ __device__ bool scout_cells(int s, const GreedyJob& J, int p, uint8_t* smem, Sco
         d[r] = __ldg(cd + j);
       }
     }
-    // The cell above, once placed.  Each cell is written once, by a single
-    // 16-bit store, so a scout that sees a value sees the final one; and the
-    // walker read that cell's record before placing it (the placement depends
-    // on it), so the walker is done with the ring slot this record reuses.
-    int up = -1;
-    if (y > 0) {
-      const uint32_t a_up = r_cells + 2u * (uint32_t)(c - gw);
+    // Wait until the walker has placed cell c - min(gw, kScoutLead): the
+    // cell above is then placed, and the counters this record is filtered by
+    // are at most kScoutLead placements old (in a region of one colour a
+    // row's placements cap dozens of the nearest materials; a record built a
+    // whole row ahead would list none left).  Each cell is written once, by a
+    // single 16-bit store, so a scout that sees a value sees the final one; and
+    // the walker read that cell's record before placing it (the placement
+    // depends on it), so the walker is done with the ring slot this record
+    // reuses (the ring holds more than gw records).
+    const int lead = c - min(gw, kScoutLead);
+    uint32_t v_lead = kUnplaced;
+    if (lead >= 0) {
+      const uint32_t a_lead = r_cells + 2u * (uint32_t)lead;
       uint32_t polls = 0;
-      uint32_t v;
-      while ((v = ld_cluster_u16(a_up)) == kUnplaced) {
+      while ((v_lead = ld_cluster_u16(a_lead)) == kUnplaced) {
         if (ld_cluster_u32(r_abort)) return false;
         if (++polls > kScoutPolls) {
           if (lane == 0) {
@@ -289,8 +403,8 @@ __device__ bool scout_cells(int s, const GreedyJob& J, int p, uint8_t* smem, Sco
         }
         __nanosleep(1000);  // the scouts run far ahead: poll the walker's SM rarely
       }
-      up = (int)v;
     }
+    const int up = y == 0 ? -1 : lead == c - gw ? (int)v_lead : (int)ld_cluster_u16(r_cells + 2u * (uint32_t)(c - gw));
     const uint32_t ep0 = ld_acquire_cluster(r_epoch);
     int bf = 0, br = 0;
     float af = inf, ar = inf;  // distance of the 33rd entry
@@ -585,8 +699,12 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
       }
       if (!done) {
         const int up = y > 0 ? (int)cells[c - gw] : -1;
-        t = full_cell(lab, J.cand_idx + (size_t)c * k, J.cand_dist + (size_t)c * k, k, p, up,
-                      row_start ? -1 : last, usage, max_usage, weight, ctrl, epoch, resets, lane);
+        if (kLabSmem)
+          t = full_cell(lab, J.cand_idx + (size_t)c * k, J.cand_dist + (size_t)c * k, k, p, up,
+                        row_start ? -1 : last, usage, max_usage, weight, ctrl, epoch, resets, lane);
+        else
+          t = full_cell_rows(lab, J.cand_idx + (size_t)c * k, J.cand_dist + (size_t)c * k, k, p, up,
+                             row_start ? -1 : last, usage, max_usage, weight, ctrl, epoch, resets, lane);
         if (lane == 0) cells[c] = (uint16_t)t;
       }
     }

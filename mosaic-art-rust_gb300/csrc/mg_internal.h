@@ -141,6 +141,8 @@ struct AnnealJob {
 };
 int launch_anneal(const float4* pal, int p, const AnnealJob* jobs_dev, const int* chain_job_dev,
                   const int* chain_id_dev, int total_chains, int max_cells, cudaStream_t stream);
+// Per job: the chain with the lowest final cost (ties: the lowest chain) into
+// its final grid; a job with no chains copies grid_in and records -1.
 int launch_select_best(const AnnealJob* jobs_dev, int n_jobs, int32_t* const* final_grids_dev,
                        int* best_chain_dev, cudaStream_t stream);
 int launch_total_cost(const float4* pal, const int32_t* grid, int gw, int gh, float* out, cudaStream_t stream);
@@ -169,23 +171,9 @@ struct BatchMosaic {
   int* best_chain;
   uint8_t* out;           // (gh*th) x (gw*tw) x 3
 };
-struct BatchQueue {
-  unsigned long long* items;  // capacity total
-  unsigned* ready;            // per slot: 1 once published
-  unsigned* head;             // next slot to take
-  unsigned* tail;             // next slot to publish
-  unsigned* chains_left;      // per mosaic
-  unsigned total;             // walks + chains of the batch
-  const uint32_t* cand_idx;
-  const float* cand_dist;
-};
 const LabConsts& host_lab_consts();
-int launch_fill_u32(unsigned* p, unsigned n, unsigned v, cudaStream_t stream);
 int launch_batch_cells(const BatchMosaic* mos, int nm, int total_cells, const LabConsts* consts, float4* lab,
                        uchar4* rgb, int warps, cudaStream_t stream);
-size_t batch_worker_smem(int k, int max_gw, int max_cells, int p, bool lab_smem);
-int launch_batch_place(const float4* pal, int p, const BatchMosaic* mos, const BatchQueue& q, int k, int max_gw,
-                       int max_cells, int workers, uint32_t* err, cudaStream_t stream);
 int launch_batch_finish(const BatchMosaic* mos, int nm, int total_cells, const uchar4* thumb_rgb,
                         const uchar4* cell_rgb, float4* adj, const uint8_t* thumbs, int tw, int th, int max_out_px,
                         cudaStream_t stream);

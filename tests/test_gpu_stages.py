@@ -135,6 +135,25 @@ def test_greedy_bit_exact(ctx, orc, p, gw, gh, max_usage, weight):
     assert resets == rresets
 
 
+@pytest.mark.parametrize("p,gw,gh,max_usage,region", [
+    (12000, 60, 40, 4, "smooth"), (12000, 150, 20, 4, "flat"), (12000, 90, 30, 1, "flat"), (5000, 120, 25, 3, "flat")])
+def test_greedy_dense_palette_bit_exact(ctx, orc, p, gw, gh, max_usage, region):
+    """Palettes too large for the walker's shared memory (Lab read from global
+    memory) and regions of one colour, where a row of placements exhausts the
+    nearest materials: penalty windows, deep first entries and resets."""
+    rng = np.random.default_rng(p + gw + max_usage)
+    pal = rand_lab(rng, p)
+    base = rand_lab(rng, 1)[0]
+    step = 3.0 if region == "smooth" else 0.05
+    cells = (base + np.cumsum(rng.normal(0, step, (gw * gh, 3)), axis=0)).astype(np.float32)
+    grid, resets = ctx.place_greedy(pal, cells, gw, gh, max_usage, 0.25)
+    rgrid, rresets = orc.place_greedy(pal, cells, gw, gh, max_usage, 0.25)
+    assert np.array_equal(grid, rgrid)
+    assert resets == rresets
+    if region == "flat":
+        assert resets > 0
+
+
 # ---- (e) annealing --------------------------------------------------------------------------------------------------------
 @pytest.mark.parametrize("p,gw,gh,iters,chains,t0,decay,greedy", [
     (60, 12, 9, 3000, 4, 100.0, 0.99995, False), (30, 7, 5, 500, 3, 1.0, 0.95, False),
