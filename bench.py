@@ -154,7 +154,7 @@ KERNEL_OF_STAGE = {"palette_lab": "region_stats_kernel", "similarity": "similari
 # the limit is the latency of one decision), and the data-parallel ones.
 SEQUENTIAL = {"greedy": "latency of one placement decision (row-major walk, sequential by definition)",
               "anneal": "latency of one round of 16 proposals per chain (32 chains, sequential within a chain)"}
-DATA_PARALLEL = ["palette_lab", "cell_lab", "nearest", "similarity", "composite"]
+DATA_PARALLEL = ["palette_lab", "nearest", "similarity", "composite"]
 
 
 def traffic_from_profiles(kernel: str):
@@ -320,6 +320,10 @@ def run_ours(args, rank, world, local):
     achieved = alg[dom_name] / (mean_stage[dom] / 1000.0) / 1e9
     stages = {STAGES[s]: {"ms": round(float(mean_stage[s]), 4),
                           "gbs": round(alg[STAGES[s]] / max(mean_stage[s], 1e-9) / 1e6, 1)} for s in range(7)}
+    # cell Lab runs on a second stream beside palette Lab and similarity: its
+    # stage time is only the part that outlasts them, not a kernel duration
+    stages["cell_lab"] = {"ms": stages["cell_lab"]["ms"], "gbs": None,
+                          "note": "runs beside palette_lab and similarity; ms is the part that outlasts them"}
     line = {
         "metric": METRIC, "value": value, "unit": "tiles/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",

@@ -246,7 +246,9 @@ int mg_plan_read(mg_plan* plan, mg_result* res);
 int mg_plan_destroy(mg_plan* plan);
 /* Device time of each stage of the last mg_plan_run, in ms (CUDA events):
  * [0] material Lab, [1] similarity, [2] cell Lab, [3] nearest, [4] greedy,
- * [5] anneal, [6] composite, [7] total.  Returns the count written. */
+ * [5] anneal, [6] composite, [7] total.  Cell Lab runs on a second stream
+ * beside [0] and [1]; [2] is the part of it that outlasts them.  Returns the
+ * count written. */
 int mg_plan_stage_ms(mg_plan* plan, float* ms, int cap);
 /* Number of kernels one mg_plan_run launches. */
 int mg_plan_launches(mg_plan* plan);

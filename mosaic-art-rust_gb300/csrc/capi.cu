@@ -68,13 +68,13 @@ struct mg_plan {
   // device buffers
   DevBuf target, mats, regions, thumb_regions, thumbs, pal_lab, thumb_rgb, sim, cell_lab, cell_rgb, cand_idx,
       cand_dist, grid_greedy, resets, init_cost, greedy_job, chain_grids, chain_res, anneal_job, final_grid,
-      finals_ptr, best_chain, adj, out, sums, err, usage, gather_src;
+      finals_ptr, best_chain, adj, out, sums, cell_sums, err, usage, gather_src;
   LabIndex index;  // bucket grid over pal_lab for the k-nearest search (when large)
   // Where the kernels read the target (a device copy, or pinned host memory in place).
   bool zero_copy = false;
   const uint8_t* target_ptr = nullptr;
   int64_t target_stride = 0;
-  cudaEvent_t ev[8] = {};
+  cudaEvent_t ev[9] = {};  // stage boundaries [0..7]; [8] joins the side stream
   bool events = false;
   int launches = 0;
   bool ran = false;
@@ -182,7 +182,9 @@ int mg_ctx_create(int device, mg_ctx** out) {
   mg_ctx* c = new mg_ctx();
   c->device = device;
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
+    if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return cuda_fail(e, "cudaStreamCreate");
   }
@@ -206,6 +208,10 @@ int mg_ctx_destroy(mg_ctx* ctx) {
                     &ctx->err, &ctx->lab_consts})
     b->release();
   ctx->nn_index.release();
+  if (ctx->side) {
+    cudaStreamSynchronize(ctx->side);
+    cudaStreamDestroy(ctx->side);
+  }
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return MG_OK;
@@ -709,7 +715,7 @@ void plan_release(mg_plan* pl) {
   for (DevBuf* b : {&pl->target, &pl->mats, &pl->regions, &pl->thumb_regions, &pl->thumbs, &pl->pal_lab,
                     &pl->thumb_rgb, &pl->sim, &pl->cell_lab, &pl->cell_rgb, &pl->cand_idx, &pl->cand_dist,
                     &pl->grid_greedy, &pl->resets, &pl->init_cost, &pl->greedy_job, &pl->chain_grids, &pl->chain_res,
-                    &pl->anneal_job, &pl->final_grid, &pl->finals_ptr, &pl->best_chain, &pl->adj, &pl->out, &pl->sums, &pl->usage, &pl->gather_src,
+                    &pl->anneal_job, &pl->final_grid, &pl->finals_ptr, &pl->best_chain, &pl->adj, &pl->out, &pl->sums, &pl->cell_sums, &pl->usage, &pl->gather_src,
                     &pl->err})
     b->release();
   pl->index.release();
@@ -861,7 +867,8 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r, bool zero_copy) {
   MG_CHECK(pl->best_chain.ensure(16));
   MG_CHECK(pl->adj.ensure(sizeof(float4) * N));
   MG_CHECK(pl->out.ensure(tb * N));
-  MG_CHECK(pl->sums.ensure(sizeof(RegionSums) * std::max(N, std::max(P, 1))));
+  MG_CHECK(pl->sums.ensure(sizeof(RegionSums) * std::max(P, 1)));
+  MG_CHECK(pl->cell_sums.ensure(sizeof(RegionSums) * std::max(N, 1)));
   MG_CHECK(pl->err.ensure(16));
   MG_CUDA(cudaMemsetAsync(pl->err.p, 0, 16, s));
   MG_CUDA(cudaMemsetAsync(pl->resets.p, 0, 16, s));
@@ -904,6 +911,14 @@ int plan_run(mg_plan* pl) {
   const unsigned long long l0 = g_launches;
   const int P = pl->P, N = pl->N;
   MG_CUDA(cudaEventRecord(pl->ev[0], s));
+  // [2] cell Lab + cell mean RGB needs only the target: on the side stream,
+  // overlapping [0] and [1]; joined back before [3]
+  cudaStream_t s2 = ctx->side;
+  MG_CUDA(cudaStreamWaitEvent(s2, pl->ev[0], 0));
+  CellGeom g{pl->gw, pl->gh, pl->cw, pl->ch, pl->target_stride};
+  MG_CHECK(launch_region_stats(pl->target_ptr, &g, nullptr, N, (int64_t)pl->cw * pl->ch, pl->cell_lab.as<float4>(),
+                               pl->cell_rgb.as<uchar4>(), pl->cell_sums.as<RegionSums>(), 1, s2));
+  MG_CUDA(cudaEventRecord(pl->ev[8], s2));
   // [0] palette ingestion: thumbnails (when not given), material Lab, thumbnail means
   if (P > 0) {
     if (pl->device_thumbs)
@@ -923,10 +938,8 @@ int plan_run(mg_plan* pl) {
   if (pl->build_sim && P > 0)
     MG_CHECK(launch_similarity(pl->pal_lab.as<float4>(), P, 0, pl->sim.as<float>(), s));
   MG_CUDA(cudaEventRecord(pl->ev[2], s));
-  // [2] cell Lab + cell mean RGB
-  CellGeom g{pl->gw, pl->gh, pl->cw, pl->ch, pl->target_stride};
-  MG_CHECK(launch_region_stats(pl->target_ptr, &g, nullptr, N, (int64_t)pl->cw * pl->ch,
-                               pl->cell_lab.as<float4>(), pl->cell_rgb.as<uchar4>(), pl->sums.as<RegionSums>(), 1, s));
+  // [2] (the rest of) cell Lab: the join
+  MG_CUDA(cudaStreamWaitEvent(s, pl->ev[8], 0));
   MG_CUDA(cudaEventRecord(pl->ev[3], s));
   // [3] k nearest per cell
   if (P > 0) {

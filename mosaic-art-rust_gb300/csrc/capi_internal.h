@@ -8,6 +8,7 @@
 struct mg_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // forked from `stream` for stages that can overlap, joined back
   mg::DevBuf in0, in1, in2, out0, out1, out2, sums, regions, err, lab_consts;
   mg_plan* gen_plan = nullptr;
   int nearest_method = mg::kNearestAuto;  // MG_NEAREST_*
