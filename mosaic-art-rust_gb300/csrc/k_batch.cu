@@ -113,62 +113,39 @@ __global__ void batch_adjust_kernel(const BatchMosaic* __restrict__ mos, int nm,
   adj[cell] = r;
 }
 
-// blockIdx.y = mosaic; a grid-stride loop over its output pixels, four per
-// thread when the tile width allows (composite.cuh).
-__global__ void __launch_bounds__(256) batch_composite_kernel(const BatchMosaic* __restrict__ mos,
-                                                              const uint8_t* __restrict__ thumbs, int tw, int th,
-                                                              const float4* __restrict__ adj) {
-  __shared__ float s_unit[256];
-  s_unit[threadIdx.x] = u8_unit(threadIdx.x);
-  __syncthreads();
-  const BatchMosaic& M = mos[blockIdx.y];
-  const int ow = M.gw * tw, oh = M.gh * th;
-  const bool do_adj = M.strength > 0.0f;
-  if ((tw & 3) == 0) {
-    const int gpr = ow >> 2, total = gpr * oh;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
-      const int oy = q / gpr, ox = (q - oy * gpr) << 2;
-      const int cy = oy / th, cx = ox / tw;
-      const int local = cy * M.gw + cx;
-      const int g = M.final_grid[local];
-      uint8_t* d = M.out + ((size_t)oy * ow + ox) * 3;
-      if (g < 0) {
-        uint32_t* dw = reinterpret_cast<uint32_t*>(d);
-        dw[0] = dw[1] = dw[2] = 0u;
-        continue;
-      }
-      const uint8_t* src = thumbs + (((size_t)g * th + (oy - cy * th)) * tw + (ox - cx * tw)) * 3;
-      Adjust a{0.0f, 1.0f, 0.0f, 1.0f};
-      if (do_adj) {
-        const float4 a4 = adj[M.cell_base + local];
-        a = Adjust{a4.x, a4.y, a4.z, a4.w};
-      }
-      composite_group4(src, d, do_adj, a, s_unit);
+// One CTA per tile (cell) of any mosaic; CTA b takes a contiguous run of the
+// flat cell index, so its mosaic is found once and then advanced.  Tables of
+// tiles alternate between two shared buffers (one barrier per tile, taken by
+// every CTA thread on every pass, padding cells included).
+__global__ void __launch_bounds__(256) batch_composite_kernel(const BatchMosaic* __restrict__ mos, int nm,
+                                                              int total_cells, const uint8_t* __restrict__ thumbs,
+                                                              int tw, int th, const float4* __restrict__ adj) {
+  __shared__ float s_bc[2][256];
+  const int per = (total_cells + gridDim.x - 1) / gridDim.x;
+  const int c0 = blockIdx.x * per, c1 = min(total_cells, c0 + per);
+  int mi = c0 < c1 ? find_mosaic(mos, nm, c0) : 0;
+  int it = 0;
+  for (int c = c0; c < c1; ++c, ++it) {
+    while (mi + 1 < nm && mos[mi + 1].cell_base <= c) ++mi;
+    const BatchMosaic& M = mos[mi];
+    const int local = c - M.cell_base;
+    const bool real = local < M.n;  // else a padding cell
+    const int g = real ? M.final_grid[local] : -1;
+    const bool adjust = M.strength > 0.0f;
+    float* bc = s_bc[it & 1];
+    Adjust a{0.0f, 1.0f, 0.0f, 1.0f};
+    if (adjust && g >= 0) {
+      const float4 a4 = adj[c];
+      a = Adjust{a4.x, a4.y, a4.z, a4.w};
+      tile_bc_table(bc, a);
     }
-    return;
-  }
-  const int64_t total = (int64_t)ow * oh;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int oy = (int)(t / ow), ox = (int)(t - (int64_t)oy * ow);
-    const int cy = oy / th, cx = ox / tw;
-    const int local = cy * M.gw + cx;
-    const int g = M.final_grid[local];
-    uint8_t o0 = 0, o1 = 0, o2 = 0;
-    if (g >= 0) {
-      const uint8_t* s = thumbs + ((size_t)g * th * tw + (size_t)(oy - cy * th) * tw + (ox - cx * tw)) * 3;
-      o0 = s[0];
-      o1 = s[1];
-      o2 = s[2];
-      if (do_adj) {
-        const float4 a4 = adj[M.cell_base + local];
-        const Adjust a{a4.x, a4.y, a4.z, a4.w};
-        adjust_pixel(a, s_unit[o0], s_unit[o1], s_unit[o2], o0, o1, o2);
-      }
-    }
-    uint8_t* d = M.out + t * 3;
-    d[0] = o0;
-    d[1] = o1;
-    d[2] = o2;
+    __syncthreads();
+    if (!real) continue;
+    const size_t pitch = (size_t)M.gw * tw * 3;
+    const int cy = local / M.gw, cx = local - cy * M.gw;
+    uint8_t* dst = M.out + (size_t)cy * th * pitch + (size_t)cx * tw * 3;
+    const uint8_t* src = g >= 0 ? thumbs + (size_t)g * tw * th * 3 : nullptr;
+    composite_tile(src, dst, tw, th, pitch, adjust, a, bc);
   }
 }
 
@@ -192,8 +169,11 @@ int launch_batch_finish(const BatchMosaic* mos, int nm, int total_cells, const u
                         cudaStream_t stream) {
   if (nm <= 0) return MG_OK;
   batch_adjust_kernel<<<(total_cells + 255) / 256, 256, 0, stream>>>(mos, nm, total_cells, thumb_rgb, cell_rgb, adj);
-  const int bx = std::max(1, std::min(((tw & 3) == 0 ? max_out_px / 4 : max_out_px) / 256 + 1, 256));
-  batch_composite_kernel<<<dim3(bx, nm), 256, 0, stream>>>(mos, thumbs, tw, th, adj);
+  int dev = 0, sms = 0;
+  MG_CUDA(cudaGetDevice(&dev));
+  MG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = std::max(1, std::min(total_cells, sms * 8));
+  batch_composite_kernel<<<blocks, tile_threads(tw, th), 0, stream>>>(mos, nm, total_cells, thumbs, tw, th, adj);
   g_launches += 2;
   MG_CUDA(cudaGetLastError());
   return MG_OK;

@@ -33,63 +33,32 @@ __global__ void cell_adjust_kernel(const int32_t* __restrict__ grid, int n, cons
   adj[c] = r;
 }
 
+// One CTA per tile (cell), grid-stride over the cells; the brightness/contrast
+// table of a tile is built in one of two shared buffers, so one barrier per
+// tile orders the build before the lookups and the previous tile's lookups
+// before the next build.
 template <bool kAdjust>
 __global__ void __launch_bounds__(256) composite_kernel(const int32_t* __restrict__ grid, int gw, int gh,
                                                         const uint8_t* __restrict__ thumbs, int tw, int th,
                                                         const float4* __restrict__ adj, uint8_t* __restrict__ out) {
-  __shared__ float s_unit[256];
-  if (kAdjust) {
-    s_unit[threadIdx.x] = u8_unit(threadIdx.x);
-    __syncthreads();
-  }
-  const int ow = gw * tw, oh = gh * th;
-  if ((tw & 3) == 0) {
-    // four pixels per thread, 32-bit index arithmetic (checked on the host)
-    const int gpr = ow >> 2, total = gpr * oh;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
-      const int oy = q / gpr, ox = (q - oy * gpr) << 2;
-      const int cy = oy / th, cx = ox / tw;
-      const int c = cy * gw + cx;
-      const int m = grid[c];
-      uint8_t* d = out + ((size_t)oy * ow + ox) * 3;
-      if (m < 0) {
-        uint32_t* dw = reinterpret_cast<uint32_t*>(d);
-        dw[0] = dw[1] = dw[2] = 0u;
-        continue;
-      }
-      const uint8_t* src = thumbs + (((size_t)m * th + (oy - cy * th)) * tw + (ox - cx * tw)) * 3;
-      Adjust a{0.0f, 1.0f, 0.0f, 1.0f};
-      if (kAdjust) {
-        const float4 a4 = adj[c];
-        a = Adjust{a4.x, a4.y, a4.z, a4.w};
-      }
-      composite_group4(src, d, kAdjust, a, s_unit);
-    }
-    return;
-  }
-  const int64_t total = (int64_t)ow * oh;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int oy = (int)(t / ow), ox = (int)(t - (int64_t)oy * ow);
-    const int cy = oy / th, cx = ox / tw;
-    const int dy = oy - cy * th, dx = ox - cx * tw;
-    const int c = cy * gw + cx;
+  __shared__ float s_bc[2][256];
+  const int n = gw * gh;
+  const size_t pitch = (size_t)gw * tw * 3;
+  int it = 0;
+  for (int c = blockIdx.x; c < n; c += gridDim.x, ++it) {
     const int m = grid[c];
-    uint8_t o0 = 0, o1 = 0, o2 = 0;
-    if (m >= 0) {
-      const uint8_t* s = thumbs + ((size_t)m * th * tw + (size_t)dy * tw + dx) * 3;
-      o0 = s[0];
-      o1 = s[1];
-      o2 = s[2];
-      if (kAdjust) {
-        const float4 a4 = adj[c];
-        const Adjust a{a4.x, a4.y, a4.z, a4.w};
-        adjust_pixel(a, s_unit[o0], s_unit[o1], s_unit[o2], o0, o1, o2);
-      }
+    float* bc = s_bc[it & 1];
+    Adjust a{0.0f, 1.0f, 0.0f, 1.0f};
+    if (kAdjust && m >= 0) {
+      const float4 a4 = adj[c];
+      a = Adjust{a4.x, a4.y, a4.z, a4.w};
+      tile_bc_table(bc, a);
     }
-    uint8_t* d = out + t * 3;
-    d[0] = o0;
-    d[1] = o1;
-    d[2] = o2;
+    __syncthreads();
+    const int cy = c / gw, cx = c - cy * gw;
+    uint8_t* dst = out + (size_t)cy * th * pitch + (size_t)cx * tw * 3;
+    const uint8_t* src = m >= 0 ? thumbs + (size_t)m * tw * th * 3 : nullptr;
+    composite_tile(src, dst, tw, th, pitch, kAdjust, a, bc);
   }
 }
 
@@ -141,10 +110,14 @@ int launch_composite(const int32_t* grid, int gw, int gh, const uint8_t* thumbs,
                      int do_adjust, uint8_t* out, cudaStream_t stream) {
   const int64_t total = (int64_t)gw * tw * gh * th;
   if (total <= 0) return MG_OK;
-  if ((tw & 3) == 0 && total / 4 > 0x7FFFFFFFll) return fail(MG_ERR_ARG, "output image too large");
-  const unsigned blocks = grid_for((tw & 3) == 0 ? total / 4 : total);
-  if (do_adjust) composite_kernel<true><<<blocks, 256, 0, stream>>>(grid, gw, gh, thumbs, tw, th, adj, out);
-  else composite_kernel<false><<<blocks, 256, 0, stream>>>(grid, gw, gh, thumbs, tw, th, adj, out);
+  int dev = 0, sms = 0;
+  MG_CUDA(cudaGetDevice(&dev));
+  MG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int cells = gw * gh;
+  const unsigned blocks = (unsigned)std::max(1, std::min(cells, sms * 8));
+  const int threads = tile_threads(tw, th);
+  if (do_adjust) composite_kernel<true><<<blocks, threads, 0, stream>>>(grid, gw, gh, thumbs, tw, th, adj, out);
+  else composite_kernel<false><<<blocks, threads, 0, stream>>>(grid, gw, gh, thumbs, tw, th, adj, out);
   g_launches += 1;
   MG_CUDA(cudaGetLastError());
   return MG_OK;

@@ -250,7 +250,9 @@ MG_HD void rgb_to_hsv(float r, float g, float b, float& h, float& s, float& v) {
 }
 
 MG_HD void hsv_to_rgb(float hue, float s, float v, float& r, float& g, float& b) {
-  float pos = MG_SUB(hue, MG_MUL(MG_FLOOR(MG_DIV(hue, 360.0f)), 360.0f));
+  // hue - floor(hue / 360) * 360: for 0 < hue < 360 the rounded quotient is
+  // below 1 (at most 1 - 2^-24), so the expression is hue itself.
+  float pos = (hue > 0.0f && hue < 360.0f) ? hue : MG_SUB(hue, MG_MUL(MG_FLOOR(MG_DIV(hue, 360.0f)), 360.0f));
   float c = MG_MUL(v, s);
   float h = MG_DIV(pos, 60.0f);
   float hm2 = MG_SUB(h, MG_MUL(MG_FLOOR(MG_MUL(h, 0.5f)), 2.0f));
@@ -311,16 +313,28 @@ MG_HD float brightness_contrast(float v, float brightness, float contrast) {
   return rclamp(MG_ADD(c, brightness), 0.0f, 1.0f);
 }
 
-// color_adjustment.rs:53-87 adjust_pixel.  `unit` maps a byte to v/255.
-MG_HD void adjust_pixel(const Adjust& a, float r, float g, float b, uint8_t& o0, uint8_t& o1, uint8_t& o2) {
-  float c0 = brightness_contrast(r, a.brightness, a.contrast);
-  float c1 = brightness_contrast(g, a.brightness, a.contrast);
-  float c2 = brightness_contrast(b, a.brightness, a.contrast);
+// fmod(x, 360).  For |x| < 720 it is x itself below 360 in magnitude, else
+// x -+ 360 with x's sign, which is exact (Sterbenz: 360 <= |x| <= 720).
+// adjust_pixel's hues stay within (-240, 540).
+MG_HD float fmod_360(float x) {
+  const float ax = x < 0.0f ? -x : x;
+  if (ax < 360.0f) return x;
+  if (ax < 720.0f) {
+    const float r = MG_SUB(ax, 360.0f);
+    return x < 0.0f ? -r : r;
+  }
+  return MG_FMOD(x, 360.0f);
+}
+
+// color_adjustment.rs:53-87 adjust_pixel after the brightness/contrast step:
+// c0..c2 are brightness_contrast of the pixel's channels (a function of the
+// byte alone, so the composite tabulates it per tile).
+MG_HD void adjust_from_bc(const Adjust& a, float c0, float c1, float c2, uint8_t& o0, uint8_t& o1, uint8_t& o2) {
   if (a.hue_shift != 0.0f || a.saturation != 1.0f) {
     float h, s, v;
     rgb_to_hsv(c0, c1, c2, h, s, v);
     float hh = MG_ADD(h, a.hue_shift);
-    float rem = MG_FMOD(hh, 360.0f);
+    float rem = fmod_360(hh);
     if (rem < 0.0f) rem = MG_ADD(rem, 360.0f);
     float ss = rclamp(MG_MUL(s, a.saturation), 0.0f, 1.0f);
     hsv_to_rgb(rem, ss, v, c0, c1, c2);
@@ -328,6 +342,12 @@ MG_HD void adjust_pixel(const Adjust& a, float r, float g, float b, uint8_t& o0,
   o0 = as_u8(rclamp(MG_MUL(c0, 255.0f), 0.0f, 255.0f));
   o1 = as_u8(rclamp(MG_MUL(c1, 255.0f), 0.0f, 255.0f));
   o2 = as_u8(rclamp(MG_MUL(c2, 255.0f), 0.0f, 255.0f));
+}
+
+// color_adjustment.rs:53-87 adjust_pixel.  r, g, b are the channels as v/255.
+MG_HD void adjust_pixel(const Adjust& a, float r, float g, float b, uint8_t& o0, uint8_t& o1, uint8_t& o2) {
+  adjust_from_bc(a, brightness_contrast(r, a.brightness, a.contrast), brightness_contrast(g, a.brightness, a.contrast),
+                 brightness_contrast(b, a.brightness, a.contrast), o0, o1, o2);
 }
 
 }  // namespace mg

@@ -217,10 +217,11 @@ def test_apply_adjustment_bit_exact(ctx, orc, adj):
             assert np.array_equal(out[y, x], orc.adjust_pixel(a, img[y, x])), (y, x)
 
 
-@pytest.mark.parametrize("strength", [0.0, 0.4])
-def test_composite_bit_exact(ctx, orc, strength):
-    rng = np.random.default_rng(21)
-    p, gw, gh, tw, th = 30, 9, 7, 12, 10
+@pytest.mark.parametrize("strength", [0.0, 0.4, 1.0])
+@pytest.mark.parametrize("tw,th", [(12, 10), (7, 5), (48, 48)])
+def test_composite_bit_exact(ctx, orc, strength, tw, th):
+    rng = np.random.default_rng(21 + tw)
+    p, gw, gh = 30, 9, 7
     thumbs = rng.integers(0, 256, (p, th, tw, 3)).astype(np.uint8)
     grid = rng.integers(-1, p, (gh, gw)).astype(np.int32)
     cell_rgb = rng.integers(0, 256, (gh * gw, 3)).astype(np.uint8)
