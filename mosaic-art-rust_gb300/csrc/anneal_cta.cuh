@@ -39,6 +39,7 @@ constexpr int kChainWarps = 4;
 constexpr int kThreads = kChainWarps * 32;
 constexpr int kRound = kChainWarps * 4;  // proposals per round (8 lanes each)
 constexpr int kCtaRing = 4 * kThreads;   // decoded proposals in shared memory
+constexpr int kConfPerWarp = (kRound - 1 + kChainWarps - 1) / kChainWarps;  // conflict tests per warp
 
 struct RoundSlot {  // one proposal's outcome of step 1
   float delta;
@@ -58,6 +59,7 @@ __device__ __forceinline__ void anneal_chain_cta(const float4* __restrict__ pal,
                                                  uint8_t* smem) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int gw = J.gw, gh = J.gh, n = gw * gh;
+  __shared__ unsigned s_conf[kChainWarps];  // written after the round's first barrier, read after the second
   int4* s_ring = reinterpret_cast<int4*>(smem);
   RoundSlot* s_round = reinterpret_cast<RoundSlot*>(smem + (size_t)kCtaRing * 16);
   float4* s_lab = reinterpret_cast<float4*>(smem + (size_t)kCtaRing * 16 + (size_t)kRound * sizeof(RoundSlot));
@@ -207,20 +209,29 @@ __device__ __forceinline__ void anneal_chain_cta(const float4* __restrict__ pal,
     }
     const unsigned acc_mask = __ballot_sync(0xffffffffu, lane < kRound && acc_q);
     // proposal q reads a cell within distance 1 of an earlier accepted swap?
-    // (branch-free: Manhattan distances of the four position pairs)
+    // (branch-free: Manhattan distances of the four position pairs).  The
+    // earlier proposals h are split over the warps -- warp w tests
+    // h in [w * kConfPerWarp, (w + 1) * kConfPerWarp) for every q -- and the
+    // warps' conflict masks are ORed through shared memory.
     const int qx1 = (int)(rq.pos1 & 0xFFFFu), qy1 = (int)(rq.pos1 >> 16);
     const int qx2 = (int)(rq.pos2 & 0xFFFFu), qy2 = (int)(rq.pos2 >> 16);
     unsigned conf_bits = 0u;
 #pragma unroll
-    for (int h = 0; h < kRound - 1; ++h) {
-      const uint32_t hp1 = __shfl_sync(0xffffffffu, rq.pos1, h), hp2 = __shfl_sync(0xffffffffu, rq.pos2, h);
+    for (int j = 0; j < kConfPerWarp; ++j) {
+      const int h = warp * kConfPerWarp + j;
+      const uint32_t hp1 = __shfl_sync(0xffffffffu, rq.pos1, h & 31), hp2 = __shfl_sync(0xffffffffu, rq.pos2, h & 31);
       const int hx1 = (int)(hp1 & 0xFFFFu), hy1 = (int)(hp1 >> 16), hx2 = (int)(hp2 & 0xFFFFu), hy2 = (int)(hp2 >> 16);
       const unsigned hit = (unsigned)(abs(hx1 - qx1) + abs(hy1 - qy1) <= 1) | (unsigned)(abs(hx1 - qx2) + abs(hy1 - qy2) <= 1) |
                            (unsigned)(abs(hx2 - qx1) + abs(hy2 - qy1) <= 1) | (unsigned)(abs(hx2 - qx2) + abs(hy2 - qy2) <= 1);
-      conf_bits |= hit & (acc_mask >> h) & (unsigned)(h < q);
+      conf_bits |= hit & (acc_mask >> (h & 31)) & (unsigned)(h < q);
     }
-    const bool conf = (conf_bits & 1u) != 0u;
-    const unsigned cmask = __ballot_sync(0xffffffffu, lane < kRound && !skip_q && conf);
+    const unsigned part = __ballot_sync(0xffffffffu, lane < kRound && (conf_bits & 1u) != 0u);
+    if (lane == 0) s_conf[warp] = part;
+    __syncthreads();
+    unsigned conf_mask = 0u;
+#pragma unroll
+    for (int w = 0; w < kChainWarps; ++w) conf_mask |= s_conf[w];
+    const unsigned cmask = conf_mask & live_mask;
     const int gc = cmask ? __ffs(cmask) - 1 : kRound;  // >= 1: proposal 0 never conflicts
     const int ncommit = (int)min((long long)gc, iters - it);
     const unsigned commit = (1u << ncommit) - 1u;  // ncommit <= kRound < 32
