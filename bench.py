@@ -55,6 +55,7 @@ def parse_args():
     ap.add_argument("--served-pool", type=int, default=64, help="distinct targets (served)")
     ap.add_argument("--served-scale", type=float, default=1.0, help="shrinks the cell range (served)")
     ap.add_argument("--served-arena-gb", type=int, default=8, help="pinned output arena (served)")
+    ap.add_argument("--batched-mosaics", type=int, default=256, help="mosaics in the batch (batched; fewer for profiling)")
     return ap.parse_args()
 
 
@@ -365,8 +366,10 @@ def run_ours(args, rank, world, local):
 
 def run_batched(args, rank, world, local):
     """256 uneven mosaics over one resident 10 000-material palette: the batched
-    pipeline (one persistent walk/chain launch, graph replay) against the same
-    mosaics run one single-mosaic batch after another (the plain path)."""
+    pipeline (cell statistics and k-nearest over every cell, every walk in one
+    launch, every chain in one launch, adjustment and composite; graph replay)
+    against the same mosaics run one single-mosaic batch after another (the
+    plain path)."""
     import ctypes as C
 
     import numpy as np
@@ -378,7 +381,8 @@ def run_batched(args, rank, world, local):
     lib = capi.load()
     ctx = capi.Context(local)
     t0 = time.perf_counter()
-    specs, mats, thumbs = job.batched_workload(seed=20251203 + 7919 * rank, allocator=lib.mg_host_alloc)
+    specs, mats, thumbs = job.batched_workload(n=args.batched_mosaics, seed=20251203 + 7919 * rank,
+                                               allocator=lib.mg_host_alloc)
     gen_s = time.perf_counter() - t0
     pal = job.Palette(ctx, mats, thumbs, 32, 32, target_aspect=4 / 3, build_similarity=True)
     reqs = job.batched_requests(specs)

@@ -257,9 +257,10 @@ int mg_plan_launches(mg_plan* plan);
  * No single reference function: the reference builds its palette once per
  * process (MosaicGenerator::new, main.rs:105-164) and then generates one
  * mosaic (main.rs:477-685).  Here the palette stays in device memory and many
- * mosaics of uneven size run through one batched pipeline whose sequential
- * stages (greedy walk, annealing chains) are work items of one persistent
- * launch; results equal mg_generate's for each mosaic bit for bit. */
+ * mosaics of uneven size run through one batched pipeline: the data-parallel
+ * stages over the cells of every mosaic at once, every greedy walk in one
+ * launch and every annealing chain in one launch; results equal mg_generate's
+ * for each mosaic bit for bit. */
 typedef struct mg_palette mg_palette;
 typedef struct mg_batch mg_batch;
 
