@@ -89,6 +89,8 @@ class Context {
   Context& operator=(const Context&) = delete;
   mg_ctx* get() const { return h_; }
   void sync() { detail::check(mg_ctx_sync(h_)); }
+  // How k-nearest queries search (MG_NEAREST_AUTO / _SCAN / _GRID; identical results).
+  void set_nearest_method(int method) { detail::check(mg_ctx_set_nearest_method(h_, method)); }
 
  private:
   mg_ctx* h_ = nullptr;
