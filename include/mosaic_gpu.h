@@ -233,7 +233,8 @@ typedef struct mg_result {
 } mg_result;
 
 void mg_request_default(mg_request* req);
-/* One complete job from host buffers to host buffers. */
+/* One complete job from host buffers to host buffers.  Inputs in pinned host
+ * memory (mg_host_alloc) are read in place over the CPU-GPU link. */
 int mg_generate(mg_ctx* ctx, const mg_request* req, mg_result* res);
 
 /* Device-resident form of the same job: mg_plan_create uploads the inputs

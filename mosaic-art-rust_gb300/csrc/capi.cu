@@ -70,6 +70,9 @@ struct mg_plan {
       cand_dist, grid_greedy, resets, init_cost, greedy_job, chain_grids, chain_res, anneal_job, final_grid,
       finals_ptr, best_chain, adj, out, sums, cell_sums, err, usage, gather_src;
   LabIndex index;  // bucket grid over pal_lab for the k-nearest search (when large)
+  // pinned host staging of the small read-backs (grid, counters, chain results)
+  void* h_read = nullptr;
+  size_t h_read_cap = 0;
   // Where the kernels read the target (a device copy, or pinned host memory in place).
   bool zero_copy = false;
   const uint8_t* target_ptr = nullptr;
@@ -712,6 +715,9 @@ void mg_request_default(mg_request* r) {
 namespace {
 
 void plan_release(mg_plan* pl) {
+  if (pl->h_read) cudaFreeHost(pl->h_read);
+  pl->h_read = nullptr;
+  pl->h_read_cap = 0;
   for (DevBuf* b : {&pl->target, &pl->mats, &pl->regions, &pl->thumb_regions, &pl->thumbs, &pl->pal_lab,
                     &pl->thumb_rgb, &pl->sim, &pl->cell_lab, &pl->cell_rgb, &pl->cand_idx, &pl->cand_dist,
                     &pl->grid_greedy, &pl->resets, &pl->init_cost, &pl->greedy_job, &pl->chain_grids, &pl->chain_res,
@@ -984,19 +990,47 @@ int plan_read(mg_plan* pl, mg_result* res) {
   cudaStream_t s = ctx->stream;
   const int N = pl->N;
   const int32_t* final_grid = pl->run_sa ? pl->final_grid.as<int32_t>() : pl->grid_greedy.as<int32_t>();
-  std::vector<int32_t> grid(N);
   ChainResult cr{};
   int bc = -1, resets = 0;
   if (res->image)
     MG_CUDA(cudaMemcpyAsync(res->image, pl->out.p, 3ull * pl->tw * pl->th * N, cudaMemcpyDeviceToHost, s));
-  MG_CUDA(cudaMemcpyAsync(grid.data(), final_grid, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, s));
-  MG_CUDA(cudaMemcpyAsync(&resets, pl->resets.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-  if (pl->run_sa) MG_CUDA(cudaMemcpyAsync(&bc, pl->best_chain.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-  MG_CHECK(finish(ctx));
-  uint32_t kerr = 0;
-  MG_CUDA(cudaMemcpy(&kerr, pl->err.p, 4, cudaMemcpyDeviceToHost));
-  if (kerr) return fail(MG_ERR_TIMEOUT, "a bounded wait inside a kernel ran out");
-  if (pl->run_sa) MG_CUDA(cudaMemcpy(&cr, pl->chain_res.as<ChainResult>() + bc, sizeof(cr), cudaMemcpyDeviceToHost));
+  // every small read-back into one pinned staging block, then one synchronisation:
+  // [grid N x int32][resets, kernel error, context error, best chain][chain results]
+  const size_t n_chains = pl->run_sa ? (size_t)std::max(pl->K, 1) : 0;
+  const size_t words = ((size_t)N + 4 + 3) & ~(size_t)3;  // keeps the chain results 16-byte aligned
+  const size_t need = words * 4 + sizeof(ChainResult) * n_chains;
+  if (pl->h_read_cap < need) {
+    if (pl->h_read) cudaFreeHost(pl->h_read);
+    pl->h_read = nullptr;
+    pl->h_read_cap = 0;
+    MG_CUDA(cudaHostAlloc(&pl->h_read, need, cudaHostAllocDefault));
+    pl->h_read_cap = need;
+  }
+  int32_t* h_grid = static_cast<int32_t*>(pl->h_read);
+  uint32_t* h_words = reinterpret_cast<uint32_t*>(h_grid + N);
+  ChainResult* h_chains = reinterpret_cast<ChainResult*>(static_cast<uint32_t*>(pl->h_read) + words);
+  h_words[0] = h_words[1] = h_words[2] = 0u;
+  h_words[3] = 0xFFFFFFFFu;
+  MG_CUDA(cudaMemcpyAsync(h_grid, final_grid, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, s));
+  MG_CUDA(cudaMemcpyAsync(&h_words[0], pl->resets.p, 4, cudaMemcpyDeviceToHost, s));
+  MG_CUDA(cudaMemcpyAsync(&h_words[1], pl->err.p, 4, cudaMemcpyDeviceToHost, s));
+  if (ctx->err.p) MG_CUDA(cudaMemcpyAsync(&h_words[2], ctx->err.p, 4, cudaMemcpyDeviceToHost, s));
+  if (pl->run_sa) {
+    MG_CUDA(cudaMemcpyAsync(&h_words[3], pl->best_chain.p, 4, cudaMemcpyDeviceToHost, s));
+    MG_CUDA(cudaMemcpyAsync(h_chains, pl->chain_res.p, sizeof(ChainResult) * n_chains, cudaMemcpyDeviceToHost, s));
+  }
+  MG_CUDA(cudaStreamSynchronize(s));
+  if (h_words[2]) {
+    MG_CUDA(cudaMemset(ctx->err.p, 0, 4));
+    return fail(MG_ERR_TIMEOUT, "a bounded wait inside a kernel ran out");
+  }
+  if (h_words[1]) return fail(MG_ERR_TIMEOUT, "a bounded wait inside a kernel ran out");
+  resets = (int)h_words[0];
+  if (pl->run_sa) {
+    bc = (int)h_words[3];
+    if (bc >= 0 && bc < (int)n_chains) cr = h_chains[bc];
+  }
+  const int32_t* grid = h_grid;
   if (res->grid)
     for (int i = 0; i < N; ++i) res->grid[i] = grid[i] < 0 ? -1 : pl->selected[grid[i]];
   res->out_w = pl->gw * pl->tw;
@@ -1074,9 +1108,10 @@ int mg_generate(mg_ctx* ctx, const mg_request* req, mg_result* res) {
   MG_CHECK(check_ctx(ctx));
   if (!res) return fail(MG_ERR_ARG, "null result");
   if (!ctx->gen_plan) ctx->gen_plan = new mg_plan();
-  MG_CHECK(plan_setup(ctx->gen_plan, ctx, req, true));
-  MG_CHECK(plan_run(ctx->gen_plan));
-  return plan_read(ctx->gen_plan, res);
+  mg_plan* pl = ctx->gen_plan;
+  MG_CHECK(plan_setup(pl, ctx, req, true));
+  MG_CHECK(plan_run(pl));
+  return plan_read(pl, res);
 }
 
 }  // extern "C"

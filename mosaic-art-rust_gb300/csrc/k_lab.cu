@@ -98,16 +98,9 @@ __global__ void __launch_bounds__(kStatThreads) region_stats_kernel(const uint8_
   const float eps = c_lab.eps, k1 = c_lab.k1, k2 = c_lab.k2;
 
   const int y0 = (int)((int64_t)chunk * h / chunks), y1 = (int)((int64_t)(chunk + 1) * h / chunks);
-  const int64_t npx = (int64_t)(y1 - y0) * w;
   long long aL = 0, aA = 0, aB = 0;
   unsigned int sr = 0, sg = 0, sb = 0;
-  // Walk pixels i = tid, tid + T, ... of the chunk with incremental (x, y).
-  int x = threadIdx.x % w, y = y0 + threadIdx.x / w;
-  const int dx = kStatThreads % w, dy = kStatThreads / w;
-  const uint8_t* img = base + off;
-  for (int64_t i = threadIdx.x; i < npx; i += kStatThreads) {
-    const uint8_t* p = img + (int64_t)y * stride + 3 * x;
-    const uint32_t r8 = p[0], g8 = p[1], b8 = p[2];
+  auto pixel = [&](uint32_t r8, uint32_t g8, uint32_t b8) {
     sr += r8;
     sg += g8;
     sb += b8;
@@ -118,11 +111,44 @@ __global__ void __launch_bounds__(kStatThreads) region_stats_kernel(const uint8_
       aA += lab_quant(A);
       aB += lab_quant(B);
     }
-    x += dx;
-    y += dy;
-    if (x >= w) {
-      x -= w;
-      ++y;
+  };
+  const uint8_t* img = base + off;
+  if ((w & 3) == 0 && (stride & 3) == 0 && ((uintptr_t)img & 3) == 0) {
+    // Four pixels of a row as three 32-bit words (fewer, wider loads: the
+    // regions may sit in pinned host memory read over the CPU-GPU link).  The
+    // sums are exact integers, so the order of the pixels does not matter.
+    const int gpr = w >> 2;
+    const int64_t ng = (int64_t)(y1 - y0) * gpr;
+    int gx = threadIdx.x % gpr, y = y0 + threadIdx.x / gpr;
+    const int dgx = kStatThreads % gpr, dgy = kStatThreads / gpr;
+    for (int64_t q = threadIdx.x; q < ng; q += kStatThreads) {
+      const uint32_t* p = reinterpret_cast<const uint32_t*>(img + (int64_t)y * stride + 12 * gx);
+      const uint32_t w0 = p[0], w1 = p[1], w2 = p[2];
+      pixel(w0 & 0xFFu, (w0 >> 8) & 0xFFu, (w0 >> 16) & 0xFFu);
+      pixel(w0 >> 24, w1 & 0xFFu, (w1 >> 8) & 0xFFu);
+      pixel((w1 >> 16) & 0xFFu, w1 >> 24, w2 & 0xFFu);
+      pixel((w2 >> 8) & 0xFFu, (w2 >> 16) & 0xFFu, w2 >> 24);
+      gx += dgx;
+      y += dgy;
+      if (gx >= gpr) {
+        gx -= gpr;
+        ++y;
+      }
+    }
+  } else {
+    // Walk pixels i = tid, tid + T, ... of the chunk with incremental (x, y).
+    const int64_t npx = (int64_t)(y1 - y0) * w;
+    int x = threadIdx.x % w, y = y0 + threadIdx.x / w;
+    const int dx = kStatThreads % w, dy = kStatThreads / w;
+    for (int64_t i = threadIdx.x; i < npx; i += kStatThreads) {
+      const uint8_t* p = img + (int64_t)y * stride + 3 * x;
+      pixel(p[0], p[1], p[2]);
+      x += dx;
+      y += dy;
+      if (x >= w) {
+        x -= w;
+        ++y;
+      }
     }
   }
   unsigned long long ur = sr, ug = sg, ub = sb;

@@ -20,7 +20,7 @@ def rand_lab(rng, n):
 
 # ---- (a) Lab reduce -------------------------------------------------------------------------------
 @pytest.mark.parametrize("w,h,gw,gh", [(1024, 768, 40, 30), (257, 131, 7, 5), (50, 50, 50, 50), (3, 3, 1, 1),
-                                       (640, 480, 13, 11)])
+                                       (640, 480, 13, 11), (1024, 768, 32, 24), (960, 720, 20, 15)])
 def test_cells_lab_bit_exact(ctx, orc, w, h, gw, gh):
     from mosaic_gpu import synth
 
