@@ -8,6 +8,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>  // driver types only: the entry point is fetched through the runtime
+
 #include "capi_internal.h"
 
 namespace mg {
@@ -73,6 +75,11 @@ struct mg_plan {
   // pinned host staging of the small read-backs (grid, counters, chain results)
   void* h_read = nullptr;
   size_t h_read_cap = 0;
+  // pinned host staging of the small uploads of a setup (regions, gather sources,
+  // job structs); reused by the next setup, which follows the previous job's
+  // read-back (a synchronisation), so no setup has to wait for its own copies
+  void* h_up = nullptr;
+  size_t h_up_cap = 0, h_up_used = 0;
   // Where the kernels read the target (a device copy, or pinned host memory in place).
   bool zero_copy = false;
   const uint8_t* target_ptr = nullptr;
@@ -135,6 +142,43 @@ const void* device_view(const void* p) {
   }
   return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
+
+// Device views of caller buffers for one setup: the first query of a pinned
+// allocation also records its extent (the driver's range attributes), so the
+// other buffers inside it -- hundreds of materials packed in one pinned block,
+// say -- need no query.  Kept for one call only: allocations change between calls.
+struct ViewCache {
+  struct Range {
+    uintptr_t lo, hi;
+    intptr_t delta;  // device address - host address
+  };
+  std::vector<Range> ranges;
+  const void* view(const void* p, size_t bytes) {
+    const uintptr_t u = (uintptr_t)p;
+    for (const Range& r : ranges)
+      if (u >= r.lo && u + bytes <= r.hi) return (const void*)(u + r.delta);
+    const void* d = device_view(p);
+    if (!d) return nullptr;
+    using GetAttr = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
+    static GetAttr get = [] {
+      void* fn = nullptr;
+      cudaDriverEntryPointQueryResult q;
+      if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+          q != cudaDriverEntryPointSuccess) {
+        cudaGetLastError();
+        fn = nullptr;
+      }
+      return reinterpret_cast<GetAttr>(fn);
+    }();
+    CUdeviceptr start = 0;
+    size_t size = 0;
+    if (get && get(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, (CUdeviceptr)u) == CUDA_SUCCESS &&
+        get(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, (CUdeviceptr)u) == CUDA_SUCCESS && size > 0 && (uintptr_t)start <= u &&
+        u + bytes <= (uintptr_t)start + size)
+      ranges.push_back(Range{(uintptr_t)start, (uintptr_t)start + size, (intptr_t)(uintptr_t)d - (intptr_t)u});
+    return d;
+  }
+};
 
 const void* device_view_or_device(const void* p) {
   cudaPointerAttributes a;
@@ -715,6 +759,9 @@ void mg_request_default(mg_request* r) {
 namespace {
 
 void plan_release(mg_plan* pl) {
+  if (pl->h_up) cudaFreeHost(pl->h_up);
+  pl->h_up = nullptr;
+  pl->h_up_cap = pl->h_up_used = 0;
   if (pl->h_read) cudaFreeHost(pl->h_read);
   pl->h_read = nullptr;
   pl->h_read_cap = 0;
@@ -796,16 +843,39 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r, bool zero_copy) {
     pl->target_ptr = pl->target.as<uint8_t>();
     pl->target_stride = (int64_t)trow;
   }
+  // the small uploads go through the plan's pinned staging block
+  {
+    const size_t need = 2 * sizeof(Region) * std::max(P, 1) + sizeof(int64_t) * std::max(P, 1) + sizeof(GreedyJob) +
+                        sizeof(AnnealJob) + sizeof(int32_t*) + 16 * 8;
+    if (pl->h_up_cap < need) {
+      if (pl->h_up) cudaFreeHost(pl->h_up);
+      pl->h_up = nullptr;
+      pl->h_up_cap = 0;
+      MG_CUDA(cudaHostAlloc(&pl->h_up, need, cudaHostAllocDefault));
+      pl->h_up_cap = need;
+    }
+    pl->h_up_used = 0;
+  }
+  auto upload_staged = [&](void* dst, const void* src, size_t bytes) -> int {
+    uint8_t* hp = static_cast<uint8_t*>(pl->h_up) + pl->h_up_used;
+    if (pl->h_up_used + bytes > pl->h_up_cap) return fail(MG_ERR_STATE, "upload staging overflow");
+    std::memcpy(hp, src, bytes);
+    pl->h_up_used += (bytes + 15) & ~(size_t)15;
+    MG_CUDA(cudaMemcpyAsync(dst, hp, bytes, cudaMemcpyHostToDevice, s));
+    return MG_OK;
+  };
   // selected materials
   pl->h_regions.resize(std::max(P, 1));
   std::vector<const void*> mdev(std::max(P, 1), nullptr);
+  ViewCache views;
   int64_t off = 0;
   for (int i = 0; i < P; ++i) {
     const int m = pl->selected[i];
     const int64_t st = r->material_stride ? r->material_stride[m] : 3ll * r->material_w[m];
     if (!valid_image(r->materials[m], r->material_w[m], r->material_h[m], st))
       return fail(MG_ERR_ARG, "invalid material " + std::to_string(m));
-    mdev[i] = pl->zero_copy ? device_view(r->materials[m]) : nullptr;
+    mdev[i] = pl->zero_copy ? views.view(r->materials[m], (size_t)st * (r->material_h[m] - 1) + 3ull * r->material_w[m])
+                            : nullptr;
     if (mdev[i]) {
       pl->h_regions[i] = Region{(int64_t)(uintptr_t)mdev[i], r->material_w[m], r->material_h[m], st};
     } else {
@@ -824,7 +894,7 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r, bool zero_copy) {
     pl->h_regions[i].offset += (int64_t)(uintptr_t)pl->mats.p;
   }
   MG_CHECK(pl->regions.ensure(sizeof(Region) * std::max(P, 1)));
-  MG_CUDA(cudaMemcpyAsync(pl->regions.p, pl->h_regions.data(), sizeof(Region) * std::max(P, 1), cudaMemcpyHostToDevice, s));
+  MG_CHECK(upload_staged(pl->regions.p, pl->h_regions.data(), sizeof(Region) * std::max(P, 1)));
   // thumbnails (input, or resized on the device in mg_plan_run)
   const size_t tb = 3ull * pl->tw * pl->th;
   MG_CHECK(pl->thumbs.ensure(tb * std::max(P, 1)));
@@ -836,9 +906,8 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r, bool zero_copy) {
       std::vector<int64_t> src(P);
       for (int i = 0; i < P; ++i) src[i] = (int64_t)(uintptr_t)thdev + (int64_t)(tb * pl->selected[i]);
       MG_CHECK(pl->gather_src.ensure(sizeof(int64_t) * P));
-      MG_CUDA(cudaMemcpyAsync(pl->gather_src.p, src.data(), sizeof(int64_t) * P, cudaMemcpyHostToDevice, s));
+      MG_CHECK(upload_staged(pl->gather_src.p, src.data(), sizeof(int64_t) * P));
       MG_CHECK(launch_gather(pl->gather_src.as<int64_t>(), P, tb, pl->thumbs.as<uint8_t>(), s));
-      MG_CUDA(cudaStreamSynchronize(s));  // `src` goes out of scope
     } else {
       int i = 0;
       while (i < P) {  // merge runs of consecutive selected materials into one copy
@@ -853,7 +922,7 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r, bool zero_copy) {
   std::vector<Region> tregs(std::max(P, 1));
   for (int i = 0; i < P; ++i) tregs[i] = Region{(int64_t)(tb * i), pl->tw, pl->th, 3ll * pl->tw};
   MG_CHECK(pl->thumb_regions.ensure(sizeof(Region) * std::max(P, 1)));
-  MG_CUDA(cudaMemcpyAsync(pl->thumb_regions.p, tregs.data(), sizeof(Region) * std::max(P, 1), cudaMemcpyHostToDevice, s));
+  MG_CHECK(upload_staged(pl->thumb_regions.p, tregs.data(), sizeof(Region) * std::max(P, 1)));
   // working buffers
   const int N = pl->N, K = std::max(pl->K, 1), k = std::max(pl->k, 1);
   MG_CHECK(pl->pal_lab.ensure(sizeof(float4) * std::max(P, 1)));
@@ -881,7 +950,7 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r, bool zero_copy) {
   GreedyJob gj{pl->cand_idx.as<uint32_t>(), pl->cand_dist.as<float>(), pl->grid_greedy.as<int32_t>(), pl->gw, pl->gh,
                pl->k, (uint32_t)pl->max_usage, pl->weight, pl->resets.as<int>(), pl->init_cost.as<float>()};
   MG_CHECK(pl->greedy_job.ensure(sizeof(GreedyJob)));
-  MG_CUDA(cudaMemcpyAsync(pl->greedy_job.p, &gj, sizeof(gj), cudaMemcpyHostToDevice, s));
+  MG_CHECK(upload_staged(pl->greedy_job.p, &gj, sizeof(gj)));
   AnnealJob aj{};
   aj.grid_in = pl->grid_greedy.as<int32_t>();
   aj.chain_grids = pl->chain_grids.as<int32_t>();
@@ -898,15 +967,17 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r, bool zero_copy) {
   aj.stream = pl->stream_id;
   aj.greedy_only = 0;
   MG_CHECK(pl->anneal_job.ensure(sizeof(AnnealJob)));
-  MG_CUDA(cudaMemcpyAsync(pl->anneal_job.p, &aj, sizeof(aj), cudaMemcpyHostToDevice, s));
+  MG_CHECK(upload_staged(pl->anneal_job.p, &aj, sizeof(aj)));
   int32_t* fp = pl->final_grid.as<int32_t>();
   MG_CHECK(pl->finals_ptr.ensure(sizeof(int32_t*)));
-  MG_CUDA(cudaMemcpyAsync(pl->finals_ptr.p, &fp, sizeof(fp), cudaMemcpyHostToDevice, s));
+  MG_CHECK(upload_staged(pl->finals_ptr.p, &fp, sizeof(fp)));
   if (!pl->events) {
     for (auto& e : pl->ev) MG_CUDA(cudaEventCreate(&e));
     pl->events = true;
   }
-  MG_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+  // mg_plan_create returns with the caller's inputs consumed; mg_generate
+  // (zero_copy) reads them during the run and synchronises at its end
+  if (!zero_copy) MG_CUDA(cudaStreamSynchronize(s));
   pl->ran = false;
   return MG_OK;
 }
