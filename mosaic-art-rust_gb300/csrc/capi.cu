@@ -85,6 +85,13 @@ struct mg_plan {
   const uint8_t* target_ptr = nullptr;
   int64_t target_stride = 0;
   cudaEvent_t ev[9] = {};  // stage boundaries [0..7]; [8] joins the side stream
+  // mg_generate with a pinned image buffer: downloaded band by band on the side
+  // stream while the next band is composited (nullptr: one composite, no download)
+  uint8_t* out_host = nullptr;
+  static constexpr int kBands = 4;
+  cudaEvent_t band_ev[kBands] = {};
+  cudaEvent_t download_done = nullptr;
+  uint8_t* downloaded_to = nullptr;  // where the last run's bands went
   bool events = false;
   int launches = 0;
   bool ran = false;
@@ -774,6 +781,11 @@ void plan_release(mg_plan* pl) {
   pl->index.release();
   if (pl->events)
     for (auto& e : pl->ev) cudaEventDestroy(e);
+  if (pl->download_done) {
+    for (auto& e : pl->band_ev) cudaEventDestroy(e);
+    cudaEventDestroy(pl->download_done);
+    pl->download_done = nullptr;
+  }
   pl->events = false;
 }
 
@@ -1047,8 +1059,31 @@ int plan_run(mg_plan* pl) {
   if (adjust)
     MG_CHECK(launch_cell_adjust(final_grid, N, pl->thumb_rgb.as<uchar4>(), pl->cell_rgb.as<uchar4>(), pl->strength,
                                 pl->adj.as<float4>(), s));
-  MG_CHECK(launch_composite(final_grid, pl->gw, pl->gh, pl->thumbs.as<uint8_t>(), pl->tw, pl->th, pl->adj.as<float4>(),
-                            adjust ? 1 : 0, pl->out.as<uint8_t>(), s));
+  pl->downloaded_to = nullptr;
+  if (!pl->out_host || pl->gh < mg_plan::kBands) {
+    MG_CHECK(launch_composite(final_grid, pl->gw, pl->gh, pl->thumbs.as<uint8_t>(), pl->tw, pl->th,
+                              pl->adj.as<float4>(), adjust ? 1 : 0, pl->out.as<uint8_t>(), s));
+  } else {
+    // bands of tile rows: band b composited on the stream, then copied to the
+    // caller's buffer on the side stream while band b + 1 is composited
+    if (!pl->download_done) {
+      for (auto& e : pl->band_ev) MG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      MG_CUDA(cudaEventCreateWithFlags(&pl->download_done, cudaEventDisableTiming));
+    }
+    const size_t row_bytes = 3ull * pl->gw * pl->tw * pl->th;  // one row of tiles in the output
+    for (int b = 0; b < mg_plan::kBands; ++b) {
+      const int r0 = (int)((int64_t)pl->gh * b / mg_plan::kBands), r1 = (int)((int64_t)pl->gh * (b + 1) / mg_plan::kBands);
+      MG_CHECK(launch_composite(final_grid + (size_t)r0 * pl->gw, pl->gw, r1 - r0, pl->thumbs.as<uint8_t>(), pl->tw,
+                                pl->th, pl->adj.as<float4>() + (size_t)r0 * pl->gw, adjust ? 1 : 0,
+                                pl->out.as<uint8_t>() + row_bytes * r0, s));
+      MG_CUDA(cudaEventRecord(pl->band_ev[b], s));
+      MG_CUDA(cudaStreamWaitEvent(ctx->side, pl->band_ev[b], 0));
+      MG_CUDA(cudaMemcpyAsync(pl->out_host + row_bytes * r0, pl->out.as<uint8_t>() + row_bytes * r0,
+                              row_bytes * (r1 - r0), cudaMemcpyDeviceToHost, ctx->side));
+    }
+    MG_CUDA(cudaEventRecord(pl->download_done, ctx->side));
+    pl->downloaded_to = pl->out_host;
+  }
   MG_CUDA(cudaEventRecord(pl->ev[7], s));
   pl->launches = (int)(g_launches - l0);
   pl->ran = true;
@@ -1063,7 +1098,8 @@ int plan_read(mg_plan* pl, mg_result* res) {
   const int32_t* final_grid = pl->run_sa ? pl->final_grid.as<int32_t>() : pl->grid_greedy.as<int32_t>();
   ChainResult cr{};
   int bc = -1, resets = 0;
-  if (res->image)
+  if (pl->downloaded_to) MG_CUDA(cudaStreamWaitEvent(s, pl->download_done, 0));  // the bands' copies, joined back
+  if (res->image && res->image != pl->downloaded_to)
     MG_CUDA(cudaMemcpyAsync(res->image, pl->out.p, 3ull * pl->tw * pl->th * N, cudaMemcpyDeviceToHost, s));
   // every small read-back into one pinned staging block, then one synchronisation:
   // [grid N x int32][resets, kernel error, context error, best chain][chain results]
@@ -1181,8 +1217,13 @@ int mg_generate(mg_ctx* ctx, const mg_request* req, mg_result* res) {
   if (!ctx->gen_plan) ctx->gen_plan = new mg_plan();
   mg_plan* pl = ctx->gen_plan;
   MG_CHECK(plan_setup(pl, ctx, req, true));
-  MG_CHECK(plan_run(pl));
-  return plan_read(pl, res);
+  // a pinned image buffer is filled band by band during the run (a pageable one
+  // would make each band's copy wait on the host)
+  pl->out_host = device_view(res->image) ? static_cast<uint8_t*>(res->image) : nullptr;
+  int st = plan_run(pl);
+  pl->out_host = nullptr;
+  if (st == MG_OK) st = plan_read(pl, res);
+  return st;
 }
 
 }  // extern "C"

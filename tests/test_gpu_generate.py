@@ -119,3 +119,32 @@ def test_full_recommended_workload(ctx, orc):
     inp, res, grid, image, ref = _compare(ctx, orc, job.WORKLOADS["recommended"], threads=16)
     assert grid.shape == (60, 80) and image.shape == (2880, 3840, 3)
     assert res.palette_size > 400 and res.best_chain >= 0
+
+
+@pytest.mark.parametrize("grid_h", [15, 3])
+def test_generate_into_pinned_buffers(ctx, grid_h):
+    """mg_generate from and into pinned host memory -- inputs read in place, the
+    image downloaded band by band while the next band is composited (grids of at
+    least four tile rows) -- gives the same bytes as from and into pageable memory."""
+    import ctypes as C
+
+    from mosaic_gpu import _capi as capi
+    from mosaic_gpu import job
+
+    lib = capi.load()
+    cfg = _small("recommended", target_w=480, target_h=24 * grid_h, n_materials=150, material_side=64, grid_w=20,
+                 grid_h=grid_h, tile_w=16, tile_h=12, iterations=300, chains=4)
+    inp = job.make_inputs(cfg)
+    ref_res, ref_grid, ref_image = job.generate(ctx, job.RequestHolder(inp))
+    pinned = job.make_inputs(cfg, allocator=lib.mg_host_alloc)
+    holder = job.RequestHolder(pinned)
+    n = int(np.prod(holder.out_shape()))
+    buf = np.ctypeslib.as_array(C.cast(lib.mg_host_alloc(n), C.POINTER(C.c_uint8)), shape=(n,))
+    image = buf.reshape(holder.out_shape())
+    for _ in range(2):  # the second call reuses the context's job buffers and staging
+        image[:] = 0
+        res, grid, _ = job.generate(ctx, holder, image)
+        assert np.array_equal(grid, ref_grid)
+        assert np.array_equal(image, ref_image)
+        assert res.best_chain == ref_res.best_chain and np.float32(res.final_cost) == np.float32(ref_res.final_cost)
+    lib.mg_host_free(buf.ctypes.data)
