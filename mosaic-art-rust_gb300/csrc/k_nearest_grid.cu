@@ -12,7 +12,7 @@
 //    (b = (z * g + y) * g + x), so a row of buckets along x is one contiguous
 //    run of entries.
 //  - Query (one warp per query): first the smallest cube of buckets around the
-//    query's bucket that holds at least 3k entries, which fixes a k-th distance
+//    query's bucket that holds at least k entries, which fixes a k-th distance
 //    t; then every bucket of the box [q - R, q + R] (R = sqrt(t) widened by a
 //    relative 1e-3 and an absolute 1e-3) not already scanned.  An entry outside
 //    that box differs from q by more than R on some axis, so its rounded
@@ -33,7 +33,7 @@ namespace {
 
 constexpr int kGridWarps = 16;
 constexpr int kGridThreads = kGridWarps * 32;
-constexpr int kBoxFactor = 3;   // the first cube holds >= kBoxFactor * k entries
+constexpr int kBoxFactor = 1;   // the first cube holds >= kBoxFactor * k entries
 constexpr int kMaxGridDim = 24; // start[] of 24^3 + 1 ints stays in shared memory
 constexpr unsigned kFull = 0xffffffffu;
 
