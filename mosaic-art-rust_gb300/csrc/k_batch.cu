@@ -56,11 +56,7 @@ __global__ void __launch_bounds__(32 * kWarps) batch_cells_kernel(const BatchMos
     const int npx = M.cw * M.ch;
     long long aL = 0, aA = 0, aB = 0;
     unsigned sr = 0, sg = 0, sb = 0;
-    int x = lane % M.cw, y = lane / M.cw;
-    const int dx = 32 % M.cw, dy = 32 / M.cw;
-    for (int i = lane; i < npx; i += 32) {
-      const uint8_t* px = base + (int64_t)y * M.stride + 3 * x;
-      const uint32_t r8 = px[0], g8 = px[1], b8 = px[2];
+    auto pixel = [&](uint32_t r8, uint32_t g8, uint32_t b8) {
       sr += r8;
       sg += g8;
       sb += b8;
@@ -69,11 +65,38 @@ __global__ void __launch_bounds__(32 * kWarps) batch_cells_kernel(const BatchMos
       aL += lab_quant(L);
       aA += lab_quant(A);
       aB += lab_quant(B);
-      x += dx;
-      y += dy;
-      if (x >= M.cw) {
-        x -= M.cw;
-        ++y;
+    };
+    if ((M.cw & 3) == 0 && (M.stride & 3) == 0 && ((uintptr_t)base & 3) == 0) {
+      // four pixels of a cell row as three 32-bit words (exact integer sums: order-free)
+      const int gpr = M.cw >> 2, ng = gpr * M.ch;
+      int gx = lane % gpr, y = lane / gpr;
+      const int dgx = 32 % gpr, dgy = 32 / gpr;
+      for (int q = lane; q < ng; q += 32) {
+        const uint32_t* p = reinterpret_cast<const uint32_t*>(base + (int64_t)y * M.stride + 12 * gx);
+        const uint32_t w0 = p[0], w1 = p[1], w2 = p[2];
+        pixel(w0 & 0xFFu, (w0 >> 8) & 0xFFu, (w0 >> 16) & 0xFFu);
+        pixel(w0 >> 24, w1 & 0xFFu, (w1 >> 8) & 0xFFu);
+        pixel((w1 >> 16) & 0xFFu, w1 >> 24, w2 & 0xFFu);
+        pixel((w2 >> 8) & 0xFFu, (w2 >> 16) & 0xFFu, w2 >> 24);
+        gx += dgx;
+        y += dgy;
+        if (gx >= gpr) {
+          gx -= gpr;
+          ++y;
+        }
+      }
+    } else {
+      int x = lane % M.cw, y = lane / M.cw;
+      const int dx = 32 % M.cw, dy = 32 / M.cw;
+      for (int i = lane; i < npx; i += 32) {
+        const uint8_t* px = base + (int64_t)y * M.stride + 3 * x;
+        pixel(px[0], px[1], px[2]);
+        x += dx;
+        y += dy;
+        if (x >= M.cw) {
+          x -= M.cw;
+          ++y;
+        }
       }
     }
 #pragma unroll
