@@ -34,6 +34,8 @@
 //    reset bumps an epoch that invalidates older snapshots.  After the walk
 //    the scout CTA computes calculate_total_cost: terms in parallel, one
 //    sequential FP32 sum in the reference's order.
+#include <cstddef>
+
 #include "greedy_walk.cuh"
 
 namespace mg {
@@ -78,10 +80,21 @@ enum Ctrl { kProgress = 0, kEpoch = 1, kAbort = 2 };
 // anything beyond it) lies inside the 2*weight window of entry i -- then, if
 // entry i is the first eligible one, the penalty cannot change the decision.
 // Palette indices are 16-bit (palettes of at most 65535).
+// When the palette's Lab is read from global memory the record also carries,
+// for each f entry, its distance, its weight against the cell above (0 in the
+// first row) and its Lab, and `f_next`, the distance of the first entry after
+// the list (+inf when the list holds every entry under the cap): the walker
+// then settles a cell whose penalty window holds several entries from shared
+// memory (window_cell).
 struct __align__(16) CellRecord {
   uint32_t kf[32];
   uint32_t kr[32];
-  uint32_t epoch, pad[3];
+  uint32_t epoch;
+  float f_next;
+  uint32_t pad[2];
+  float wd[32];
+  float wu[32];
+  float4 wl[32];
 };
 // A scout's working copy of one record (in its own CTA).
 struct ScoutStage {
@@ -90,11 +103,13 @@ struct ScoutStage {
 };
 
 // Records live in a ring.  A scout writes cell c's record once the walker has
-// placed the cell above (c - gw), so the walker is done with every record up
-// to c - gw + 2; a ring of more than gw + 2 slots keeps that slot free.
+// placed cell c - lead (lead = min(gw, kScoutLead)), so the walker is past
+// every record up to c - lead and reads at most two ahead of its cell; a ring
+// of more than lead + 3 slots keeps the slot of record c - R free.
 __host__ __device__ inline int ring_size(int gw) {
+  const int lead = gw < kScoutLead ? gw : kScoutLead;
   int r = 32;
-  while (r < gw + 4) r <<= 1;
+  while (r < lead + 4) r <<= 1;
   return r;
 }
 
@@ -347,8 +362,9 @@ __device__ inline WalkerLayout walker_layout(uint8_t* smem, int n, int p, int R)
 // (The layout is recomputed here rather than passed by reference: a struct
 // whose address escapes would turn the walker's shared-memory pointers into
 // generic ones.)
-__device__ bool scout_cells(int s, const GreedyJob& J, int p, uint8_t* smem, ScoutStage& S, int R,
-                            uint32_t* err) {
+template <bool kWindow>
+__device__ bool scout_cells(int s, const GreedyJob& J, const float4* __restrict__ pal, int p, uint8_t* smem,
+                            ScoutStage& S, int R, uint32_t* err) {
   const int lane = threadIdx.x & 31;
   const int gw = J.gw, k = J.k, n = gw * J.gh;
   const WalkerLayout L = walker_layout(smem, n, p, R);
@@ -456,6 +472,23 @@ __device__ bool scout_cells(int s, const GreedyJob& J, int p, uint8_t* smem, Sco
       st_cluster_v4(rr + 16u * (uint32_t)lane, v);
     }
     if (lane == 0) st_cluster_u32(rr + 256u, ep0 == ep1 ? ep0 : kInvalidEpoch);
+    if (kWindow) {
+      // distance, weight against the cell above and Lab of each f entry (wgt
+      // as full_cell computes it), and the distance after the list
+      float d = inf, wu = 0.0f;
+      float4 la = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (lane < cf) {
+        d = S.df[lane];
+        la = __ldg(pal + (kf_final & 0xFFFFu));
+        if (use_pen && up >= 0) wu = wgt(la, __ldg(pal + up));
+      }
+      const uint32_t wrec = rr + (uint32_t)offsetof(CellRecord, wd);
+      st_cluster_u32(wrec + 4u * (uint32_t)lane, __float_as_uint(d));
+      st_cluster_u32(rr + (uint32_t)offsetof(CellRecord, wu) + 4u * (uint32_t)lane, __float_as_uint(wu));
+      st_cluster_v4(rr + (uint32_t)offsetof(CellRecord, wl) + 16u * (uint32_t)lane,
+                    make_uint4(__float_as_uint(la.x), __float_as_uint(la.y), __float_as_uint(la.z), 0u));
+      if (lane == 0) st_cluster_u32(rr + (uint32_t)offsetof(CellRecord, f_next), __float_as_uint(cf < 32 ? inf : af));
+    }
     fence_cluster();
     __syncwarp();
     if (lane == 0) st_release_cluster(r_seq + 4u * slot, (uint32_t)(c + 1));
@@ -488,7 +521,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
     // ---- the scouts, then (CTA 1) the final cost of the walk
     ScoutStage* stage = reinterpret_cast<ScoutStage*>(smem);
     float* terms = reinterpret_cast<float*>(smem + (size_t)kWarps * sizeof(ScoutStage));
-    bool ok = scout_cells((int)(rank - 1) * kWarps + warp, J, p, smem, stage[warp], R, err);
+    bool ok = scout_cells<!kLabSmem>((int)(rank - 1) * kWarps + warp, J, pal, p, smem, stage[warp], R, err);
     if (rank > 1) {
       cluster_sync_all();
       return;
@@ -622,6 +655,42 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
     r.ui = (r.key != 0xFFFFFFFFu && r.ti < (uint32_t)p) ? usage[r.ti] : 0xFFFFFFFFu;
     return r;
   };
+  // A cell (not a row start) whose first eligible f entry has later entries
+  // inside its penalty window, settled from the record when the palette's Lab
+  // is in global memory: the window's entries are the list's entries under the
+  // cap now, other than the left neighbour's material, with distance below
+  // d(first) + 2*weight (f_next >= that bound closes the window inside the
+  // list); each scores d + (w_up + w_left) * weight in full_cell's arithmetic
+  // and the lowest score, then the lowest position, wins -- full_cell's
+  // decision.  Commits it and returns the material; -1 when the window may
+  // reach past the list (then full_cell decides).
+  auto window_cell = [&](int cc, const Cur& cu, int left, bool has_up) -> int {
+    const CellRecord& Rc = rec[cc & (R - 1)];
+    const bool elig = cu.key != 0xFFFFFFFFu && cu.ui < max_usage && (int)cu.ti != left;
+    const unsigned em = __ballot_sync(0xffffffffu, elig);
+    if (!em) return -1;
+    const int e0 = __ffs(em) - 1;
+    const float dl = Rc.wd[lane];
+    const float b0 = __fadd_rn(__shfl_sync(0xffffffffu, dl, e0), __fmul_rn(2.0f, weight));
+    if (!(Rc.f_next >= b0)) return -1;
+    const bool in = elig && lane >= e0 && dl < b0;
+    // the left neighbour's Lab: its entry in the previous cell's list, else global memory
+    const CellRecord& Rp = rec[(cc - 1) & (R - 1)];
+    const uint32_t pk = Rp.kf[lane];
+    const unsigned pm = __ballot_sync(0xffffffffu, pk != 0xFFFFFFFFu && (pk & 0xFFFFu) == (uint32_t)left);
+    const float4 lab_left = pm ? Rp.wl[__ffs(pm) - 1] : __ldg(pal + left);
+    float pen = has_up ? Rc.wu[lane] : 0.0f;  // 0 + w_up, exactly
+    pen = __fadd_rn(pen, wgt(Rc.wl[lane], lab_left));
+    const uint32_t sb = in ? __float_as_uint(__fadd_rn(dl, __fmul_rn(pen, weight))) : 0xFFFFFFFFu;
+    const uint32_t mn = __reduce_min_sync(0xffffffffu, sb);
+    const int win = mn == 0xFFFFFFFFu ? e0 : __ffs(__ballot_sync(0xffffffffu, sb == mn)) - 1;
+    const int tw = (int)__shfl_sync(0xffffffffu, cu.ti, win);
+    if (lane == win) {
+      usage[cu.ti] = cu.ui + 1u;
+      cells[cc] = (uint16_t)tw;
+    }
+    return tw;
+  };
   Cur cur{0xFFFFFFFFu, 0u, 0xFFFFFFFFu};
   bool cur_fresh = true;  // cur's counters include the previous commit
   Head h1{0u, 0xFFFFFFFFu, 0xFFFFFFFFu};
@@ -694,6 +763,14 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
             usage[cur.ti] = ui + 1u;
             cells[c] = (uint16_t)t;
           }
+          done = true;
+        }
+      }
+      if (!kLabSmem && !done && !row_start && chosen != 0xFFFFFFFFu && (chosen & 0x10000u) &&
+          rec[c & (R - 1)].epoch == epoch) {
+        const int tw = window_cell(c, cur, last, y > 0);
+        if (tw >= 0) {
+          t = tw;
           done = true;
         }
       }
