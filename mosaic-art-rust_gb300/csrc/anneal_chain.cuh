@@ -1,5 +1,5 @@
-// anneal_chain.cuh -- one simulated-annealing chain by one warp, shared by the
-// standalone kernel (k_anneal.cu) and the persistent batch kernel (k_batch.cu).
+// anneal_chain.cuh -- one simulated-annealing chain by one warp (anneal_kernel
+// in k_anneal.cu, the fallback of the CTA form of anneal_cta.cuh).
 //
 // k_anneal.cu -- (e) simulated annealing, K independent chains per mosaic,
 // plus the batched adjacency evaluators of the C ABI.

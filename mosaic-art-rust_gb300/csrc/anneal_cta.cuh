@@ -1,6 +1,7 @@
 // anneal_cta.cuh -- one simulated-annealing chain by one CTA of kChainWarps
-// warps (the standalone annealing kernel; the batch kernel keeps the one-warp
-// chain of anneal_chain.cuh, whose rules this follows exactly).
+// warps (anneal_cta_kernel, for single mosaics and for every chain of a batch;
+// the one-warp chain of anneal_chain.cuh, whose rules this follows exactly, is
+// the fallback when the CTA form does not fit in shared memory).
 //
 // Reference: optimizer.rs:41-129 MosaicOptimizer::optimize, optimizer.rs:132-198
 // optimize_greedy, adjacency.rs:133-214 calculate_swap_delta.

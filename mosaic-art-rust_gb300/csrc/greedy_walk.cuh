@@ -1,6 +1,6 @@
-// greedy_walk.cuh -- the greedy placement walk of one mosaic by one warp,
-// shared by the standalone kernel (k_greedy.cu) and the persistent batch
-// kernel (k_batch.cu).
+// greedy_walk.cuh -- the greedy placement walk of one mosaic by one warp
+// (greedy_kernel in k_greedy.cu: palettes above 65535, grids narrower than 8
+// cells, walks whose scouted form does not fit in shared memory).
 //
 // k_greedy.cu -- (d) greedy usage-limited, adjacency-penalised placement.
 //

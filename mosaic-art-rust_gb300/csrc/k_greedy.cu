@@ -29,9 +29,11 @@
 //    with its `clear` bit set it is the reference's choice, bit for bit.  In
 //    every other case (window not clear, no entry passes, a reset since the
 //    snapshot for the filtered list) the walker evaluates the cell in full,
-//    exactly as greedy_walk does.  A scout reads the cell above only after the
-//    walker has committed it (acquire/release on a progress counter) and a
-//    reset bumps an epoch that invalidates older snapshots.  After the walk
+//    exactly as greedy_walk does -- except that with the palette Lab in global
+//    memory a window that closes inside the filtered list is settled from the
+//    record (window_cell).  A scout builds a record once the walker has placed
+//    the cell kScoutLead cells (or a row) back, polling the walker's 16-bit
+//    grid, and a reset bumps an epoch that invalidates older snapshots.  After the walk
 //    the scout CTA computes calculate_total_cost: terms in parallel, one
 //    sequential FP32 sum in the reference's order.
 #include <cstddef>
