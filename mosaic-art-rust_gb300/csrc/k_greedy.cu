@@ -8,8 +8,8 @@
 //
 // Two kernels:
 //  - greedy_kernel: one warp walks one mosaic (greedy_walk.cuh).  Used for
-//    palettes whose counters do not fit in shared memory, palettes above 65535
-//    materials and grids narrower than 8 cells.
+//    palettes above 65535 materials, grids narrower than 8 cells and walks
+//    whose three-CTA form does not fit in shared memory.
 //  - greedy_pair_kernel: a cluster of three CTAs per mosaic.  The walk is a
 //    chain of dependent decisions, so its speed is the latency of one decision.
 //    One warp of CTA 0 (the walker) makes the decisions; 64 scout warps in
