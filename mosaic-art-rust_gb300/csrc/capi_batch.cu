@@ -45,7 +45,7 @@ struct mg_batch {
   std::vector<size_t> out_off;
   DevBuf targets, mos, cell_lab, cell_rgb, cand_idx, cand_dist, grids, finals, chain_grids, results, resets,
       init_cost, best, adj, out, err, gjobs, usage, ajobs, chain_job, chain_id, finals_ptr;
-  // walk jobs (gjobs): the n_wide mosaics with rows of >= 8 cells first, then the rest
+  // walk jobs (gjobs): the n_wide mosaics that walk in the three-CTA form first, then the rest
   int n_wide = 0, wide_gw = 0, wide_cells = 0, narrow_gw = 0, narrow_cells = 0;
   // tuned launch shapes
   int cells_warps = 8, nn_chunk = 2048;
@@ -275,14 +275,15 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
   std::vector<int> order(n);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return b->cells[a] > b->cells[c]; });
-  // walk jobs, wide rows first
+  // walk jobs: those that walk in the three-CTA form first (one launch), the
+  // rest (narrow grids, grids too large for its shared memory) one warp each
   std::vector<GreedyJob> jobs;
   jobs.reserve(std::max(n, 1));
   b->n_wide = b->wide_gw = b->wide_cells = b->narrow_gw = b->narrow_cells = 0;
   for (int pass = 0; pass < 2; ++pass) {
     for (int i : order) {
       const BatchMosaic& M = b->h_mos[i];
-      if ((M.gw >= 8) != (pass == 0)) continue;
+      if (greedy_scouted_fits(M.gw, M.n, pal->P) != (pass == 0)) continue;
       jobs.push_back(GreedyJob{b->cand_idx.as<uint32_t>() + (size_t)M.cell_base * k,
                                b->cand_dist.as<float>() + (size_t)M.cell_base * k, M.grid, M.gw, M.gh, k, M.max_usage,
                                M.weight, M.n_resets, M.init_cost});
@@ -377,7 +378,7 @@ int batch_enqueue(mg_batch* b, bool with_events) {
     if (b->n - b->n_wide > 0)
       MG_CHECK(launch_greedy(pal->pal_lab.as<float4>(), P, b->gjobs.as<GreedyJob>() + b->n_wide, b->n - b->n_wide, k,
                              b->narrow_gw, b->narrow_cells, usage ? usage + (size_t)b->n_wide * P : nullptr,
-                             b->err.as<uint32_t>(), s));
+                             b->err.as<uint32_t>(), s, true));
     // every annealing chain of every mosaic (k_anneal.cu), then per mosaic the
     // best chain -- or the greedy grid when it is not optimised -- as its final grid
     MG_CHECK(launch_anneal(pal->pal_lab.as<float4>(), P, b->ajobs.as<AnnealJob>(), b->chain_job.as<int>(),

@@ -835,8 +835,14 @@ size_t greedy_shared_bytes(int k, int gw, int p, bool lab_smem, bool usage_smem)
   return greedy_smem_bytes(k, gw, p, lab_smem, usage_smem);
 }
 
+bool greedy_scouted_fits(int gw, int n, int p) {
+  constexpr size_t kMaxSmem = 220 * 1024;
+  // the largest ring any row width uses, the palette Lab outside shared memory
+  return gw >= 8 && p <= 65535 && pair_smem_bytes(kScoutLead, n, p, false) <= kMaxSmem;
+}
+
 int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_jobs, int k, int max_gw,
-                  int max_cells, uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream) {
+                  int max_cells, uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream, bool one_warp) {
   if (n_jobs <= 0) return MG_OK;
   if (k < 1 || k > 100) return fail(MG_ERR_ARG, "candidate count must be in 1..100");
   constexpr size_t kMaxSmem = 220 * 1024;
@@ -853,7 +859,7 @@ int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_job
   }
   // The scouted walk: counters in shared memory, 16-bit palette indices, rows
   // of at least 8 cells.
-  if (max_gw >= 8 && p <= 65535) {
+  if (!one_warp && max_gw >= 8 && p <= 65535) {
     bool lab_smem = pair_smem_bytes(max_gw, max_cells, p, true) <= kMaxSmem;
     const size_t bytes = pair_smem_bytes(max_gw, max_cells, p, lab_smem);
     if (bytes <= kMaxSmem) {

@@ -119,9 +119,14 @@ struct GreedyJob {
   float* total_cost;         // 1 float: calculate_total_cost of the placed grid
 };
 // Candidate arrays must hold ceil(N/16)*16 rows (the walk streams 16 rows per copy).
+// one_warp: every job walks in the one-warp form (else the three-CTA form when
+// every job allows it).
 int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_jobs, int k, int max_gw,
-                  int max_cells, uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream);
+                  int max_cells, uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream, bool one_warp = false);
 inline size_t padded_cells(int n) { return ((size_t)n + 15) / 16 * 16; }
+// Whether a mosaic of gw x (n / gw) cells over a palette of p walks in the
+// three-CTA form (else one warp).
+bool greedy_scouted_fits(int gw, int n, int p);
 
 // (e) annealing chains.
 struct ChainResult {
