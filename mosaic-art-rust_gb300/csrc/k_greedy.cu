@@ -32,8 +32,10 @@
 //    exactly as greedy_walk does -- except that with the palette Lab in global
 //    memory a window that closes inside the filtered list is settled from the
 //    record (window_cell).  A scout builds a record once the walker has placed
-//    the cell kScoutLead cells (or a row) back, polling the walker's 16-bit
-//    grid, and a reset bumps an epoch that invalidates older snapshots.  After the walk
+//    the cell kScoutLead cells (or a row) back, polling the walker's ring of
+//    placed cells, and a reset bumps an epoch that invalidates older snapshots.
+//    The walker's shared memory holds rings (records, placed cells), not the
+//    grid, so a mosaic of any cell count walks in this form.  After the walk
 //    the scout CTA computes calculate_total_cost: terms in parallel, one
 //    sequential FP32 sum in the reference's order.
 #include <cstddef>
@@ -115,14 +117,35 @@ __host__ __device__ inline int ring_size(int gw) {
   return r;
 }
 
-// Shared memory of the walker CTA: control words, record ring, sequence
-// words, the placed grid (16-bit, kUnplaced until placed), usage counters,
-// optionally the palette Lab.
+// The placed cells live in the walker CTA's shared memory in one of two forms:
+//  - the grid, 16-bit, kUnplaced until placed (copied to global memory after
+//    the walk);
+//  - when the grid does not fit: a ring of words (cell index & 0xFFFF) << 16 |
+//    material, one 32-bit store publishing a placement and naming its cell.
+//    The walker reads the cell above its own; a scout reads its lead cell and
+//    the cell above its cell.  The walker never passes a cell whose record is
+//    missing, so no cell read is more than gw + kScoutLead + 64 behind the
+//    newest placement, and a ring of more slots than that keeps every cell
+//    until it is read.  The global grid receives each placement as it is made.
 constexpr uint16_t kUnplaced = 0xFFFFu;
-__host__ __device__ inline size_t walker_smem_bytes(int gw, int n, int p, bool lab_smem) {
+constexpr uint32_t kNoCell = 0xFFFFFFFFu;  // a ring slot no placement has written yet
+__host__ __device__ inline int cell_ring_size(int gw) {
+  int r = 64;
+  while (r < gw + kScoutLead + 72) r <<= 1;
+  return r;
+}
+__device__ __forceinline__ uint32_t cell_word(int c, int t) { return ((uint32_t)c << 16) | ((uint32_t)t & 0xFFFFu); }
+
+// Shared memory of the walker CTA: control words, record ring, sequence
+// words, the placed cells (grid or ring), usage counters, optionally the
+// palette Lab.
+__host__ __device__ inline size_t cells_bytes(int gw, int n, bool ring) {
+  return ring ? (size_t)cell_ring_size(gw) * 4 : align16((size_t)n * 2);
+}
+__host__ __device__ inline size_t walker_smem_bytes(int gw, int n, int p, bool lab_smem, bool ring) {
   const int R = ring_size(gw);
   size_t b = 16 + (size_t)R * sizeof(CellRecord) + (size_t)R * 4;
-  b += align16((size_t)n * 2);
+  b += cells_bytes(gw, n, ring);
   b += align16((size_t)p * 4);
   if (lab_smem) b += (size_t)p * 16;
   return b;
@@ -131,8 +154,8 @@ __host__ __device__ inline size_t walker_smem_bytes(int gw, int n, int p, bool l
 __host__ __device__ inline size_t scout_cta_smem_bytes() {
   return (size_t)kWarps * sizeof(ScoutStage) + (size_t)kCostChunk * 8;
 }
-__host__ __device__ inline size_t pair_smem_bytes(int gw, int n, int p, bool lab_smem) {
-  const size_t a = walker_smem_bytes(gw, n, p, lab_smem), b = scout_cta_smem_bytes();
+__host__ __device__ inline size_t pair_smem_bytes(int gw, int n, int p, bool lab_smem, bool ring) {
+  const size_t a = walker_smem_bytes(gw, n, p, lab_smem, ring), b = scout_cta_smem_bytes();
   return a > b ? a : b;
 }
 
@@ -344,17 +367,19 @@ struct WalkerLayout {
   uint32_t* ctrl;
   CellRecord* rec;
   uint32_t* seq;
-  uint16_t* cells;
+  uint32_t* ring;    // the placed cells as a ring (kRing) ...
+  uint16_t* grid16;  // ... or as the 16-bit grid; the same address
   uint32_t* usage;
   float4* lab;
 };
-__device__ inline WalkerLayout walker_layout(uint8_t* smem, int n, int p, int R) {
+__device__ inline WalkerLayout walker_layout(uint8_t* smem, int gw, int n, int p, int R, bool ring) {
   WalkerLayout L;
   L.ctrl = reinterpret_cast<uint32_t*>(smem);
   L.rec = reinterpret_cast<CellRecord*>(smem + 16);
   L.seq = reinterpret_cast<uint32_t*>(L.rec + R);
-  L.cells = reinterpret_cast<uint16_t*>(L.seq + R);
-  L.usage = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(L.cells) + align16((size_t)n * 2));
+  L.ring = L.seq + R;
+  L.grid16 = reinterpret_cast<uint16_t*>(L.ring);
+  L.usage = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(L.ring) + cells_bytes(gw, n, ring));
   L.lab = reinterpret_cast<float4*>(reinterpret_cast<uint8_t*>(L.usage) + align16((size_t)p * 4));
   return L;
 }
@@ -364,12 +389,12 @@ __device__ inline WalkerLayout walker_layout(uint8_t* smem, int n, int p, int R)
 // (The layout is recomputed here rather than passed by reference: a struct
 // whose address escapes would turn the walker's shared-memory pointers into
 // generic ones.)
-template <bool kWindow>
+template <bool kWindow, bool kRing>
 __device__ bool scout_cells(int s, const GreedyJob& J, const float4* __restrict__ pal, int p, uint8_t* smem,
                             ScoutStage& S, int R, uint32_t* err) {
   const int lane = threadIdx.x & 31;
   const int gw = J.gw, k = J.k, n = gw * J.gh;
-  const WalkerLayout L = walker_layout(smem, n, p, R);
+  const WalkerLayout L = walker_layout(smem, gw, n, p, R, kRing);
   const uint32_t max_usage = J.max_usage;
   const bool use_pen = J.weight > 0.0f;
   const float two_w = __fmul_rn(2.0f, J.weight);
@@ -378,7 +403,8 @@ __device__ bool scout_cells(int s, const GreedyJob& J, const float4* __restrict_
   const unsigned lt = (1u << lane) - 1u;
   // the walker CTA's words, in the cluster window
   const uint32_t r_epoch = cluster_map(&L.ctrl[kEpoch], 0), r_abort = cluster_map(&L.ctrl[kAbort], 0);
-  const uint32_t r_usage = cluster_map(L.usage, 0), r_cells = cluster_map(L.cells, 0);
+  const uint32_t r_usage = cluster_map(L.usage, 0), r_cells = cluster_map(L.ring, 0);
+  const int cmask = cell_ring_size(gw) - 1;
   const uint32_t r_rec = cluster_map(L.rec, 0), r_seq = cluster_map(L.seq, 0);
   for (int c = s; c < n; c += kScouts) {
     const int y = c / gw;
@@ -406,11 +432,20 @@ __device__ bool scout_cells(int s, const GreedyJob& J, const float4* __restrict_
     // depends on it), so the walker is done with the ring slot this record
     // reuses (the ring holds more than gw records).
     const int lead = c - min(gw, kScoutLead);
-    uint32_t v_lead = kUnplaced;
+    uint32_t v_lead = kNoCell;  // the lead cell's material in the low 16 bits
     if (lead >= 0) {
-      const uint32_t a_lead = r_cells + 2u * (uint32_t)lead;
+      const uint32_t a_lead = kRing ? r_cells + 4u * (uint32_t)(lead & cmask) : r_cells + 2u * (uint32_t)lead;
+      const uint32_t tag = (uint32_t)lead & 0xFFFFu;
       uint32_t polls = 0;
-      while ((v_lead = ld_cluster_u16(a_lead)) == kUnplaced) {
+      auto placed = [&]() {
+        if (kRing) {
+          v_lead = ld_cluster_u32(a_lead);
+          return (v_lead >> 16) == tag;
+        }
+        v_lead = ld_cluster_u16(a_lead);
+        return v_lead != kUnplaced;
+      };
+      while (!placed()) {
         if (ld_cluster_u32(r_abort)) return false;
         if (++polls > kScoutPolls) {
           if (lane == 0) {
@@ -422,7 +457,10 @@ __device__ bool scout_cells(int s, const GreedyJob& J, const float4* __restrict_
         __nanosleep(1000);  // the scouts run far ahead: poll the walker's SM rarely
       }
     }
-    const int up = y == 0 ? -1 : lead == c - gw ? (int)v_lead : (int)ld_cluster_u16(r_cells + 2u * (uint32_t)(c - gw));
+    const int up = y == 0           ? -1
+                   : lead == c - gw ? (int)(v_lead & 0xFFFFu)
+                   : kRing          ? (int)(ld_cluster_u32(r_cells + 4u * (uint32_t)((c - gw) & cmask)) & 0xFFFFu)
+                                    : (int)ld_cluster_u16(r_cells + 2u * (uint32_t)(c - gw));
     const uint32_t ep0 = ld_acquire_cluster(r_epoch);
     int bf = 0, br = 0;
     float af = inf, ar = inf;  // distance of the 33rd entry
@@ -498,7 +536,7 @@ __device__ bool scout_cells(int s, const GreedyJob& J, const float4* __restrict_
   return true;
 }
 
-template <bool kLabSmem>
+template <bool kLabSmem, bool kRing>
 __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps * 32)
     greedy_pair_kernel(const float4* __restrict__ pal, int p, const GreedyJob* __restrict__ jobs, uint32_t* err) {
   extern __shared__ __align__(128) uint8_t smem[];
@@ -507,14 +545,17 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gw = J.gw, gh = J.gh, k = J.k, n = gw * gh;
   const int R = ring_size(gw);
-  const WalkerLayout L = walker_layout(smem, n, p, R);
+  const WalkerLayout L = walker_layout(smem, gw, n, p, R, kRing);
   if (rank == 0) {
     for (int i = threadIdx.x; i < p; i += blockDim.x) {
       L.usage[i] = 0;
       if (kLabSmem) L.lab[i] = pal[i];
     }
     for (int i = threadIdx.x; i < R; i += blockDim.x) L.seq[i] = 0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) L.cells[i] = kUnplaced;
+    if (kRing)
+      for (int i = threadIdx.x; i < cell_ring_size(gw); i += blockDim.x) L.ring[i] = kNoCell;
+    else
+      for (int i = threadIdx.x; i < n; i += blockDim.x) L.grid16[i] = kUnplaced;
     if (threadIdx.x < 4) L.ctrl[threadIdx.x] = 0;
   }
   cluster_sync_all();  // the walker CTA's state exists before any scout reads it
@@ -523,7 +564,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
     // ---- the scouts, then (CTA 1) the final cost of the walk
     ScoutStage* stage = reinterpret_cast<ScoutStage*>(smem);
     float* terms = reinterpret_cast<float*>(smem + (size_t)kWarps * sizeof(ScoutStage));
-    bool ok = scout_cells<!kLabSmem>((int)(rank - 1) * kWarps + warp, J, pal, p, smem, stage[warp], R, err);
+    bool ok = scout_cells<!kLabSmem, kRing>((int)(rank - 1) * kWarps + warp, J, pal, p, smem, stage[warp], R, err);
     if (rank > 1) {
       cluster_sync_all();
       return;
@@ -589,7 +630,18 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
   uint32_t* ctrl = L.ctrl;
   CellRecord* rec = L.rec;
   uint32_t* seq = L.seq;
-  uint16_t* cells = L.cells;
+  uint32_t* ring = L.ring;
+  uint16_t* grid16 = L.grid16;
+  const int cmask = cell_ring_size(gw) - 1;
+  // a placement: the 16-bit grid, or the ring word and the global grid
+  auto place = [&](int cc, int tt) {
+    if (kRing) {
+      ring[cc & cmask] = cell_word(cc, tt);
+      J.grid[cc] = tt;
+    } else {
+      grid16[cc] = (uint16_t)tt;
+    }
+  };
   uint32_t* usage = L.usage;
   const float4* s_lab = L.lab;
   const uint32_t max_usage = J.max_usage;
@@ -689,7 +741,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
     const int tw = (int)__shfl_sync(0xffffffffu, cu.ti, win);
     if (lane == win) {
       usage[cu.ti] = cu.ui + 1u;
-      cells[cc] = (uint16_t)tw;
+      place(cc, tw);
     }
     return tw;
   };
@@ -730,7 +782,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
       const int t = (int)(chosen & 0xFFFFu);
       if (lane == (int)(chosen >> 17)) {
         usage[cur.ti] = cur.ui + 1u;
-        cells[c] = (uint16_t)t;
+        place(c, t);
       }
       __syncwarp();
       last = t;
@@ -750,7 +802,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
       // only the next record was late
       if (lane == (int)(chosen >> 17)) {
         usage[cur.ti] = cur.ui + 1u;
-        cells[c] = (uint16_t)t;
+        place(c, t);
       }
     } else {
       const bool row_start = x == 0;
@@ -763,7 +815,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
           t = (int)(b & 0xFFFFu);
           if (lane == (int)(b >> 17)) {
             usage[cur.ti] = ui + 1u;
-            cells[c] = (uint16_t)t;
+            place(c, t);
           }
           done = true;
         }
@@ -777,14 +829,14 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
         }
       }
       if (!done) {
-        const int up = y > 0 ? (int)cells[c - gw] : -1;
+        const int up = y == 0 ? -1 : kRing ? (int)(ring[(c - gw) & cmask] & 0xFFFFu) : (int)grid16[c - gw];
         if (kLabSmem)
           t = full_cell(lab, J.cand_idx + (size_t)c * k, J.cand_dist + (size_t)c * k, k, p, up,
                         row_start ? -1 : last, usage, max_usage, weight, ctrl, epoch, resets, lane);
         else
           t = full_cell_rows(lab, J.cand_idx + (size_t)c * k, J.cand_dist + (size_t)c * k, k, p, up,
                              row_start ? -1 : last, usage, max_usage, weight, ctrl, epoch, resets, lane);
-        if (lane == 0) cells[c] = (uint16_t)t;
+        if (lane == 0) place(c, t);
       }
     }
     __syncwarp();
@@ -820,8 +872,12 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
       *reinterpret_cast<volatile uint32_t*>(&ctrl[kAbort]) = 1u;
     }
   } else {
-    // the placed grid to global memory, then the completion the scout CTA waits for
-    for (int i = lane; i < n; i += 32) J.grid[i] = (int32_t)cells[i];
+    // the placed grid in global memory (every lane's stores visible) before the
+    // completion the scout CTA waits for
+    if (kRing)
+      __threadfence();
+    else
+      for (int i = lane; i < n; i += 32) J.grid[i] = (int32_t)grid16[i];
     if (lane == 0 && J.n_resets) *J.n_resets = resets;
     __syncwarp();
     if (lane == 0) st_release_cluster(smem_u32(&ctrl[kProgress]), (uint32_t)n);
@@ -838,7 +894,8 @@ size_t greedy_shared_bytes(int k, int gw, int p, bool lab_smem, bool usage_smem)
 bool greedy_scouted_fits(int gw, int n, int p) {
   constexpr size_t kMaxSmem = 220 * 1024;
   // the largest ring any row width uses, the palette Lab outside shared memory
-  return gw >= 8 && p <= 65535 && pair_smem_bytes(kScoutLead, n, p, false) <= kMaxSmem;
+  return gw >= 8 && p <= 65535 &&
+         (pair_smem_bytes(gw, n, p, false, false) <= kMaxSmem || pair_smem_bytes(gw, n, p, false, true) <= kMaxSmem);
 }
 
 int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_jobs, int k, int max_gw,
@@ -853,20 +910,29 @@ int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_job
     MG_CUDA(cudaFuncSetAttribute(greedy_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
     MG_CUDA(cudaFuncSetAttribute(greedy_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
     MG_CUDA(cudaFuncSetAttribute(greedy_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
-    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
-    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
     configured_device = dev;
   }
   // The scouted walk: counters in shared memory, 16-bit palette indices, rows
   // of at least 8 cells.
   if (!one_warp && max_gw >= 8 && p <= 65535) {
-    bool lab_smem = pair_smem_bytes(max_gw, max_cells, p, true) <= kMaxSmem;
-    const size_t bytes = pair_smem_bytes(max_gw, max_cells, p, lab_smem);
-    if (bytes <= kMaxSmem) {
-      if (lab_smem)
-        greedy_pair_kernel<true><<<(1 + kScoutCtas) * n_jobs, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
-      else
-        greedy_pair_kernel<false><<<(1 + kScoutCtas) * n_jobs, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
+    // the grid before the ring (a shorter walker loop), the palette Lab in shared memory before global
+    const bool fit[4] = {pair_smem_bytes(max_gw, max_cells, p, true, false) <= kMaxSmem,
+                         pair_smem_bytes(max_gw, max_cells, p, false, false) <= kMaxSmem,
+                         pair_smem_bytes(max_gw, max_cells, p, true, true) <= kMaxSmem,
+                         pair_smem_bytes(max_gw, max_cells, p, false, true) <= kMaxSmem};
+    const int form = fit[0] ? 0 : fit[1] ? 1 : fit[2] ? 2 : fit[3] ? 3 : -1;
+    if (form >= 0) {
+      const bool lab_smem = form == 0 || form == 2, ring = form >= 2;
+      const size_t bytes = pair_smem_bytes(max_gw, max_cells, p, lab_smem, ring);
+      const unsigned grid = (1 + kScoutCtas) * n_jobs;
+      if (form == 0) greedy_pair_kernel<true, false><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
+      else if (form == 1) greedy_pair_kernel<false, false><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
+      else if (form == 2) greedy_pair_kernel<true, true><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
+      else greedy_pair_kernel<false, true><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
       g_launches += 1;
       MG_CUDA(cudaGetLastError());
       return MG_OK;
