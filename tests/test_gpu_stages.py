@@ -154,6 +154,23 @@ def test_greedy_dense_palette_bit_exact(ctx, orc, p, gw, gh, max_usage, region):
         assert resets > 0
 
 
+@pytest.mark.parametrize("p,max_usage,region", [(700, 3, "smooth"), (12000, 4, "flat")])
+def test_greedy_ring_form_bit_exact(ctx, orc, p, max_usage, region):
+    """A 300x150 grid (45 000 cells) is too large for the walker's shared-memory
+    copy of the grid, so the placed cells are kept as a ring of tagged words and
+    written to the global grid as they are placed."""
+    gw, gh = 300, 150
+    rng = np.random.default_rng(p + max_usage)
+    pal = rand_lab(rng, p)
+    base = rand_lab(rng, 1)[0]
+    step = 3.0 if region == "smooth" else 0.05
+    cells = (base + np.cumsum(rng.normal(0, step, (gw * gh, 3)), axis=0)).astype(np.float32)
+    grid, resets = ctx.place_greedy(pal, cells, gw, gh, max_usage, 0.25)
+    rgrid, rresets = orc.place_greedy(pal, cells, gw, gh, max_usage, 0.25)
+    assert np.array_equal(grid, rgrid)
+    assert resets == rresets
+
+
 # ---- (e) annealing --------------------------------------------------------------------------------------------------------
 @pytest.mark.parametrize("p,gw,gh,iters,chains,t0,decay,greedy", [
     (60, 12, 9, 3000, 4, 100.0, 0.99995, False), (30, 7, 5, 500, 3, 1.0, 0.95, False),
