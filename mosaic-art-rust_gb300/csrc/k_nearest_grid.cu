@@ -18,6 +18,9 @@
 //    that box differs from q by more than R on some axis, so its rounded
 //    squared distance exceeds t (the rounding of one subtraction, one square
 //    and two sums is below 1e-6 relative) and it cannot be among the k nearest.
+//    The box edges fl(q -+ R) carry an absolute error of |q| * 2^-24, which the
+//    1e-3 widening covers while |q| * 6e-8 < 1e-3 * (sqrt(t) + 1), i.e. for
+//    colour components below 1.6e4 in magnitude (Lab's are within +-130).
 //  - Each batch of 32 row segments (two per row: the box row minus the part of
 //    it inside the cube already scanned) is prefix-summed across the warp, and
 //    the warp walks the concatenated entries 32 at a time, each lane finding
@@ -238,7 +241,7 @@ __global__ void __launch_bounds__(kGridThreads, 2) nearest_grid_kernel(
     if (!box_is_all(c, g)) {
       __syncwarp();
       warp_merge(W, len, nbuf, thr, k, lane);
-      // len == k here: the cube holds >= min(P, 3k) >= k entries
+      // the cube holds >= min(P, k) entries: len == k unless P < k
       const float r = __fsqrt_rn(__uint_as_float((uint32_t)(thr >> 32)));
       const float R = __fadd_rn(__fmul_rn(r, 1.001f), 1e-3f);
       const Box o = len < k ? Box{0, g - 1, 0, g - 1, 0, g - 1} : Box{grid_coord(__fsub_rn(q.x, R), H.lo[0], H.inv[0], g), grid_coord(__fadd_rn(q.x, R), H.lo[0], H.inv[0], g),
