@@ -54,6 +54,7 @@ _SIGS = [
     ("orc_total_cost", C.c_float, [_f32p, C.c_int, _i32p, C.c_int, C.c_int]),
     ("orc_swap_delta", C.c_float, [_f32p, C.c_int, _i32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     ("orc_place_greedy", C.c_int, [_f32p, C.c_int, _f32p, C.c_int, C.c_int, C.c_int, C.c_float, _i32p, _ip]),
+    ("orc_place_greedy_gui", C.c_int, [_f32p, C.c_int, _f32p, C.c_int, C.c_int, C.c_int, C.c_float, _i32p, _ip]),
     ("orc_philox", None, [_u32p, _u32p, _u32p]),
     ("orc_exp", C.c_float, [C.c_float]),
     ("orc_anneal", None, [_f32p, C.c_int, _i32p, C.c_int, C.c_int, C.c_long, C.c_float, C.c_float, C.c_uint64,
@@ -161,13 +162,16 @@ def nearest_n(pal: np.ndarray, queries: np.ndarray, k: int):
     return idx, dist
 
 
-def place_greedy(pal, cell_lab, gw, gh, max_usage, weight):
+def place_greedy(pal, cell_lab, gw, gh, max_usage, weight, gui=False):
+    """The CLI's greedy placement (main.rs:335-475), or with gui=True the GUI
+    generator's scoring (gui/app_full.rs:1396-1470)."""
     pal = np.ascontiguousarray(pal, np.float32).reshape(-1, 3)
     cl = np.ascontiguousarray(cell_lab, np.float32).reshape(-1, 3)
     grid = np.zeros(gw * gh, np.int32)
     resets = C.c_int()
-    lib().orc_place_greedy(p(pal, C.c_float), pal.shape[0], p(cl, C.c_float), gw, gh, max_usage, weight,
-                           p(grid, C.c_int32), C.byref(resets))
+    fn = lib().orc_place_greedy_gui if gui else lib().orc_place_greedy
+    fn(p(pal, C.c_float), pal.shape[0], p(cl, C.c_float), gw, gh, max_usage, weight, p(grid, C.c_int32),
+       C.byref(resets))
     return grid.reshape(gh, gw), resets.value
 
 

@@ -489,8 +489,14 @@ float orc_swap_delta(const float* pal, int p, const int32_t* grid, int gw, int g
 // squared Lab distance; score = squared distance + weighted penalty; strict <
 // keeps the first of equal scores.  Fallback: global usage reset, first
 // candidate that passes the same-neighbour ban, else the nearest one.
-int orc_place_greedy(const float* pal, int p, const float* cell_lab, int gw, int gh, int max_usage,
-                     float weight, int32_t* grid, int* n_resets) {
+//
+// gui: the GUI generator's selection instead (gui/app_full.rs:1396-1470
+// find_best_tile_primary, with the same two fallbacks at :1475-1568): score =
+// sqrt of the squared distance (the candidate's distance recomputed as
+// (dl^2 + da^2) + db^2, the same bits) + the penalty, computed for every weight;
+// best starts at +inf, so a candidate only wins with a score below it.
+static int place_greedy(const float* pal, int p, const float* cell_lab, int gw, int gh, int max_usage,
+                        float weight, bool gui, int32_t* grid, int* n_resets) {
   const int n = gw * gh;
   for (int i = 0; i < n; ++i) grid[i] = -1;
   int resets = 0;
@@ -515,14 +521,14 @@ int orc_place_greedy(const float* pal, int p, const float* cell_lab, int gw, int
     for (int x = 0; x < gw; ++x) {
       orc_nearest_n(pal, p, cell_lab + 3 * (y * gw + x), k, cidx.data(), cdist.data());
       int best = -1;
-      float best_score = 0.0f;
+      float best_score = gui ? INFINITY : 0.0f;
       for (int j = 0; j < k; ++j) {
         int t = (int)cidx[j];
         if (!(usage[t] < (uint32_t)max_usage)) continue;
         if (!can_place(t, x, y)) continue;
-        float pen = weight > 0.0f ? orc_penalty(pal, p, t, x, y, grid, gw, gh, weight) : 0.0f;
-        float score = cdist[j] + pen;
-        if (best < 0 || score < best_score) { best = t; best_score = score; }
+        float pen = gui || weight > 0.0f ? orc_penalty(pal, p, t, x, y, grid, gw, gh, weight) : 0.0f;
+        float score = (gui ? std::sqrt(cdist[j]) : cdist[j]) + pen;
+        if ((!gui && best < 0) || score < best_score) { best = t; best_score = score; }
       }
       if (best >= 0) {
         usage[best] += 1;
@@ -540,6 +546,16 @@ int orc_place_greedy(const float* pal, int p, const float* cell_lab, int gw, int
     }
   if (n_resets) *n_resets = resets;
   return 0;
+}
+
+int orc_place_greedy(const float* pal, int p, const float* cell_lab, int gw, int gh, int max_usage,
+                     float weight, int32_t* grid, int* n_resets) {
+  return place_greedy(pal, p, cell_lab, gw, gh, max_usage, weight, false, grid, n_resets);
+}
+
+int orc_place_greedy_gui(const float* pal, int p, const float* cell_lab, int gw, int gh, int max_usage,
+                         float weight, int32_t* grid, int* n_resets) {
+  return place_greedy(pal, p, cell_lab, gw, gh, max_usage, weight, true, grid, n_resets);
 }
 
 void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { philox4x32_10(ctr, key, out); }

@@ -55,6 +55,9 @@ float orc_swap_delta(const float* pal, int p, const int32_t* grid, int gw, int g
                      int x1, int y1, int x2, int y2);
 int   orc_place_greedy(const float* pal, int p, const float* cell_lab, int gw, int gh,
                        int max_usage, float weight, int32_t* grid, int* n_resets);
+/* the GUI generator's scoring (gui/app_full.rs:1396-1470): sqrt distance + penalty */
+int   orc_place_greedy_gui(const float* pal, int p, const float* cell_lab, int gw, int gh,
+                           int max_usage, float weight, int32_t* grid, int* n_resets);
 
 /* ---- annealing (optimizer.rs:41-129) -------------------------------------- */
 void  orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

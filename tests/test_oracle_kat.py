@@ -327,3 +327,48 @@ def test_greedy_empty_palette(orc):
 def test_greedy_single_material_falls_back_to_nearest(orc):
     grid, resets = orc.place_greedy(np.array([[50, 0, 0]], np.float32), np.zeros((4, 3), np.float32), 2, 2, 3, 0.3)
     assert np.all(grid == 0)
+
+
+# ---- gui/app_full.rs:1396-1568 the GUI generator's selection ----------------------------------------------------------
+def test_gui_scoring_known_answer(orc):
+    """Left neighbour T0 = (50,0,0); the cell wants (52,0,0).  T1 = (51,0,0) is 1 away
+    (squared 1) and 1 from T0 (penalty 1/2 per unit weight); T2 = (54,0,0) is 2 away
+    (squared 4) and 4 from T0 (penalty 1/5).  At weight 5 the CLI scores 1 + 2.5 vs
+    4 + 1 and keeps T1; the GUI scores sqrt: 1 + 2.5 vs 2 + 1 and takes T2."""
+    lab = np.array([[50, 0, 0], [51, 0, 0], [54, 0, 0]], np.float32)
+    cells = np.array([[50, 0, 0], [52, 0, 0]], np.float32)
+    cli, r1 = orc.place_greedy(lab, cells, 2, 1, 10, 5.0)
+    gui, r2 = orc.place_greedy(lab, cells, 2, 1, 10, 5.0, gui=True)
+    assert cli.tolist() == [[0, 1]] and gui.tolist() == [[0, 2]] and r1 == r2 == 0
+    f = np.float32
+    assert f(1) + f(5) * f(0.5) < f(4) + f(5) * (f(1) / f(5))
+    assert f(2) + f(5) * (f(1) / f(5)) < f(1) + f(5) * f(0.5)
+
+
+def test_gui_equals_cli_without_penalty(orc):
+    """sqrt is monotone and candidates come in ascending distance, so with weight 0
+    the GUI picks the CLI's tile everywhere, fallbacks (usage resets) included."""
+    rng = np.random.default_rng(5)
+    resets = 0
+    for p, mu in [(3, 1), (40, 2), (150, 1), (400, 3)]:
+        lab = np.empty((p, 3), np.float32)
+        lab[:, 0] = rng.uniform(0, 100, p)
+        lab[:, 1:] = rng.uniform(-60, 60, (p, 2))
+        cells = lab[rng.integers(0, p, 12 * 9)] + rng.normal(0, 2, (12 * 9, 3)).astype(np.float32)
+        a, ra = orc.place_greedy(lab, cells, 12, 9, mu, 0.0)
+        b, rb = orc.place_greedy(lab, cells, 12, 9, mu, 0.0, gui=True)
+        assert np.array_equal(a, b) and ra == rb
+        resets += ra
+    assert resets > 0  # the fallback path ran
+
+
+def test_gui_penalty_changes_choices(orc):
+    """With a penalty the two scorings part: sqrt shrinks the colour term against it."""
+    rng = np.random.default_rng(6)
+    lab = np.empty((2000, 3), np.float32)
+    lab[:, 0] = rng.uniform(0, 100, 2000)
+    lab[:, 1:] = rng.uniform(-60, 60, (2000, 2))
+    cells = lab[rng.integers(0, 2000, 400)] + rng.normal(0, 3, (400, 3)).astype(np.float32)
+    a, _ = orc.place_greedy(lab, cells, 20, 20, 4, 100.0)
+    b, _ = orc.place_greedy(lab, cells, 20, 20, 4, 100.0, gui=True)
+    assert np.all(b >= 0) and not np.array_equal(a, b)
