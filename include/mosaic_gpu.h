@@ -96,6 +96,35 @@ int mg_images_lab(mg_ctx* ctx, const uint8_t* const* imgs, const int* w, const i
 int mg_select_palette(const int* widths, const int* heights, int n, float target_aspect,
                       float tolerance, int max_materials, int* selected);
 
+/* ---- image files: the two ends of the path (host code) --------------------------- */
+/* main.rs:492, 548 image::open + DynamicImage::to_rgb8 (image 0.25.6 / png
+ * 0.17.16) for PNG data held in memory, and main.rs:672 DynamicImage::save
+ * for a .png path.  Every PNG 1.2 colour type, bit depth and interlace is
+ * read: grey is replicated to three channels, alpha dropped, palette indices
+ * looked up, 1/2/4-bit grey scaled to 8 bits, 16-bit samples rounded to 8
+ * bits.  Chunk CRCs and the zlib checksum are checked (MG_ERR_ARG with a
+ * message on any defect).  These calls need no context or GPU and may run on
+ * any thread. */
+/* Width and height of the PNG file data[0..n). */
+int mg_png_info(const uint8_t* data, size_t n, int* w, int* h);
+/* Decodes into out: h rows of `stride` bytes (>= 3*w), e.g. pinned memory from
+ * mg_host_alloc that mg_generate then reads in place. */
+int mg_png_decode(const uint8_t* data, size_t n, uint8_t* out, int64_t stride);
+/* `count` files on up to `threads` host threads (<= 0: one per hardware
+ * thread); status (nullable) receives each file's code; returns the first
+ * failure's code (its message names the file's position). */
+int mg_png_decode_batch(const uint8_t* const* data, const size_t* n, int count, uint8_t* const* out,
+                        const int64_t* stride, int threads, int* status);
+/* Largest file mg_png_encode writes for a w x h image (0 for invalid sizes). */
+size_t mg_png_encode_bound(int w, int h);
+/* Encodes an RGB8 image as an 8-bit RGB PNG: per row the filter with the
+ * smallest sum of absolute residuals; level 0 stores the rows uncompressed,
+ * level 1 codes each 64 KB block with its own Huffman code (or stores it when
+ * that is smaller).  out must hold mg_png_encode_bound(w, h) bytes (else
+ * MG_ERR_ARG with *len = that bound); *len receives the file size. */
+int mg_png_encode(const uint8_t* rgb, int w, int h, int64_t stride, int level, int threads, uint8_t* out,
+                  size_t cap, size_t* len);
+
 /* ---- similarity database --------------------------------------------------------- */
 /* similarity.rs:69-82 build_similarities (+ similarity.rs:141-146
  * calculate_lab_distance) on the device.  layout MG_SIM_FULL or

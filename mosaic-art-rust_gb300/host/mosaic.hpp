@@ -14,6 +14,8 @@
 //   ColorAdjustment /
 //   calculate_optimal_adjustment            color_adjustment.rs:6-154
 //   generate_mosaic                         main.rs:105-164 + 477-685
+//   open_png / save_png                     main.rs:492, 548, 672 (image::open
+//                                           + to_rgb8, DynamicImage::save)
 // plus RAII handles for the resident palette, batches and the request loop.
 //
 // Error behaviour: where the crate returns Option the mirror returns
@@ -42,6 +44,7 @@
 #include <cstring>
 #include <filesystem>
 #include <fstream>
+#include <iterator>
 #include <map>
 #include <memory>
 #include <optional>
@@ -123,6 +126,40 @@ struct RgbImage {
   std::vector<uint8_t> pixels;  // height x width x 3
   RgbImageView view() const { return {pixels.data(), width, height, 3 * (int64_t)width}; }
 };
+
+// ---- image files: PNG at the two ends of the path --------------------------------------
+// PNG data held in memory as RGB8 (image::load_from_memory + to_rgb8).
+inline RgbImage decode_png(const uint8_t* data, size_t n) {
+  RgbImage img;
+  detail::check(mg_png_info(data, n, &img.width, &img.height));
+  img.pixels.resize((size_t)img.width * img.height * 3);
+  detail::check(mg_png_decode(data, n, img.pixels.data(), 3 * (int64_t)img.width));
+  return img;
+}
+// main.rs:492, 548: image::open(path)?.to_rgb8() for a PNG file.
+inline RgbImage open_png(const Path& path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw Error(MG_ERR_ARG, "cannot open " + path.string());
+  std::vector<uint8_t> data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  return decode_png(data.data(), data.size());
+}
+// An RGB8 image as PNG file data: level 0 stores the filtered rows, level 1
+// codes each 64 KB block with its own Huffman code; `threads` <= 0: all.
+inline std::vector<uint8_t> encode_png(const RgbImageView& img, int level = 1, int threads = 0) {
+  std::vector<uint8_t> out(mg_png_encode_bound(img.width, img.height));
+  size_t len = 0;
+  detail::check(mg_png_encode(img.data, img.width, img.height, img.row_bytes(), level, threads, out.data(),
+                              out.size(), &len));
+  out.resize(len);
+  return out;
+}
+// main.rs:672: DynamicImage::save(path) for a .png path.
+inline void save_png(const RgbImageView& img, const Path& path, int level = 1, int threads = 0) {
+  const std::vector<uint8_t> data = encode_png(img, level, threads);
+  std::ofstream f(path, std::ios::binary | std::ios::trunc);
+  if (!f || !f.write(reinterpret_cast<const char*>(data.data()), (std::streamsize)data.size()))
+    throw Error(MG_ERR_ARG, "cannot write " + path.string());
+}
 
 // similarity.rs:141-146
 inline float calculate_lab_distance(const Lab& a, const Lab& b) {

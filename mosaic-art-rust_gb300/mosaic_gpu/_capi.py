@@ -141,6 +141,13 @@ SIGNATURES = [
                                 C.c_int, _f32p, _u8p]),
     ("mg_select_palette", C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_float, C.c_float,
                                     C.c_int, C.POINTER(C.c_int)]),
+    ("mg_png_info", C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("mg_png_decode", C.c_int, [C.c_void_p, C.c_size_t, _u8p, C.c_int64]),
+    ("mg_png_decode_batch", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_size_t), C.c_int, C.POINTER(_u8p),
+                                      _i64p, C.c_int, C.POINTER(C.c_int)]),
+    ("mg_png_encode_bound", C.c_size_t, [C.c_int, C.c_int]),
+    ("mg_png_encode", C.c_int, [_u8p, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_int, _u8p, C.c_size_t,
+                                C.POINTER(C.c_size_t)]),
     ("mg_similarity_build", C.c_int, [C.c_void_p, _f32p, C.c_int, C.c_int, _f32p]),
     ("mg_lab_distance", C.c_float, [_f32p, _f32p]),
     ("mg_nearest_n", C.c_int, [C.c_void_p, _f32p, C.c_int, _f32p, C.c_int, C.c_int, _u32p, _f32p]),
@@ -376,3 +383,55 @@ def improvement_percentage(r: SaResult) -> float:
 def color_adjustment_new(b: float, c: float, h: float, s: float):
     a = load().mg_color_adjustment_new(b, c, h, s)
     return (a.brightness, a.contrast, a.hue_shift, a.saturation)
+
+
+# ---- PNG files (host code: no context, no GPU) -----------------------------------------
+def png_info(data: bytes) -> tuple[int, int]:
+    w, h = C.c_int(), C.c_int()
+    check(load().mg_png_info(data, len(data), C.byref(w), C.byref(h)))
+    return w.value, h.value
+
+
+def png_decode(data: bytes, out: np.ndarray | None = None) -> np.ndarray:
+    """The file as an (h, w, 3) uint8 array (written into `out`, e.g. a view
+    of pinned memory, when given)."""
+    w, h = png_info(data)
+    if out is None:
+        out = np.empty((h, w, 3), np.uint8)
+    if out.dtype != np.uint8 or out.ndim != 3 or out.shape != (h, w, 3) or out.strides[1:] != (3, 1):
+        raise ValueError("out must be a (h, w, 3) uint8 array with contiguous rows")
+    check(load().mg_png_decode(data, len(data), ptr(out, C.c_uint8), out.strides[0]))
+    return out
+
+
+def png_decode_batch(files: list[bytes], threads: int = 0) -> tuple[list[np.ndarray | None], list[int]]:
+    """Decodes every file on up to `threads` threads; (images, status codes)."""
+    n = len(files)
+    outs = []
+    for f in files:
+        try:
+            w, h = png_info(f)
+            outs.append(np.empty((h, w, 3), np.uint8))
+        except MosaicError:
+            outs.append(np.zeros((1, 1, 3), np.uint8))  # decode reports the defect
+    bufs = [C.create_string_buffer(f, len(f)) for f in files]
+    data = (C.c_void_p * max(n, 1))(*[C.cast(b, C.c_void_p) for b in bufs])
+    sizes = (C.c_size_t * max(n, 1))(*[len(f) for f in files])
+    out_p = (_u8p * max(n, 1))(*[ptr(o, C.c_uint8) for o in outs])
+    strides = (C.c_int64 * max(n, 1))(*[o.strides[0] for o in outs])
+    status = (C.c_int * max(n, 1))()
+    load().mg_png_decode_batch(data, sizes, n, out_p, strides, threads, status)
+    codes = [status[i] for i in range(n)]
+    return [o if c == MG_OK else None for o, c in zip(outs, codes)], codes
+
+
+def png_encode(img: np.ndarray, level: int = 1, threads: int = 0) -> bytes:
+    img = np.ascontiguousarray(img, np.uint8)
+    h, w = img.shape[:2]
+    lib = load()
+    cap = lib.mg_png_encode_bound(w, h)
+    out = np.empty(max(cap, 1), np.uint8)
+    n = C.c_size_t()
+    check(lib.mg_png_encode(ptr(img, C.c_uint8), w, h, img.strides[0], level, threads, ptr(out, C.c_uint8), cap,
+                            C.byref(n)))
+    return out[: n.value].tobytes()

@@ -435,6 +435,45 @@ static void generate_tests() {
   CHECK(empty && none.palette_size == 0);
 }
 
+static void png_tests() {  // main.rs:1888-1912 (missing, corrupted files), 2219-2240 (save, then load)
+  RgbImage red;  // create_test_image(100, 100, Rgb([255, 0, 0]))
+  red.width = red.height = 100;
+  red.pixels.resize(100 * 100 * 3);
+  for (size_t i = 0; i < red.pixels.size(); i += 3) red.pixels[i] = 255;
+  RgbImage noise;
+  noise.width = 37;
+  noise.height = 23;
+  noise.pixels.resize(37 * 23 * 3);
+  for (size_t i = 0; i < noise.pixels.size(); ++i) noise.pixels[i] = (uint8_t)((i * 7) ^ (i >> 5));
+  const Path file = tmp_file("_test.PNG");
+  for (const RgbImage* img : {&red, &noise})
+    for (int level : {0, 1}) {
+      save_png(img->view(), file, level, 2);
+      const RgbImage back = open_png(file);
+      CHECK(back.width == img->width && back.height == img->height && back.pixels == img->pixels);
+    }
+  const std::string junk = "this is not an image";
+  {
+    std::ofstream f(file, std::ios::binary | std::ios::trunc);
+    f << junk;
+  }
+  bool threw = false;
+  try {
+    open_png(file);
+  } catch (const Error& e) {
+    threw = e.code() == MG_ERR_ARG;
+  }
+  CHECK(threw);
+  std::filesystem::remove(file);
+  threw = false;
+  try {
+    open_png(tmp_file("_nonexistent.png"));
+  } catch (const Error&) {
+    threw = true;
+  }
+  CHECK(threw);
+}
+
 int main(int argc, char** argv) {
   const bool gpu = argc > 1 && std::strcmp(argv[1], "--gpu") == 0;
   usage_tracker_tests();
@@ -444,6 +483,7 @@ int main(int argc, char** argv) {
   similarity_host_tests();
   color_host_tests();
   result_tests();
+  png_tests();
   if (gpu) {
     average_lab_tests();
     similarity_device_tests();

@@ -1,0 +1,363 @@
+"""PNG files at the two ends of the path (csrc/io_png.cpp; image::open + to_rgb8
+of main.rs:492/548 and DynamicImage::save of main.rs:672), on the CPU.
+
+The checker is independent of the library: PNG files are written here with
+Python's zlib (every compression level and strategy, so stored, fixed- and
+dynamic-Huffman blocks and long matches all occur) from numpy-filtered rows
+(every filter type), for every colour type, bit depth and both interlace
+methods, and the expected RGB8 follows the conversions to_rgb8 applies (grey
+replicated, alpha dropped, palette looked up, low-bit grey scaled, 16-bit
+rounded).  Files the library writes are inflated here with zlib and checked
+row by row against the image they encode (check_rows).  Defective files must
+fail with MG_ERR_ARG, never crash.
+"""
+import struct
+import zlib
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+SIG = b"\x89PNG\r\n\x1a\n"
+ADAM7 = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2)]
+CHANNELS = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}
+
+
+@pytest.fixture(scope="module")
+def capi(built):
+    from mosaic_gpu import _capi
+
+    return _capi
+
+
+def chunk(kind: bytes, data: bytes) -> bytes:
+    return struct.pack(">I", len(data)) + kind + data + struct.pack(">I", zlib.crc32(kind + data) & 0xFFFFFFFF)
+
+
+def paeth(a, b, c):
+    p = a + b - c
+    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+    if pa <= pb and pa <= pc:
+        return a
+    return b if pb <= pc else c
+
+
+def filter_rows(rows: np.ndarray, bpp: int, rng) -> bytes:
+    """rows: (h, rowbytes) uint8; each row gets a random filter type."""
+    out = bytearray()
+    prev = np.zeros(rows.shape[1], np.int32)
+    for r in rows.astype(np.int32):
+        f = int(rng.integers(0, 5))
+        a = np.concatenate([np.zeros(bpp, np.int32), r[:-bpp]]) if len(r) > bpp else np.zeros_like(r)
+        c = np.concatenate([np.zeros(bpp, np.int32), prev[:-bpp]]) if len(r) > bpp else np.zeros_like(r)
+        if f == 0:
+            res = r
+        elif f == 1:
+            res = r - a
+        elif f == 2:
+            res = r - prev
+        elif f == 3:
+            res = r - ((a + prev) >> 1)
+        else:
+            res = r - np.array([paeth(int(x), int(y), int(z)) for x, y, z in zip(a, prev, c)], np.int32)
+        out.append(f)
+        out += (res & 0xFF).astype(np.uint8).tobytes()
+        prev = r
+    return bytes(out)
+
+
+def pack_samples(samples: np.ndarray, depth: int) -> np.ndarray:
+    """(h, n) samples of `depth` bits -> (h, rowbytes) bytes, MSB first / big-endian."""
+    h, n = samples.shape
+    if depth == 8:
+        return samples.astype(np.uint8)
+    if depth == 16:
+        s = samples.astype(np.uint16)
+        return np.stack([(s >> 8).astype(np.uint8), (s & 0xFF).astype(np.uint8)], -1).reshape(h, 2 * n)
+    per = 8 // depth
+    pad = (-n) % per
+    s = np.concatenate([samples, np.zeros((h, pad), samples.dtype)], 1).reshape(h, -1, per).astype(np.uint32)
+    shifts = np.array([8 - depth * (i + 1) for i in range(per)], np.uint32)
+    return (s << shifts).sum(-1).astype(np.uint8)
+
+
+def write_png(samples: np.ndarray, color: int, depth: int, rng, interlace=0, level=6, strategy=zlib.Z_DEFAULT_STRATEGY,
+              plte: bytes | None = None, extra=(), idat_split=1) -> bytes:
+    """samples: (h, w, channels) integers of `depth` bits."""
+    h, w, ch = samples.shape
+    bits_pp = ch * depth
+    bpp = max(1, bits_pp // 8)
+    raw = bytearray()
+    passes = ADAM7 if interlace else [(0, 0, 1, 1)]
+    for x0, y0, dx, dy in passes:
+        sub = samples[y0::dy, x0::dx]
+        if sub.shape[0] == 0 or sub.shape[1] == 0:
+            continue
+        rows = pack_samples(sub.reshape(sub.shape[0], -1), depth)
+        raw += filter_rows(rows, bpp, rng)
+    comp = zlib.compressobj(level, zlib.DEFLATED, 15, 9, strategy)
+    z = comp.compress(bytes(raw)) + comp.flush()
+    out = SIG + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, color, 0, 0, interlace))
+    for kind, data in extra:
+        out += chunk(kind, data)
+    if plte is not None:
+        out += chunk(b"PLTE", plte)
+    cuts = sorted(set([0, len(z)] + [int(v) for v in rng.integers(0, len(z) + 1, idat_split - 1)]))
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        out += chunk(b"IDAT", z[a:b])
+    if len(cuts) == 1:
+        out += chunk(b"IDAT", z)
+    return out + chunk(b"IEND", b"")
+
+
+def expected_rgb(samples: np.ndarray, color: int, depth: int, plte: bytes | None = None) -> np.ndarray:
+    s = samples.astype(np.uint32)
+    if depth == 16:
+        s = (s + 128) // 257
+    elif depth < 8 and color == 0:
+        s = s * (255 // ((1 << depth) - 1))
+    if color == 3:
+        pal = np.frombuffer(plte, np.uint8).reshape(-1, 3)
+        full = np.zeros((256, 3), np.uint8)
+        full[: len(pal)] = pal
+        return full[s[..., 0]]
+    if color in (0, 4):
+        return np.repeat(s[..., :1], 3, axis=2).astype(np.uint8)
+    return s[..., :3].astype(np.uint8)
+
+
+def parse(data: bytes):
+    """(IHDR fields, zlib-inflated image data) of a PNG, CRCs checked."""
+    assert data[:8] == SIG
+    pos, z, ihdr = 8, b"", None
+    while pos < len(data):
+        (n,) = struct.unpack(">I", data[pos:pos + 4])
+        kind, body = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
+        (crc,) = struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])
+        assert crc == zlib.crc32(kind + body) & 0xFFFFFFFF
+        if kind == b"IHDR":
+            ihdr = struct.unpack(">IIBBBBB", body)
+        elif kind == b"IDAT":
+            z += body
+        pos += 12 + n
+    return ihdr, zlib.decompress(z)
+
+
+def check_rows(data: bytes, rgb: np.ndarray) -> None:
+    """`rgb` is the R, G, B content of the 8-bit, non-interlaced RGB or RGBA PNG
+    `data`: refiltering rgb with each row's own filter type reproduces the
+    file's filtered bytes of those channels.  Unfiltering is the unique inverse
+    of that, so this pins every pixel, and it vectorises over whole images."""
+    (w, h, depth, color, _, _, inter), raw = parse(data)
+    assert depth == 8 and color in (2, 6) and inter == 0 and rgb.shape == (h, w, 3)
+    ch = CHANNELS[color]
+    raw = np.frombuffer(raw, np.uint8).reshape(h, 1 + w * ch)
+    f = raw[:, 0].astype(np.int32)[:, None, None]
+    res = raw[:, 1:].reshape(h, w, ch)[..., :3].astype(np.int32)
+    x = rgb.astype(np.int32)
+    a = np.zeros_like(x)
+    a[:, 1:] = x[:, :-1]
+    b = np.zeros_like(x)
+    b[1:] = x[:-1]
+    c = np.zeros_like(x)
+    c[1:, 1:] = x[:-1, :-1]
+    p = a + b - c
+    pa, pb, pc = np.abs(p - a), np.abs(p - b), np.abs(p - c)
+    pae = np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, b, c))
+    pred = np.select([f == 0, f == 1, f == 2, f == 3, f == 4], [0 * x, a, b, (a + b) >> 1, pae])
+    assert np.all(f <= 4)
+    assert np.array_equal((x - pred) & 0xFF, res)
+
+
+CASES = [(0, 1), (0, 2), (0, 4), (0, 8), (0, 16), (2, 8), (2, 16), (3, 1), (3, 2), (3, 4), (3, 8), (4, 8), (4, 16),
+         (6, 8), (6, 16)]
+
+
+@pytest.mark.parametrize("interlace", [0, 1])
+@pytest.mark.parametrize("color,depth", CASES)
+def test_decode_every_format(capi, color, depth, interlace):
+    rng = np.random.default_rng(color * 100 + depth * 2 + interlace)
+    for w, h in [(1, 1), (3, 2), (9, 5), (17, 13), (33, 8)]:
+        ch = CHANNELS[color]
+        top = (1 << depth) - 1
+        plte = None
+        if color == 3:
+            npal = int(rng.integers(1, min(256, top + 1) + 1))
+            plte = rng.integers(0, 256, 3 * npal, dtype=np.uint8).tobytes()
+            top = min(top, 255)  # indices past the palette read as black
+        samples = rng.integers(0, top + 1, (h, w, ch)).astype(np.uint32)
+        data = write_png(samples, color, depth, rng, interlace=interlace, plte=plte)
+        assert capi.png_info(data) == (w, h)
+        got = capi.png_decode(data)
+        assert np.array_equal(got, expected_rgb(samples, color, depth, plte)), (w, h)
+
+
+@pytest.mark.parametrize("level,strategy", [(0, zlib.Z_DEFAULT_STRATEGY), (1, zlib.Z_DEFAULT_STRATEGY),
+                                            (6, zlib.Z_DEFAULT_STRATEGY), (9, zlib.Z_DEFAULT_STRATEGY),
+                                            (9, zlib.Z_FILTERED), (6, zlib.Z_HUFFMAN_ONLY), (6, zlib.Z_RLE),
+                                            (6, zlib.Z_FIXED)])
+def test_decode_every_deflate_form(capi, level, strategy):
+    """Smooth and noisy content (long matches, overlapping copies, literals),
+    split over several IDAT chunks with ancillary chunks in front."""
+    rng = np.random.default_rng(level * 10 + strategy)
+    y, x = np.mgrid[0:150, 0:211]
+    smooth = np.stack([(x // 7) % 256, (y // 3) % 256, np.full_like(x, 77)], -1)
+    noisy = rng.integers(0, 256, (150, 211, 3))
+    img = np.where(rng.random((150, 211, 1)) < 0.2, noisy, smooth).astype(np.uint32)
+    data = write_png(img, 2, 8, rng, level=level, strategy=strategy, idat_split=5,
+                     extra=[(b"gAMA", struct.pack(">I", 45455)), (b"tEXt", b"Comment\x00test")])
+    assert np.array_equal(capi.png_decode(data), img.astype(np.uint8))
+
+
+def test_decode_into_strided_buffer(capi):
+    rng = np.random.default_rng(3)
+    img = rng.integers(0, 256, (20, 30, 3)).astype(np.uint32)
+    data = write_png(img, 2, 8, rng)
+    big = np.full((20, 40, 3), 7, np.uint8)
+    view = big[:, 5:35]
+    out = np.ascontiguousarray(view)  # contiguous rows of 90 bytes
+    capi.png_decode(data, out)
+    assert np.array_equal(out, img.astype(np.uint8))
+    lib = capi.load()
+    rc = lib.mg_png_decode(data, len(data), capi.ptr(big, np.ctypeslib.ctypes.c_uint8), big.strides[0])
+    assert rc == 0 and np.array_equal(big[:, :30], img.astype(np.uint8)) and np.all(big[:, 30:] == 7)
+
+
+def _corrupt_cases(rng):
+    img = rng.integers(0, 256, (12, 9, 3)).astype(np.uint32)
+    good = write_png(img, 2, 8, rng)
+    cases = {"empty": b"", "signature": b"\x00" + good[1:], "truncated_header": good[:20]}
+    b = bytearray(good)
+    b[20] ^= 1  # IHDR data, CRC now wrong
+    cases["ihdr_crc"] = bytes(b)
+    idat = good.index(b"IDAT")
+    b = bytearray(good)
+    b[idat + 10] ^= 0x40  # compressed data, CRC now wrong
+    cases["idat_crc"] = bytes(b)
+    cases["cut_in_idat"] = good[: idat + 20]
+    # valid CRCs, broken contents
+    def rebuild(z, w=9, h=12, depth=8, color=2):
+        return SIG + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, color, 0, 0, 0)) + chunk(b"IDAT", z) + \
+            chunk(b"IEND", b"")
+    raw = bytes(12 * (1 + 27))
+    z = zlib.compress(raw)
+    cases["adler"] = rebuild(z[:-1] + bytes([z[-1] ^ 1]))
+    cases["short_data"] = rebuild(zlib.compress(raw[:-5]))
+    cases["long_data"] = rebuild(zlib.compress(raw + bytes(40)))
+    cases["bad_filter"] = rebuild(zlib.compress(b"\x07" + raw[1:]))
+    cases["bad_depth"] = rebuild(z, depth=3)
+    cases["bad_color"] = rebuild(z, color=5)
+    cases["zero_width"] = rebuild(z, w=0)
+    cases["palette_without_plte"] = rebuild(zlib.compress(bytes(12 * 10)), color=3)
+    cases["zlib_header"] = rebuild(b"\x00\x00" + z[2:])
+    cases["bad_block_type"] = rebuild(b"\x78\x01\x07" + z[3:])
+    cases["unknown_critical"] = good[:33] + chunk(b"ABCD", b"x") + good[33:]
+    return cases
+
+
+def test_defective_files_fail_cleanly(capi):
+    rng = np.random.default_rng(4)
+    for name, data in _corrupt_cases(rng).items():
+        out = np.zeros((64, 64, 3), np.uint8)
+        lib = capi.load()
+        rc = lib.mg_png_decode(data, len(data), capi.ptr(out, np.ctypeslib.ctypes.c_uint8), 64 * 3)
+        assert rc == capi.MG_ERR_ARG, name
+        assert lib.mg_last_error().decode(), name
+
+
+def test_truncation_at_every_byte_never_crashes(capi):
+    rng = np.random.default_rng(5)
+    img = rng.integers(0, 256, (6, 7, 3)).astype(np.uint32)
+    data = write_png(img, 2, 8, rng, level=9)
+    lib = capi.load()
+    out = np.zeros((6, 7, 3), np.uint8)
+    for cut in range(len(data) - 12):  # IEND (the last 12 bytes) is optional
+        rc = lib.mg_png_decode(data[:cut], cut, capi.ptr(out, np.ctypeslib.ctypes.c_uint8), 21)
+        assert rc == capi.MG_ERR_ARG, cut
+
+
+def test_random_bit_flips_never_crash(capi):
+    rng = np.random.default_rng(6)
+    img = rng.integers(0, 256, (16, 16, 3)).astype(np.uint32)
+    good = write_png(img, 2, 8, rng)
+    idat = good.index(b"IDAT") + 4
+    n = struct.unpack(">I", good[idat - 8:idat - 4])[0]
+    lib = capi.load()
+    out = np.zeros((16, 16, 3), np.uint8)
+    for t in range(300):
+        body = bytearray(good[idat:idat + n])
+        for _ in range(int(rng.integers(1, 4))):
+            body[int(rng.integers(0, n))] ^= 1 << int(rng.integers(0, 8))
+        data = good[:idat - 8] + chunk(b"IDAT", bytes(body)) + good[idat + n + 4:]
+        rc = lib.mg_png_decode(data, len(data), capi.ptr(out, np.ctypeslib.ctypes.c_uint8), 48)
+        assert rc in (capi.MG_OK, capi.MG_ERR_ARG)
+
+
+@pytest.mark.parametrize("level", [0, 1])
+def test_encode_reads_back(capi, level):
+    rng = np.random.default_rng(7 + level)
+    for w, h in [(1, 1), (2, 3), (31, 17), (200, 3)]:
+        img = rng.integers(0, 256, (h, w, 3), dtype=np.uint8)
+        data = capi.png_encode(img, level)
+        check_rows(data, img)
+        assert len(data) <= capi.load().mg_png_encode_bound(w, h)
+
+
+def test_encode_large_compresses_and_round_trips(capi):
+    """Several 64 KB blocks and IDAT chunks, thread counts 1 and 8 give the same file."""
+    y, x = np.mgrid[0:1200, 0:1700]
+    img = np.stack([(x // 3) % 256, (y // 2) % 256, ((x + y) // 5) % 256], -1).astype(np.uint8)
+    img[::37] = 255
+    a = capi.png_encode(img, 1, threads=1)
+    b = capi.png_encode(img, 1, threads=8)
+    assert a == b
+    s = capi.png_encode(img, 0)
+    assert len(a) < 0.5 * len(s) and len(s) >= img.nbytes
+    check_rows(a, img)  # zlib inflates it (Adler-32 included) to the image's rows
+    check_rows(s, img)
+    assert np.array_equal(capi.png_decode(a), img) and np.array_equal(capi.png_decode(s), img)
+
+
+def test_encode_arguments(capi):
+    lib = capi.load()
+    img = np.zeros((4, 4, 3), np.uint8)
+    n = np.ctypeslib.ctypes.c_size_t()
+    small = np.zeros(10, np.uint8)
+    u8 = np.ctypeslib.ctypes.c_uint8
+    rc = lib.mg_png_encode(capi.ptr(img, u8), 4, 4, 12, 1, 1, capi.ptr(small, u8), 10, np.ctypeslib.ctypes.byref(n))
+    assert rc == capi.MG_ERR_ARG and n.value == lib.mg_png_encode_bound(4, 4)
+    assert lib.mg_png_encode_bound(0, 4) == 0
+    with pytest.raises(capi.MosaicError):
+        capi.png_encode(img, level=2)
+
+
+def test_batch_decode(capi):
+    rng = np.random.default_rng(8)
+    imgs, files = [], []
+    for i in range(40):
+        w, h = int(rng.integers(1, 60)), int(rng.integers(1, 60))
+        img = rng.integers(0, 256, (h, w, 3)).astype(np.uint32)
+        imgs.append(img.astype(np.uint8))
+        files.append(write_png(img, 2, 8, rng, interlace=i % 2))
+    files[13] = files[13][:-40]  # cut inside the image data
+    got, codes = capi.png_decode_batch(files, threads=6)
+    for i, (img, g, c) in enumerate(zip(imgs, got, codes)):
+        if i == 13:
+            assert c == capi.MG_ERR_ARG and g is None
+        else:
+            assert c == capi.MG_OK and np.array_equal(g, img)
+    assert "file 13" in capi.load().mg_last_error().decode()
+
+
+@pytest.mark.parametrize("name", ["examples/mosaic.png", "docs/public/hero-image.png"])
+def test_reference_example_images(capi, name):
+    """The PNG files shipped with mosaic-art-rust (an RGBA mosaic the tool made,
+    3840x2160, and an RGB image in 32 IDAT chunks), where the source tree is
+    present: decoded, then checked row by row against the files' own filtered
+    data as zlib inflates it."""
+    path = Path("/root/reference") / name
+    if not path.exists():
+        pytest.skip("mosaic-art-rust source tree not present")
+    data = path.read_bytes()
+    rgb = capi.png_decode(data)
+    check_rows(data, rgb)
