@@ -361,3 +361,47 @@ def test_reference_example_images(capi, name):
     data = path.read_bytes()
     rgb = capi.png_decode(data)
     check_rows(data, rgb)
+
+
+def test_fuzz_under_sanitizers(tmp_path):
+    """Mutated files (tests/cpp/png_fuzz.cpp) against the decoder built with
+    AddressSanitizer and UndefinedBehaviorSanitizer: small seeds of every
+    format, and large ones that take the two-thread pipeline."""
+    import shutil
+    import subprocess
+
+    repo = Path(__file__).resolve().parents[1]
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    exe = tmp_path / "png_fuzz"
+    cmd = ["g++", "-O1", "-g", "-std=c++17", "-fsanitize=address,undefined", "-fno-sanitize-recover=undefined",
+           f"-I{repo / 'include'}", "-pthread", str(repo / "tests" / "cpp" / "png_fuzz.cpp"),
+           str(repo / "mosaic-art-rust_gb300" / "csrc" / "io_png.cpp"), "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0 and "sanitize" in r.stderr:
+        pytest.skip("the compiler has no sanitizer runtime")
+    assert r.returncode == 0, r.stderr
+    rng = np.random.default_rng(1)
+    small, large = [], []
+    for color, depth in CASES:
+        for inter in (0, 1):
+            top = (1 << depth) - 1
+            plte = rng.integers(0, 256, 3 * min(256, top + 1), dtype=np.uint8).tobytes() if color == 3 else None
+            s = rng.integers(0, top + 1, (13, 11, CHANNELS[color])).astype(np.uint32)
+            p = tmp_path / f"s{color}_{depth}_{inter}.png"
+            p.write_bytes(write_png(s, color, depth, rng, interlace=inter, plte=plte, level=int(rng.integers(0, 10))))
+            small.append(str(p))
+    y, x = np.mgrid[0:600, 0:800]
+    img = np.stack([(x // 3) % 256, (y // 2) % 256, ((x + y) // 5) % 256], -1)
+    img = np.where(rng.random((600, 800, 1)) < 0.3, rng.integers(0, 256, (600, 800, 3)), img).astype(np.uint32)
+    for i, (kw, im, color) in enumerate([(dict(level=6, idat_split=3), img, 2),
+                                         (dict(level=1, strategy=zlib.Z_RLE),
+                                          np.concatenate([img, img[..., :1]], -1), 6)]):
+        p = tmp_path / f"l{i}.png"
+        p.write_bytes(write_png(im, color, 8, rng, **kw))
+        large.append(str(p))
+    env = dict(__import__("os").environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=0")
+    for iters, seeds in ((2000, small), (60, large)):
+        r = subprocess.run([str(exe), str(iters), *seeds], capture_output=True, text=True, timeout=600, env=env)
+        assert r.returncode == 0, r.stdout + r.stderr[-3000:]
+        assert "decoded" in r.stdout
