@@ -108,7 +108,8 @@ int mg_select_palette(const int* widths, const int* heights, int n, float target
 /* Width and height of the PNG file data[0..n). */
 int mg_png_info(const uint8_t* data, size_t n, int* w, int* h);
 /* Decodes into out: h rows of `stride` bytes (>= 3*w), e.g. pinned memory from
- * mg_host_alloc that mg_generate then reads in place. */
+ * mg_host_alloc that mg_generate then reads in place.  On failure the
+ * contents of out are unspecified. */
 int mg_png_decode(const uint8_t* data, size_t n, uint8_t* out, int64_t stride);
 /* `count` files on up to `threads` host threads (<= 0: one per hardware
  * thread); status (nullable) receives each file's code; returns the first
