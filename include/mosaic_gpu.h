@@ -153,6 +153,19 @@ int mg_nearest_n(mg_ctx* ctx, const float* palette_lab, int p, const float* quer
 #define MG_NEAREST_GRID 2
 int mg_ctx_set_nearest_method(mg_ctx* ctx, int method);
 
+/* How this context scores a candidate in the greedy placement:
+ * MG_SCORING_CLI (the default) as main.rs:335-418, squared Lab distance +
+ * adjacency penalty; MG_SCORING_GUI as the GUI generator,
+ * gui/app_full.rs:1396-1470 find_best_tile_primary, Lab distance (its square
+ * root) + adjacency penalty.  Candidates, usage limits, the same-neighbour ban
+ * and the fallbacks are the same in both; the GUI's fixed 100 candidates are
+ * min(P, 100) like the CLI's, and its lack of colour adjustment is strength 0.
+ * Applies to mg_place_greedy and to mg_generate / mg_plan_create called
+ * afterwards; batches and the request loop score as the CLI. */
+#define MG_SCORING_CLI 0
+#define MG_SCORING_GUI 1
+int mg_ctx_set_scoring(mg_ctx* ctx, int scoring);
+
 /* ---- adjacency ------------------------------------------------------------------ */
 /* adjacency.rs:63-88 calculate_penalty for n (candidate, x, y) triples
  * (cxy: n*3 ints) against one grid; out: n floats (weighted). */

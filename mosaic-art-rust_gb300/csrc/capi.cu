@@ -62,7 +62,7 @@ struct mg_plan {
   int W = 0, H = 0, gw = 0, gh = 0, cw = 0, ch = 0, tw = 0, th = 0, N = 0, P = 0, K = 0, k = 0;
   int64_t iters = 0;
   float weight = 0, strength = 0, t0 = 100.0f, decay = 0.99995f;
-  int max_usage = 0, enable_opt = 0, build_sim = 0, device_thumbs = 0, run_sa = 0;
+  int max_usage = 0, enable_opt = 0, build_sim = 0, device_thumbs = 0, run_sa = 0, scoring = 0;
   uint64_t seed = 0;
   uint32_t stream_id = 0;
   std::vector<int> selected;
@@ -283,6 +283,13 @@ int mg_ctx_set_nearest_method(mg_ctx* ctx, int method) {
   if (method != MG_NEAREST_AUTO && method != MG_NEAREST_SCAN && method != MG_NEAREST_GRID)
     return fail(MG_ERR_ARG, "unknown nearest method");
   ctx->nearest_method = method;
+  return MG_OK;
+}
+
+int mg_ctx_set_scoring(mg_ctx* ctx, int scoring) {
+  if (!ctx) return fail(MG_ERR_ARG, "null context");
+  if (scoring != MG_SCORING_CLI && scoring != MG_SCORING_GUI) return fail(MG_ERR_ARG, "unknown scoring");
+  ctx->scoring = scoring;
   return MG_OK;
 }
 
@@ -563,6 +570,7 @@ int mg_place_greedy(mg_ctx* ctx, const float* palette_lab, int p, const float* c
   MG_CHECK(ctx->nn_index.build(ctx->in0.as<float4>(), p, ctx->nearest_method, k, ctx->stream));
   MG_CHECK(launch_nearest(ctx->in0.as<float4>(), p, ctx->in1.as<float4>(), n, k, ctx->out0.as<uint32_t>(),
                           ctx->out1.as<float>(), ctx->err.as<uint32_t>(), ctx->stream, 2048, &ctx->nn_index));
+  if (ctx->scoring == MG_SCORING_GUI) MG_CHECK(launch_sqrt_inplace(ctx->out1.as<float>(), (size_t)n * k, ctx->stream));
   int32_t* d_grid = ctx->out2.as<int32_t>();
   int* d_resets = reinterpret_cast<int*>(d_grid + n);
   GreedyJob job{ctx->out0.as<uint32_t>(), ctx->out1.as<float>(), d_grid, gw, gh, k,
@@ -825,6 +833,7 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r, bool zero_copy) {
   pl->seed = r->seed;
   pl->stream_id = r->stream;
   pl->build_sim = r->build_similarity;
+  pl->scoring = ctx->scoring;
   // palette selection (main.rs:166-261)
   pl->selected.assign(std::max(r->n_materials, 1), 0);
   const float target_aspect = (float)r->target_w / (float)r->target_h;
@@ -1035,6 +1044,8 @@ int plan_run(mg_plan* pl) {
     MG_CHECK(pl->index.build(pl->pal_lab.as<float4>(), P, ctx->nearest_method, pl->k, s));
     MG_CHECK(launch_nearest(pl->pal_lab.as<float4>(), P, pl->cell_lab.as<float4>(), N, pl->k, pl->cand_idx.as<uint32_t>(),
                             pl->cand_dist.as<float>(), pl->err.as<uint32_t>(), s, 2048, &pl->index));
+    if (pl->scoring == MG_SCORING_GUI)
+      MG_CHECK(launch_sqrt_inplace(pl->cand_dist.as<float>(), (size_t)N * pl->k, s));
   }
   MG_CUDA(cudaEventRecord(pl->ev[4], s));
   // [4] greedy placement

@@ -12,6 +12,7 @@ struct mg_ctx {
   mg::DevBuf in0, in1, in2, out0, out1, out2, sums, regions, err, lab_consts;
   mg_plan* gen_plan = nullptr;
   int nearest_method = mg::kNearestAuto;  // MG_NEAREST_*
+  int scoring = 0;                        // MG_SCORING_*
   mg::LabIndex nn_index;                  // grid of the last single-call palette
 };
 

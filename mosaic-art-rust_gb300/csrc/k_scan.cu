@@ -13,6 +13,8 @@
 //    (distance, index) order and ties go to the lowest index -- and appends keys
 //    below the current k-th best to a per-warp buffer.  A full buffer is
 //    bitonic-sorted and merged into the sorted top-k list (merge-path ranks).
+#include <algorithm>
+
 #include "mg_internal.h"
 #include "mg_ptx.cuh"
 #include "topk_warp.cuh"
@@ -180,6 +182,27 @@ int launch_nearest_t(const float4* pal, int p, const float4* queries, int nq, in
 }
 
 }  // namespace
+
+namespace {
+// The GUI generator's colour term (gui/app_full.rs:1435-1440): the square root
+// of each candidate's squared distance, correctly rounded like f32::sqrt.
+__global__ void __launch_bounds__(256) sqrt_inplace_kernel(float* __restrict__ v, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    v[i] = __fsqrt_rn(v[i]);
+}
+}  // namespace
+
+int launch_sqrt_inplace(float* v, size_t n, cudaStream_t stream) {
+  if (n == 0) return MG_OK;
+  int dev = 0, sms = 0;
+  MG_CUDA(cudaGetDevice(&dev));
+  MG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const size_t blocks = std::min<size_t>((n + 255) / 256, (size_t)sms * 8);
+  sqrt_inplace_kernel<<<(unsigned)blocks, 256, 0, stream>>>(v, n);
+  g_launches += 1;
+  MG_CUDA(cudaGetLastError());
+  return MG_OK;
+}
 
 int launch_nearest(const float4* pal, int p, const float4* queries, int nq, int k, uint32_t* idx, float* dist,
                    uint32_t* err, cudaStream_t stream, int chunk, const LabIndex* index) {

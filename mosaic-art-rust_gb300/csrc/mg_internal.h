@@ -85,6 +85,8 @@ struct LabIndex;
 int launch_nearest(const float4* pal, int p, const float4* queries, int nq, int k, uint32_t* idx,
                    float* dist, uint32_t* err, cudaStream_t stream, int chunk = 2048,
                    const LabIndex* index = nullptr);
+// v[i] = sqrt(v[i]) for i < n (the GUI generator's colour term over candidate distances).
+int launch_sqrt_inplace(float* v, size_t n, cudaStream_t stream);
 
 // (b) the same search through a bucket grid over the palette's Lab colours
 // (k_nearest_grid.cu): identical results, far fewer distances for P >> k.

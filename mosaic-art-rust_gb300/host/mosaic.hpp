@@ -94,6 +94,9 @@ class Context {
   void sync() { detail::check(mg_ctx_sync(h_)); }
   // How k-nearest queries search (MG_NEAREST_AUTO / _SCAN / _GRID; identical results).
   void set_nearest_method(int method) { detail::check(mg_ctx_set_nearest_method(h_, method)); }
+  // How the greedy placement scores candidates: MG_SCORING_CLI (main.rs:335-418)
+  // or MG_SCORING_GUI (gui/app_full.rs:1396-1470, the GUI generator).
+  void set_scoring(int scoring) { detail::check(mg_ctx_set_scoring(h_, scoring)); }
 
  private:
   mg_ctx* h_ = nullptr;

@@ -17,6 +17,7 @@ from .build import BUILD
 MG_OK, MG_ERR_ARG, MG_ERR_OOM, MG_ERR_CUDA, MG_ERR_TIMEOUT, MG_ERR_BUDGET, MG_ERR_STATE = range(7)
 MG_SIM_FULL, MG_SIM_TRIANGULAR = 0, 1
 MG_NEAREST_AUTO, MG_NEAREST_SCAN, MG_NEAREST_GRID = 0, 1, 2
+MG_SCORING_CLI, MG_SCORING_GUI = 0, 1
 
 _u8p = C.POINTER(C.c_uint8)
 _f32p = C.POINTER(C.c_float)
@@ -130,6 +131,7 @@ SIGNATURES = [
     ("mg_ctx_sync", C.c_int, [C.c_void_p]),
     ("mg_ctx_stream", C.c_void_p, [C.c_void_p]),
     ("mg_ctx_set_nearest_method", C.c_int, [C.c_void_p, C.c_int]),
+    ("mg_ctx_set_scoring", C.c_int, [C.c_void_p, C.c_int]),
     ("mg_host_alloc", C.c_void_p, [C.c_size_t]),
     ("mg_host_free", None, [C.c_void_p]),
     ("mg_average_lab", C.c_int, [C.c_void_p, _u8p, C.c_int, C.c_int, C.c_int64, _f32p]),
@@ -282,6 +284,11 @@ class Context:
     def set_nearest_method(self, method: int) -> None:
         """MG_NEAREST_AUTO / MG_NEAREST_SCAN / MG_NEAREST_GRID (identical results)."""
         check(self.lib.mg_ctx_set_nearest_method(self.h, method))
+
+    def set_scoring(self, scoring: int) -> None:
+        """MG_SCORING_CLI (squared distance + penalty, main.rs) or MG_SCORING_GUI
+        (distance + penalty, gui/app_full.rs) for the greedy placement."""
+        check(self.lib.mg_ctx_set_scoring(self.h, scoring))
 
     def nearest_n(self, pal, queries, k: int):
         pal, q = _lab3(pal), _lab3(queries)

@@ -26,7 +26,8 @@ class OracleJob(C.Structure):
                 ("gw", C.c_int), ("gh", C.c_int), ("max_materials", C.c_int), ("aspect_tol", C.c_float),
                 ("max_usage", C.c_int), ("weight", C.c_float), ("color_strength", C.c_float),
                 ("enable_opt", C.c_int), ("iters", C.c_long), ("t0", C.c_float), ("decay", C.c_float),
-                ("chains", C.c_int), ("seed", C.c_uint64), ("stream", C.c_uint32), ("threads", C.c_int)]
+                ("chains", C.c_int), ("seed", C.c_uint64), ("stream", C.c_uint32), ("threads", C.c_int),
+                ("gui_scoring", C.c_int)]
 
 
 class OracleOut(C.Structure):
@@ -242,8 +243,9 @@ def composite(grid, thumbs, cell_rgb, thumb_rgb, strength):
     return out
 
 
-def generate(inp, threads: int = 1, want_image: bool = True, stream: int = 0):
-    """Run the whole job on the CPU from mosaic_gpu.job.Inputs (Philox stream id `stream`)."""
+def generate(inp, threads: int = 1, want_image: bool = True, stream: int = 0, gui: bool = False):
+    """Run the whole job on the CPU from mosaic_gpu.job.Inputs (Philox stream id
+    `stream`; gui: the GUI generator's greedy scoring)."""
     cfg = inp.cfg
     tw, th = inp.tile
     n = len(inp.mats)
@@ -265,6 +267,7 @@ def generate(inp, threads: int = 1, want_image: bool = True, stream: int = 0):
     job.enable_opt = 1 if cfg.enable_optimization else 0
     job.iters, job.t0, job.decay = cfg.iterations, 100.0, 0.99995
     job.chains, job.seed, job.stream, job.threads = cfg.chains, cfg.seed, stream, threads
+    job.gui_scoring = 1 if gui else 0
     N = cfg.grid_w * cfg.grid_h
     grid = np.zeros(N, np.int32)
     image = np.zeros((cfg.grid_h * th, cfg.grid_w * tw, 3), np.uint8) if want_image else None

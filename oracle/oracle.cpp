@@ -772,7 +772,8 @@ int orc_generate(const orc_job* J, orc_out* O) {
   });
   std::vector<int32_t> grid(N);
   int resets = 0;
-  orc_place_greedy(pal.data(), P, cell_lab.data(), J->gw, J->gh, J->max_usage, J->weight, grid.data(), &resets);
+  place_greedy(pal.data(), P, cell_lab.data(), J->gw, J->gh, J->max_usage, J->weight, J->gui_scoring != 0, grid.data(),
+               &resets);
   if (O->greedy_grid) std::memcpy(O->greedy_grid, grid.data(), sizeof(int32_t) * N);
 
   std::vector<int32_t> final_grid = grid;

@@ -93,6 +93,7 @@ typedef struct orc_job {
   int max_usage; float weight; float color_strength;
   int enable_opt; long iters; float t0, decay; int chains; uint64_t seed; uint32_t stream;
   int threads;
+  int gui_scoring;  /* 1: the GUI generator's scoring (orc_place_greedy_gui) */
 } orc_job;
 
 typedef struct orc_out {

@@ -192,3 +192,30 @@ def test_generate_from_png_files(ctx):
         assert np.array_equal(capi.png_decode(capi.png_encode(image)), image)
     finally:
         lib.mg_host_free(addr)
+
+
+def test_generate_gui_scoring(ctx, orc):
+    """A whole job under the GUI generator's scoring (mg_ctx_set_scoring) against
+    the oracle's GUI job: grid, chains and image; the CLI scoring gives a
+    different mosaic here (weight 2), and the context returns to it after."""
+    from mosaic_gpu import _capi as capi
+    from mosaic_gpu import job
+
+    cfg = _small("recommended", target_w=480, target_h=360, n_materials=150, material_side=32, grid_w=20, grid_h=15,
+                 tile_w=12, tile_h=12, iterations=500, chains=4, weight=2.0)
+    inp = job.make_inputs(cfg)
+    ctx.set_scoring(capi.MG_SCORING_GUI)
+    try:
+        res, grid, image = job.generate(ctx, job.RequestHolder(inp))
+    finally:
+        ctx.set_scoring(capi.MG_SCORING_CLI)
+    ref = orc.generate(inp, threads=8, gui=True)
+    assert res.palette_size == ref["p"] and res.n_resets == ref["n_resets"]
+    assert np.array_equal(grid, ref["grid"])
+    assert int(np.abs(image.astype(np.int16) - ref["image"].astype(np.int16)).max(initial=0)) <= 1
+    assert res.best_chain == ref["best_chain"]
+    assert np.float32(res.final_cost) == np.float32(ref["final_cost"])
+    cli_res, cli_grid, _ = job.generate(ctx, job.RequestHolder(inp))
+    assert np.array_equal(cli_grid, orc.generate(inp, threads=8, want_image=False)["grid"])
+    assert not np.array_equal(cli_grid, grid)
+

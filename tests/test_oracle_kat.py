@@ -372,3 +372,17 @@ def test_gui_penalty_changes_choices(orc):
     a, _ = orc.place_greedy(lab, cells, 20, 20, 4, 100.0)
     b, _ = orc.place_greedy(lab, cells, 20, 20, 4, 100.0, gui=True)
     assert np.all(b >= 0) and not np.array_equal(a, b)
+
+
+def test_gui_scoring_through_the_whole_job(orc):
+    """orc_generate with the GUI's scoring: at weight 0 the same mosaic as the
+    CLI's; at weight 2 the two part (the GPU tests compare each with the device)."""
+    from mosaic_gpu import job
+
+    for weight, same in [(0.0, True), (2.0, False)]:
+        cfg = job.scaled(job.WORKLOADS["recommended"], target_w=240, target_h=180, n_materials=150, material_side=32,
+                         grid_w=20, grid_h=15, tile_w=8, tile_h=8, iterations=200, chains=2, weight=weight)
+        inp = job.make_inputs(cfg)
+        a = orc.generate(inp, threads=4, gui=True)
+        b = orc.generate(inp, threads=4)
+        assert np.array_equal(a["greedy_grid"], b["greedy_grid"]) == same
