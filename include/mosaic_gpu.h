@@ -160,8 +160,8 @@ int mg_ctx_set_nearest_method(mg_ctx* ctx, int method);
  * root) + adjacency penalty.  Candidates, usage limits, the same-neighbour ban
  * and the fallbacks are the same in both; the GUI's fixed 100 candidates are
  * min(P, 100) like the CLI's, and its lack of colour adjustment is strength 0.
- * Applies to mg_place_greedy and to mg_generate / mg_plan_create called
- * afterwards; batches and the request loop score as the CLI. */
+ * Applies to mg_place_greedy, and to plans, mg_generate calls, batches and
+ * servers set up on the context afterwards. */
 #define MG_SCORING_CLI 0
 #define MG_SCORING_GUI 1
 int mg_ctx_set_scoring(mg_ctx* ctx, int scoring);

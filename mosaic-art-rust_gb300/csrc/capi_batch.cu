@@ -49,6 +49,7 @@ struct mg_batch {
   int n_wide = 0, wide_gw = 0, wide_cells = 0, narrow_gw = 0, narrow_cells = 0;
   // tuned launch shapes
   int cells_warps = 8, nn_chunk = 2048;
+  int scoring = 0;  // MG_SCORING_* of the context when the batch was set up
   bool tuned = false;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -155,6 +156,7 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
   if (!pal || (n > 0 && !ms) || n < 0) return fail(MG_ERR_ARG, "invalid batch");
   b->ctx = ctx;
   b->device = ctx->device;
+  b->scoring = ctx->scoring;
   b->pal = pal;
   b->n = n;
   const int tw = pal->tw, th = pal->th, k = std::max(pal->k, 1);
@@ -367,6 +369,8 @@ int batch_enqueue(mg_batch* b, bool with_events) {
     MG_CHECK(launch_nearest(pal->pal_lab.as<float4>(), P, b->cell_lab.as<float4>(), b->total_cells, k,
                             b->cand_idx.as<uint32_t>(), b->cand_dist.as<float>(), b->err.as<uint32_t>(), s, b->nn_chunk,
                             &pal->index));
+  if (P > 0 && b->scoring == MG_SCORING_GUI)
+    MG_CHECK(launch_sqrt_inplace(b->cand_dist.as<float>(), (size_t)b->total_cells * k, s));
   if (with_events) MG_CUDA(record(b, b->ev[2], s));
   if (P > 0) {
     // every greedy walk: rows of >= 8 cells by the scouted walk, the rest one

@@ -209,6 +209,7 @@ int mg_server_create(mg_ctx* ctx, mg_palette* pal, const mg_server_config* cfg, 
   S->slots.resize(cfg->slots);
   for (auto& sl : S->slots) {
     int st = mg_ctx_create(ctx->device, &sl.ctx);
+    if (st == MG_OK) sl.ctx->scoring = ctx->scoring;  // the creator's greedy scoring
     if (st == MG_OK && cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess) st = MG_ERR_CUDA;
     if (st != MG_OK) {
       mg_server_destroy(S);
