@@ -189,6 +189,31 @@ def cpu_baseline(inp, seconds: float = 10.0):
                       f"path; material Lab and chains across {cores} threads, cells and greedy walk sequential"}
 
 
+def file_ends(target: np.ndarray):
+    """The path's file ends on this machine's host cores, beside the step (not
+    part of `value` or `e2e`): the workload's target encoded as PNG (level 1,
+    all threads) and decoded back (best of three), with the round trip checked."""
+    try:
+        import numpy as np
+
+        from mosaic_gpu import _capi as capi
+
+        t0 = time.perf_counter()
+        data = capi.png_encode(target, level=1, threads=0)
+        enc_ms = 1000 * (time.perf_counter() - t0)
+        out = np.empty((target.shape[0], target.shape[1], 3), np.uint8)
+        dec_ms = float("inf")
+        for _ in range(3):
+            t0 = time.perf_counter()
+            capi.png_decode(data, out)
+            dec_ms = min(dec_ms, 1000 * (time.perf_counter() - t0))
+        return {"what": "PNG encode (level 1, all host threads) and decode of the target", "png_bytes": len(data),
+                "pixels_bytes": int(target.nbytes), "encode_ms": round(enc_ms, 2), "decode_ms": round(dec_ms, 2),
+                "round_trip_exact": bool(np.array_equal(out, target)), "host_threads": os.cpu_count()}
+    except Exception as e:  # a supplementary figure never costs the bench line
+        return {"error": str(e)[:200]}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -356,6 +381,8 @@ def run_ours(args, rank, world, local):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(inp)
+    if rank == 0 and world == 1:
+        line["file_ends"] = file_ends(inp.target)
     if rank == 0:
         print(json.dumps(line), flush=True)
     plan.close()
