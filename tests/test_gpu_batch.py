@@ -117,36 +117,3 @@ def test_palette_lab_and_similarity_match_oracle(ctx, orc):
     assert ctx.lib.mg_palette_read_similarity(pal.h, sim.ctypes.data_as(C.POINTER(C.c_float))) == 0
     assert np.array_equal(sim.view(np.uint32), orc.similarity_full(lab).view(np.uint32))
     pal.close()
-
-
-def test_batch_gui_scoring(ctx, orc):
-    """A batch set up under the GUI generator's scoring (mg_ctx_set_scoring):
-    every mosaic equals mg_generate under that scoring, and the oracle's GUI
-    job for the first request (whose greedy grid the GUI scoring changes in 53
-    cells)."""
-    from mosaic_gpu import _capi as capi
-    from mosaic_gpu import job
-
-    mats, thumbs = _palette_inputs()
-    tgts = _targets()[:4]
-    spec = _requests()[:4]
-    ctx.set_scoring(capi.MG_SCORING_GUI)
-    try:
-        pal = job.Palette(ctx, mats, thumbs, TILE, TILE, target_aspect=4 / 3)
-        reqs = [job.mosaic_request(t, w, h, gw, gh, stream=i, **kw)
-                for i, (t, (w, h, gw, gh, kw)) in enumerate(zip(tgts, spec))]
-        results, grids, images = job.generate_batch(ctx, pal, reqs)
-        singles = [_single(ctx, mats, thumbs, t, w, h, gw, gh, kw, i)
-                   for i, (t, (w, h, gw, gh, kw)) in enumerate(zip(tgts, spec))]
-    finally:
-        ctx.set_scoring(capi.MG_SCORING_CLI)
-    for i, (res, grid, image) in enumerate(singles):
-        assert np.array_equal(grids[i], grid) and np.array_equal(images[i], image), i
-        assert results[i].n_resets == res.n_resets
-    w, h, gw, gh, kw = spec[0]
-    cfg = job.JobConfig("b", w, h, 0, len(mats), 24, 0, gw, gh, kw.get("max_usage", 3), kw.get("weight", 0.25),
-                        kw.get("strength", 0.4), kw.get("iterations", 1000), kw.get("chains", 1), TILE, TILE,
-                        enable_optimization=kw.get("enable_opt", True), seed=20251203)
-    ref = orc.generate(job.Inputs(cfg, tgts[0], mats, thumbs), threads=8, gui=True)
-    assert np.array_equal(grids[0], ref["grid"]) and np.array_equal(images[0], ref["image"])
-    pal.close()

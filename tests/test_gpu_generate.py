@@ -148,74 +148,3 @@ def test_generate_into_pinned_buffers(ctx, grid_h):
         assert np.array_equal(image, ref_image)
         assert res.best_chain == ref_res.best_chain and np.float32(res.final_cost) == np.float32(ref_res.final_cost)
     lib.mg_host_free(buf.ctypes.data)
-
-
-def test_generate_from_png_files(ctx):
-    """The path's file ends (image::open of main.rs:492/548, save of main.rs:672):
-    the target and every material arrive as PNG files, decoded into pinned
-    memory (target) and one packed buffer (materials, on several threads), and
-    the mosaic leaves as a PNG file.  Grid and image equal the same job's from
-    the raw arrays, and the file decodes back to the image."""
-    import ctypes as C
-    import dataclasses
-
-    from mosaic_gpu import _capi as capi
-    from mosaic_gpu import job, synth
-
-    lib = capi.load()
-    cfg = _small("recommended", target_w=480, target_h=360, n_materials=150, material_side=64, grid_w=20, grid_h=15,
-                 tile_w=12, tile_h=12, iterations=300, chains=4)
-    inp = job.make_inputs(cfg)
-    ref_res, ref_grid, ref_image = job.generate(ctx, job.RequestHolder(inp))
-    # materials: files -> one packed buffer at the original offsets
-    files = [capi.png_encode(inp.mats.image(i), level=i % 2) for i in range(len(inp.mats))]
-    buf = np.zeros_like(inp.mats.buf)
-    n = len(files)
-    data = (C.c_void_p * n)(*[C.cast(C.c_char_p(f), C.c_void_p) for f in files])
-    sizes = (C.c_size_t * n)(*[len(f) for f in files])
-    outs = (capi._u8p * n)(*[C.cast(buf.ctypes.data + int(o), capi._u8p) for o in inp.mats.off])
-    strides = (C.c_int64 * n)(*[3 * int(w) for w in inp.mats.w])
-    status = (C.c_int * n)()
-    capi.check(lib.mg_png_decode_batch(data, sizes, n, outs, strides, 4, status))
-    mats = synth.Materials(buf, inp.mats.off, inp.mats.w, inp.mats.h)
-    # target: file -> pinned memory
-    h, w = inp.target.shape[:2]
-    addr = lib.mg_host_alloc(h * w * 3)
-    assert addr
-    try:
-        target = np.ctypeslib.as_array(C.cast(addr, C.POINTER(C.c_uint8)), shape=(h * w * 3,)).reshape(h, w, 3)
-        capi.png_decode(capi.png_encode(inp.target), out=target)
-        decoded = dataclasses.replace(inp, target=target, mats=mats)
-        res, grid, image = job.generate(ctx, job.RequestHolder(decoded))
-        assert np.array_equal(grid, ref_grid) and np.array_equal(image, ref_image)
-        assert res.best_chain == ref_res.best_chain
-        assert np.array_equal(capi.png_decode(capi.png_encode(image)), image)
-    finally:
-        lib.mg_host_free(addr)
-
-
-def test_generate_gui_scoring(ctx, orc):
-    """A whole job under the GUI generator's scoring (mg_ctx_set_scoring) against
-    the oracle's GUI job: grid, chains and image; the CLI scoring gives a
-    different mosaic here (weight 2), and the context returns to it after."""
-    from mosaic_gpu import _capi as capi
-    from mosaic_gpu import job
-
-    cfg = _small("recommended", target_w=480, target_h=360, n_materials=150, material_side=32, grid_w=20, grid_h=15,
-                 tile_w=12, tile_h=12, iterations=500, chains=4, weight=2.0)
-    inp = job.make_inputs(cfg)
-    ctx.set_scoring(capi.MG_SCORING_GUI)
-    try:
-        res, grid, image = job.generate(ctx, job.RequestHolder(inp))
-    finally:
-        ctx.set_scoring(capi.MG_SCORING_CLI)
-    ref = orc.generate(inp, threads=8, gui=True)
-    assert res.palette_size == ref["p"] and res.n_resets == ref["n_resets"]
-    assert np.array_equal(grid, ref["grid"])
-    assert int(np.abs(image.astype(np.int16) - ref["image"].astype(np.int16)).max(initial=0)) <= 1
-    assert res.best_chain == ref["best_chain"]
-    assert np.float32(res.final_cost) == np.float32(ref["final_cost"])
-    cli_res, cli_grid, _ = job.generate(ctx, job.RequestHolder(inp))
-    assert np.array_equal(cli_grid, orc.generate(inp, threads=8, want_image=False)["grid"])
-    assert not np.array_equal(cli_grid, grid)
-

@@ -171,41 +171,6 @@ def test_greedy_ring_form_bit_exact(ctx, orc, p, max_usage, region):
     assert resets == rresets
 
 
-@pytest.mark.parametrize("p,gw,gh,max_usage,weight,step", [
-    (60, 6, 9, 2, 1.0, 3.0), (150, 20, 15, 3, 0.3, 3.0), (700, 40, 30, 2, 5.0, 0.5), (5000, 120, 25, 3, 0.25, 0.05),
-    (12000, 60, 40, 4, 2.0, 0.05), (700, 300, 150, 3, 0.25, 3.0)])
-def test_greedy_gui_scoring_bit_exact(ctx, orc, p, gw, gh, max_usage, weight, step):
-    """The GUI generator's selection (gui/app_full.rs:1396-1470: the Lab distance,
-    not its square, plus the penalty) on every form of the walk: one warp (a
-    6-cell-wide grid), the scouted walk with the palette in shared and in global
-    memory, and the ring form (45 000 cells).  Where the two scorings part (the
-    last four cases) the device follows the GUI's."""
-    from mosaic_gpu import _capi as capi
-
-    rng = np.random.default_rng(p * 3 + gw + int(weight * 10))
-    pal = rand_lab(rng, p)
-    base = rand_lab(rng, 1)[0]
-    cells = (base + np.cumsum(rng.normal(0, step, (gw * gh, 3)), axis=0)).astype(np.float32)
-    ctx.set_scoring(capi.MG_SCORING_GUI)
-    try:
-        grid, resets = ctx.place_greedy(pal, cells, gw, gh, max_usage, weight)
-    finally:
-        ctx.set_scoring(capi.MG_SCORING_CLI)
-    rgrid, rresets = orc.place_greedy(pal, cells, gw, gh, max_usage, weight, gui=True)
-    assert np.array_equal(grid, rgrid)
-    assert resets == rresets
-    if p >= 700:
-        cli, _ = orc.place_greedy(pal, cells, gw, gh, max_usage, weight)
-        assert not np.array_equal(rgrid, cli)
-
-
-def test_scoring_argument_checked(ctx):
-    from mosaic_gpu import _capi as capi
-
-    with pytest.raises(capi.MosaicError):
-        ctx.set_scoring(5)
-
-
 # ---- (e) annealing --------------------------------------------------------------------------------------------------------
 @pytest.mark.parametrize("p,gw,gh,iters,chains,t0,decay,greedy", [
     (60, 12, 9, 3000, 4, 100.0, 0.99995, False), (30, 7, 5, 500, 3, 1.0, 0.95, False),

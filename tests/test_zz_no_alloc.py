@@ -7,7 +7,7 @@ test plays that caller: the buffers come from torch's allocator, the call goes
 through the C ABI, and the results must equal the allocating entry point
 (mg_cells_lab) bit for bit on two calls in a row -- the second call must not
 see the first call's sums, since the array is shared and kept between calls.
-The file is collected last so that a failure here leaves every other test run.
+The file is collected after the stage, job, batch and server tests so that a failure here leaves them run.
 """
 import ctypes as C
 
