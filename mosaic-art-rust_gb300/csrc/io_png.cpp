@@ -171,7 +171,50 @@ struct Huff {
   }
 };
 
-struct FixedCodes {
+// Literal/length lookups of kBits bits: an entry decodes one symbol, or two
+// literals whose codes together fit in kBits (two output bytes per lookup on
+// literal-heavy data).  Entry: bits 0-8 the (first) symbol, 9-16 the second
+// literal, 24-28 the bits consumed, 30-31 the symbol count (0: a code longer
+// than kBits, decoded by Huff).
+struct PairTable {
+  static constexpr int kBits = 11;
+  uint32_t e[1u << kBits];
+  void build(const Huff& h) {
+    std::memset(e, 0, sizeof(e));
+    uint32_t code = 0;
+    int idx = 0;
+    for (int len = 1; len <= 15; ++len) {
+      for (int j = 0; j < h.count[len]; ++j, ++idx, ++code) {
+        if (len > kBits) continue;
+        const uint32_t v = 1u << 30 | (uint32_t)len << 24 | h.sym[idx];
+        for (uint32_t f = reverse_bits(code, len); f < (1u << kBits); f += 1u << len) e[f] = v;
+      }
+      code <<= 1;
+    }
+    // Descending, so e[i >> l1] (<= i) still holds its single entry; the
+    // second code is known when its l2 bits lie within the kBits - l1 known ones.
+    for (uint32_t i = (1u << kBits); i-- > 0;) {
+      const uint32_t a = e[i];
+      const uint32_t s1 = a & 0x1FFu, l1 = (a >> 24) & 31u;
+      if ((a >> 30) != 1 || s1 >= 256 || l1 >= (uint32_t)kBits) continue;
+      const uint32_t b = e[i >> l1];
+      const uint32_t s2 = b & 0x1FFu, l2 = (b >> 24) & 31u;
+      if ((b >> 30) != 1 || s2 >= 256 || l1 + l2 > (uint32_t)kBits) continue;
+      e[i] = 2u << 30 | (l1 + l2) << 24 | s2 << 9 | s1;
+    }
+  }
+};
+
+// Whether two literal codes of h can fit in one PairTable lookup.
+bool pairs_possible(const Huff& h, const uint8_t* lens) {
+  int shortest = 16;
+  for (int i = 0; i < 256; ++i)
+    if (lens[i]) shortest = std::min(shortest, (int)lens[i]);
+  (void)h;
+  return 2 * shortest <= PairTable::kBits;
+}
+
+struct FixedCodes {  // literal codes of 8 and 9 bits: no pairs
   Huff lit, dist;
   FixedCodes() {
     uint8_t l[288];
@@ -274,6 +317,7 @@ bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Statu
   };
   size_t pos = 0;
   Huff dyn[2];
+  PairTable dyn_pairs;
   bool last = false;
   while (!last) {
     last = bits(1) != 0;
@@ -299,9 +343,11 @@ bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Statu
     }
     const Huff* lit;
     const Huff* dist;
+    const PairTable* pairs;
     if (type == 1) {
       lit = &fixed_codes().lit;
       dist = &fixed_codes().dist;
+      pairs = nullptr;
     } else if (type == 2) {
       const int hlit = (int)bits(5) + 257, hdist = (int)bits(5) + 1, hclen = (int)bits(4) + 4;
       if (hlit > 286 || hdist > 30) return st.bad(MG_ERR_ARG, "PNG image data: bad code counts");
@@ -338,6 +384,11 @@ bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Statu
         return st.bad(MG_ERR_ARG, "PNG image data: bad Huffman code");
       lit = &dyn[0];
       dist = &dyn[1];
+      pairs = nullptr;
+      if (pairs_possible(dyn[0], lens)) {
+        dyn_pairs.build(dyn[0]);
+        pairs = &dyn_pairs;
+      }
     } else {
       return st.bad(MG_ERR_ARG, "PNG image data: bad block type");
     }
@@ -348,7 +399,25 @@ bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Statu
         next_pub = pos + kPublish;
       }
       if (bitcnt < 48) refill();
-      const int s = decode(*lit);
+      const uint32_t pe = pairs ? pairs->e[bitbuf & ((1u << PairTable::kBits) - 1)] : 0u;
+      int s;
+      if ((pe >> 30) == 2 && want - pos >= 2) {
+        out[pos] = (uint8_t)pe;
+        out[pos + 1] = (uint8_t)(pe >> 9);
+        pos += 2;
+        const int len = (int)((pe >> 24) & 31u);
+        bitbuf >>= len;
+        bitcnt -= len;
+        continue;
+      }
+      if ((pe >> 30) == 1) {
+        s = (int)(pe & 0x1FFu);
+        const int len = (int)((pe >> 24) & 31u);
+        bitbuf >>= len;
+        bitcnt -= len;
+      } else {
+        s = decode(*lit);  // a code longer than the table, or a pair where one byte is left
+      }
       if (s < 256) {
         if (s < 0) return st.bad(MG_ERR_ARG, "PNG image data: bad literal/length code");
         if (pos >= want) return st.bad(MG_ERR_ARG, "PNG image data: more data than the image holds");

@@ -405,3 +405,16 @@ def test_fuzz_under_sanitizers(tmp_path):
         r = subprocess.run([str(exe), str(iters), *seeds], capture_output=True, text=True, timeout=600, env=env)
         assert r.returncode == 0, r.stdout + r.stderr[-3000:]
         assert "decoded" in r.stdout
+
+
+def test_literal_pairs_at_every_length(capi):
+    """Literal-only streams of short codes (two literals per table lookup),
+    ending on every parity of the output size, including one byte left when a
+    pair would be next."""
+    rng = np.random.default_rng(9)
+    for w in range(1, 12):
+        for h in (1, 2, 3, 7):
+            img = rng.integers(0, 3, (h, w, 3)).astype(np.uint32)  # few distinct bytes: 1-3 bit codes
+            for strategy in (zlib.Z_HUFFMAN_ONLY, zlib.Z_DEFAULT_STRATEGY):
+                data = write_png(img, 2, 8, rng, level=6, strategy=strategy)
+                assert np.array_equal(capi.png_decode(data), img.astype(np.uint8)), (w, h, strategy)
