@@ -205,12 +205,11 @@ struct PairTable {
   }
 };
 
-// Whether two literal codes of h can fit in one PairTable lookup.
-bool pairs_possible(const Huff& h, const uint8_t* lens) {
+// Whether two literal codes (lengths lens[0..255]) can fit in one PairTable lookup.
+bool pairs_possible(const uint8_t* lens) {
   int shortest = 16;
   for (int i = 0; i < 256; ++i)
     if (lens[i]) shortest = std::min(shortest, (int)lens[i]);
-  (void)h;
   return 2 * shortest <= PairTable::kBits;
 }
 
@@ -385,7 +384,7 @@ bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Statu
       lit = &dyn[0];
       dist = &dyn[1];
       pairs = nullptr;
-      if (pairs_possible(dyn[0], lens)) {
+      if (pairs_possible(lens)) {
         dyn_pairs.build(dyn[0]);
         pairs = &dyn_pairs;
       }
