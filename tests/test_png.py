@@ -347,6 +347,8 @@ def test_batch_decode(capi):
         else:
             assert c == capi.MG_OK and np.array_equal(g, img)
     assert "file 13" in capi.load().mg_last_error().decode()
+    again, codes0 = capi.png_decode_batch(files, threads=0)  # one thread per hardware thread
+    assert codes0 == codes and all(g is None or np.array_equal(g, a) for g, a in zip(again, got) if a is not None)
 
 
 @pytest.mark.parametrize("name", ["examples/mosaic.png", "docs/public/hero-image.png"])
