@@ -243,14 +243,19 @@ const FixedCodes& fixed_codes() {
 // and its extra bits (15 + 5 + 15 + 13).
 constexpr size_t kInflateSlack = 8;
 constexpr size_t kPublish = 1u << 16;
+// part: src is one independent piece of the deflate data (no zlib header, no
+// reference before its own output); decoding stops, without the Adler-32
+// check, at the first block boundary where `want` bytes are out.
 bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Status& st,
-                  std::atomic<size_t>* progress = nullptr) {
-  if (n < 6) return st.bad(MG_ERR_ARG, "PNG image data: zlib stream too short");
-  const unsigned cmf = src[0], flg = src[1];
-  if ((cmf & 0x0F) != 8 || (cmf >> 4) > 7 || ((cmf << 8) | flg) % 31 != 0)
-    return st.bad(MG_ERR_ARG, "PNG image data: bad zlib header");
-  if (flg & 0x20) return st.bad(MG_ERR_ARG, "PNG image data: preset dictionary");
-  const uint8_t* ip = src + 2;
+                  std::atomic<size_t>* progress = nullptr, bool part = false) {
+  if (!part) {
+    if (n < 6) return st.bad(MG_ERR_ARG, "PNG image data: zlib stream too short");
+    const unsigned cmf = src[0], flg = src[1];
+    if ((cmf & 0x0F) != 8 || (cmf >> 4) > 7 || ((cmf << 8) | flg) % 31 != 0)
+      return st.bad(MG_ERR_ARG, "PNG image data: bad zlib header");
+    if (flg & 0x20) return st.bad(MG_ERR_ARG, "PNG image data: preset dictionary");
+  }
+  const uint8_t* ip = part ? src : src + 2;
   const uint8_t* const iend = src + n;
   uint64_t bitbuf = 0;
   int bitcnt = 0;
@@ -318,7 +323,7 @@ bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Statu
   Huff dyn[2];
   PairTable dyn_pairs;
   bool last = false;
-  while (!last) {
+  while (!last && !(part && pos == want)) {
     last = bits(1) != 0;
     const uint32_t type = bits(2);
     if (type == 0) {
@@ -449,6 +454,7 @@ bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Statu
     if (progress) progress->store(pos, std::memory_order_release);
   }
   if (pos != want) return st.bad(MG_ERR_ARG, "PNG image data: less data than the image holds");
+  if (part) return true;
   {
     const int drop = bitcnt & 7;
     bitbuf >>= drop;
@@ -458,6 +464,25 @@ bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Statu
   if (overrun()) return st.bad(MG_ERR_ARG, "PNG image data: truncated");
   if (a != adler32(1, out, want)) return st.bad(MG_ERR_ARG, "PNG image data: Adler-32 mismatch");
   return true;
+}
+
+// fn(0..n-1) on up to `threads` threads (<= 0: one per hardware thread).
+template <typename F>
+void parallel_for(size_t n, int threads, F&& fn) {
+  if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int t = (int)std::max<size_t>(1, std::min<size_t>(n, (size_t)threads));
+  if (t <= 1) {
+    for (size_t i = 0; i < n; ++i) fn(i);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  auto work = [&]() {
+    for (size_t i; (i = next.fetch_add(1)) < n;) fn(i);
+  };
+  std::vector<std::thread> pool;
+  for (int k = 1; k < t; ++k) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
 }
 
 // ---- PNG decode -------------------------------------------------------------------------
@@ -634,6 +659,44 @@ void row_to_rgb(const Header& H, const uint8_t* x, uint32_t width, const uint8_t
 
 constexpr size_t kPipelineMin = 1u << 20;  // inflated bytes below which one thread does everything
 
+// Files this library writes carry a private chunk "mgIX" (ancillary, unsafe to
+// copy, so an editor that rewrites the image data drops it): the count of
+// independent deflate parts, then per part its offset in the zlib stream and
+// in the inflated data (big-endian u32, then u64 pairs).  Parts share no
+// back-references, so they inflate on all threads; any inconsistency, or a
+// part that fails, leaves the serial inflate to decide.
+bool inflate_indexed(const std::vector<uint8_t>& z, const uint8_t* idx, size_t idx_len, uint8_t* raw, size_t total) {
+  if (idx_len < 4 || z.size() < 6) return false;
+  const size_t count = be32(idx);
+  if (count == 0 || count > (idx_len - 4) / 16 || idx_len != 4 + 16 * count) return false;
+  std::vector<size_t> zo(count + 1), ro(count + 1);
+  for (size_t i = 0; i < count; ++i) {
+    const uint8_t* q = idx + 4 + 16 * i;
+    zo[i] = (size_t)((uint64_t)be32(q) << 32 | be32(q + 4));
+    ro[i] = (size_t)((uint64_t)be32(q + 8) << 32 | be32(q + 12));
+  }
+  zo[count] = z.size() - 4;  // the Adler-32 follows the last part
+  ro[count] = total;
+  if (zo[0] != 2 || ro[0] != 0) return false;
+  for (size_t i = 0; i < count; ++i)
+    if (zo[i + 1] <= zo[i] || ro[i + 1] <= ro[i] || zo[i + 1] > z.size() - 4 || ro[i + 1] > total) return false;
+  std::vector<uint32_t> adl(count);
+  std::atomic<bool> ok{true};
+  parallel_for(count, 0, [&](size_t i) {
+    Status st;
+    if (!ok.load(std::memory_order_relaxed)) return;
+    if (!inflate_zlib(z.data() + zo[i], zo[i + 1] - zo[i], raw + ro[i], ro[i + 1] - ro[i], st, nullptr, true)) {
+      ok.store(false);
+      return;
+    }
+    adl[i] = adler32(1, raw + ro[i], ro[i + 1] - ro[i]);
+  });
+  if (!ok.load()) return false;
+  uint32_t a = adl[0];
+  for (size_t i = 1; i < count; ++i) a = adler32_combine(a, adl[i], ro[i + 1] - ro[i]);
+  return a == be32(z.data() + z.size() - 4);
+}
+
 int decode_png(const uint8_t* d, size_t n, uint8_t* out, int64_t stride, Status& st, bool pipelined) {
   Header H;
   if (!parse_header(d, n, H, st)) return st.code;
@@ -643,6 +706,8 @@ int decode_png(const uint8_t* d, size_t n, uint8_t* out, int64_t stride, Status&
   uint8_t plte[768];
   int plte_n = 0;
   bool seen_idat = false;
+  const uint8_t* index = nullptr;
+  size_t index_len = 0;
   size_t pos = 8;
   try {
     while (pos + 12 <= n) {
@@ -658,6 +723,9 @@ int decode_png(const uint8_t* d, size_t n, uint8_t* out, int64_t stride, Status&
         if (len % 3 != 0 || len > 768 || len == 0) return st.bad(MG_ERR_ARG, "PNG: bad PLTE length"), st.code;
         std::memcpy(plte, data, len);
         plte_n = (int)(len / 3);
+      } else if (!std::memcmp(type, "mgIX", 4)) {
+        index = data;
+        index_len = len;
       } else if (!std::memcmp(type, "IEND", 4)) {
         break;
       } else if (!(type[0] & 0x20) && std::memcmp(type, "IHDR", 4) != 0) {
@@ -701,7 +769,9 @@ int decode_png(const uint8_t* d, size_t n, uint8_t* out, int64_t stride, Status&
     auto run_inflate = [&]() {
       if (!inflate_zlib(z.data(), z.size(), raw.get(), total, ist, &progress)) inflate_failed.store(true);
     };
-    if (pipelined && total >= kPipelineMin) {
+    if (pipelined && total >= kPipelineMin && index && inflate_indexed(z, index, index_len, raw.get(), total)) {
+      progress.store(total);
+    } else if (pipelined && total >= kPipelineMin) {
       try {
         worker = std::thread(run_inflate);
       } catch (const std::exception&) {
@@ -968,25 +1038,6 @@ void filter_row(const uint8_t* cur, const uint8_t* prev, size_t rb, uint8_t* dst
   }
 }
 
-// fn(0..n-1) on up to `threads` threads (<= 0: one per hardware thread).
-template <typename F>
-void parallel_for(size_t n, int threads, F&& fn) {
-  if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
-  const int t = (int)std::max<size_t>(1, std::min<size_t>(n, (size_t)threads));
-  if (t <= 1) {
-    for (size_t i = 0; i < n; ++i) fn(i);
-    return;
-  }
-  std::atomic<size_t> next{0};
-  auto work = [&]() {
-    for (size_t i; (i = next.fetch_add(1)) < n;) fn(i);
-  };
-  std::vector<std::thread> pool;
-  for (int k = 1; k < t; ++k) pool.emplace_back(work);
-  work();
-  for (auto& th : pool) th.join();
-}
-
 constexpr size_t kPart = 65535;
 constexpr size_t kIdatMax = 1u << 20;
 
@@ -995,7 +1046,7 @@ size_t encode_bound(int w, int h) {
   const size_t raw = (size_t)h * (1 + 3 * (size_t)w);
   const size_t parts = (raw + kPart - 1) / kPart;
   const size_t z = 2 + raw + 5 * parts + 16 + 4;  // zlib header, stored worst case, Adler-32
-  return 8 + 25 + z + 12 * (z / kIdatMax + 1) + 12;
+  return 8 + 25 + (12 + 4 + 16 * parts) + z + 12 * (z / kIdatMax + 1) + 12;  // ... + the mgIX index
 }
 
 int encode_png(const uint8_t* rgb, int w, int h, int64_t stride, int level, int threads, uint8_t* out, size_t cap,
@@ -1047,6 +1098,23 @@ int encode_png(const uint8_t* rgb, int w, int h, int64_t stride, int level, int 
     o[20] = 0;  // no interlace
     put_be32(o + 21, crc32_update(0, o + 4, 17));
     o += 25;
+    {  // mgIX: where each independent part starts in the zlib stream and in the rows
+      const uint32_t ilen = (uint32_t)(4 + 16 * parts);
+      put_be32(o, ilen);
+      std::memcpy(o + 4, "mgIX", 4);
+      uint8_t* q = o + 8;
+      put_be32(q, (uint32_t)parts);
+      for (size_t i = 0; i < parts; ++i) {
+        uint8_t* e = q + 4 + 16 * i;
+        const uint64_t zoff = part_at[i], roff = (uint64_t)i * kPart;
+        put_be32(e, (uint32_t)(zoff >> 32));
+        put_be32(e + 4, (uint32_t)zoff);
+        put_be32(e + 8, (uint32_t)(roff >> 32));
+        put_be32(e + 12, (uint32_t)roff);
+      }
+      put_be32(o + 8 + ilen, crc32_update(0, o + 4, 4 + ilen));
+      o += 12 + ilen;
+    }
     const size_t chunks = (zlen + kIdatMax - 1) / kIdatMax;
     parallel_for(chunks, threads, [&](size_t c) {
       const size_t z0 = c * kIdatMax, clen = std::min(kIdatMax, zlen - z0);

@@ -365,10 +365,11 @@ def test_reference_example_images(capi, name):
     check_rows(data, rgb)
 
 
-def test_fuzz_under_sanitizers(tmp_path):
+def test_fuzz_under_sanitizers(tmp_path, capi):
     """Mutated files (tests/cpp/png_fuzz.cpp) against the decoder built with
     AddressSanitizer and UndefinedBehaviorSanitizer: small seeds of every
-    format, and large ones that take the two-thread pipeline."""
+    format, large ones that take the two-thread pipeline, and one written by
+    the library, whose part index takes the all-threads inflate."""
     import shutil
     import subprocess
 
@@ -402,6 +403,9 @@ def test_fuzz_under_sanitizers(tmp_path):
         p = tmp_path / f"l{i}.png"
         p.write_bytes(write_png(im, color, 8, rng, **kw))
         large.append(str(p))
+    p = tmp_path / "indexed.png"
+    p.write_bytes(capi.png_encode(img.astype(np.uint8), 1))
+    large.append(str(p))
     env = dict(__import__("os").environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=0")
     for iters, seeds in ((2000, small), (60, large)):
         r = subprocess.run([str(exe), str(iters), *seeds], capture_output=True, text=True, timeout=600, env=env)
@@ -420,3 +424,38 @@ def test_literal_pairs_at_every_length(capi):
             for strategy in (zlib.Z_HUFFMAN_ONLY, zlib.Z_DEFAULT_STRATEGY):
                 data = write_png(img, 2, 8, rng, level=6, strategy=strategy)
                 assert np.array_equal(capi.png_decode(data), img.astype(np.uint8)), (w, h, strategy)
+
+
+def _with_chunk_body(data: bytes, kind: bytes, fn) -> bytes:
+    """data with chunk `kind`'s body replaced by fn(body) (CRC recomputed)."""
+    pos, out = 8, bytearray(data[:8])
+    while pos < len(data):
+        (n,) = struct.unpack(">I", data[pos:pos + 4])
+        k, body = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
+        out += chunk(k, fn(body)) if k == kind else data[pos:pos + 12 + n]
+        pos += 12 + n
+    return bytes(out)
+
+
+def test_indexed_parts_decode_in_parallel_and_fall_back(capi):
+    """The library's files carry an index of independent deflate parts (mgIX)
+    that large ones inflate from on all threads; a damaged or misleading index
+    (offsets moved inside a part, a wrong count) leaves the serial inflate to
+    give the same image."""
+    y, x = np.mgrid[0:700, 0:900]
+    img = np.stack([(x * 3) % 256, (y * 5) % 256, (x ^ y) % 256], -1).astype(np.uint8)
+    for level in (0, 1):
+        data = capi.png_encode(img, level)
+        assert b"mgIX" in data
+        assert np.array_equal(capi.png_decode(data), img)
+
+        def shift(body, by=7):
+            b = bytearray(body)
+            off = struct.unpack(">Q", bytes(b[4 + 16:4 + 24]))[0]  # part 1's stream offset
+            b[4 + 16:4 + 24] = struct.pack(">Q", off + by)
+            return bytes(b)
+
+        for fn in (shift, lambda b: struct.pack(">I", 3) + b[4:], lambda b: b[:-16], lambda b: b"\x00" * len(b)):
+            bent = _with_chunk_body(data, b"mgIX", fn)
+            assert np.array_equal(capi.png_decode(bent), img)
+        check_rows(data, img)
