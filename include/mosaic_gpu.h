@@ -121,8 +121,11 @@ size_t mg_png_encode_bound(int w, int h);
 /* Encodes an RGB8 image as an 8-bit RGB PNG: per row the filter with the
  * smallest sum of absolute residuals; level 0 stores the rows uncompressed,
  * level 1 codes each 64 KB block with its own Huffman code (or stores it when
- * that is smaller).  out must hold mg_png_encode_bound(w, h) bytes (else
- * MG_ERR_ARG with *len = that bound); *len receives the file size. */
+ * that is smaller).  The blocks share no back-references and a private
+ * ancillary chunk ("mgIX", ignored by other readers) indexes them, so
+ * mg_png_decode inflates a large file of this library's on all threads.
+ * out must hold mg_png_encode_bound(w, h) bytes (else MG_ERR_ARG with
+ * *len = that bound); *len receives the file size. */
 int mg_png_encode(const uint8_t* rgb, int w, int h, int64_t stride, int level, int threads, uint8_t* out,
                   size_t cap, size_t* len);
 
