@@ -242,8 +242,9 @@ int mg_ctx_create(int device, mg_ctx** out) {
     delete c;
     return cuda_fail(e, "cudaStreamCreate");
   }
-  upload_lab_consts(c->stream);
-  int s = ensure_err(c);
+  const cudaError_t ue = upload_lab_consts(c->stream);
+  int s = ue == cudaSuccess ? MG_OK : cuda_fail(ue, "upload_lab_consts");
+  if (s == MG_OK) s = ensure_err(c);
   if (s == MG_OK) s = finish(c);
   if (s != MG_OK) {
     mg_ctx_destroy(c);

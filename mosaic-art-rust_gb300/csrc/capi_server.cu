@@ -217,8 +217,13 @@ int mg_server_create(mg_ctx* ctx, mg_palette* pal, const mg_server_config* cfg, 
     }
     sl.batch = server_batch_new();
   }
-  S->dispatcher = std::thread(dispatch_loop, S);
-  S->completer = std::thread(complete_loop, S);
+  try {
+    S->dispatcher = std::thread(dispatch_loop, S);
+    S->completer = std::thread(complete_loop, S);
+  } catch (const std::exception&) {
+    mg_server_destroy(S);  // nothing submitted yet: stops and joins whichever thread started
+    return fail(MG_ERR_OOM, "cannot start the server's dispatcher and completion threads");
+  }
   *out = S;
   return MG_OK;
 }

@@ -244,10 +244,15 @@ const FixedCodes& fixed_codes() {
 constexpr size_t kInflateSlack = 8;
 constexpr size_t kPublish = 1u << 16;
 // part: src is one independent piece of the deflate data (no zlib header, no
-// reference before its own output); decoding stops, without the Adler-32
-// check, at the first block boundary where `want` bytes are out.
+// reference before its own output), inflated without the Adler-32 check into
+// out[0, want) while other threads write the neighbouring parts, so nothing
+// is written past `want`.  The piece must decode to exactly `want` bytes and
+// end exactly at src + n on a byte boundary; only the final piece carries
+// BFINAL.  Anything else fails, and the caller falls back to the serial
+// inflate of the whole stream.
+enum PartKind { kWhole = 0, kInnerPart = 1, kFinalPart = 2 };
 bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Status& st,
-                  std::atomic<size_t>* progress = nullptr, bool part = false) {
+                  std::atomic<size_t>* progress = nullptr, PartKind part = kWhole) {
   if (!part) {
     if (n < 6) return st.bad(MG_ERR_ARG, "PNG image data: zlib stream too short");
     const unsigned cmf = src[0], flg = src[1];
@@ -294,6 +299,8 @@ bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Statu
   };
   // more bits consumed than the input held
   auto overrun = [&]() { return (size_t)(bitcnt / 8) < phantom; };
+  // all of [src, src + n) consumed, on a byte boundary
+  auto at_end = [&]() { return 8 * ((size_t)(ip - src) + phantom) - (size_t)bitcnt == 8 * n; };
   // next symbol of h (>= 15 buffered bits), -1 on a code outside the set
   auto decode = [&](const Huff& h) -> int {
     const uint16_t e = h.fast[bitbuf & ((1u << Huff::kFast) - 1)];
@@ -323,7 +330,7 @@ bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Statu
   Huff dyn[2];
   PairTable dyn_pairs;
   bool last = false;
-  while (!last && !(part && pos == want)) {
+  while (!last && !(part && pos == want && at_end())) {
     last = bits(1) != 0;
     const uint32_t type = bits(2);
     if (type == 0) {
@@ -438,10 +445,12 @@ bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Statu
       if (len > want - pos) return st.bad(MG_ERR_ARG, "PNG image data: more data than the image holds");
       uint8_t* o = out + pos;
       const uint8_t* from = o - d;
-      if (d >= 8) {
+      if (d >= 8 && (!part || want - pos >= ((len + 7) & ~(size_t)7))) {
         // 8-byte steps, each reading bytes at least 8 behind what it writes;
-        // the last step may write up to 7 bytes past the match (the output
-        // buffer has kInflateSlack spare bytes, overwritten by what follows)
+        // the last step may write up to 7 bytes past the match (a whole
+        // stream's buffer has kInflateSlack spare bytes, overwritten by what
+        // follows; a part copies exactly near its end instead, as the bytes
+        // after it belong to the next part's thread)
         for (size_t k = 0; k < len; k += 8) std::memcpy(o + k, from + k, 8);
       } else if (d == 1) {
         std::memset(o, *from, len);
@@ -454,7 +463,14 @@ bool inflate_zlib(const uint8_t* src, size_t n, uint8_t* out, size_t want, Statu
     if (progress) progress->store(pos, std::memory_order_release);
   }
   if (pos != want) return st.bad(MG_ERR_ARG, "PNG image data: less data than the image holds");
-  if (part) return true;
+  if (part) {
+    if (last != (part == kFinalPart)) return st.bad(MG_ERR_ARG, "PNG image data: part ends on the wrong block");
+    const int drop = bitcnt & 7;
+    bitbuf >>= drop;
+    bitcnt -= drop;
+    if (overrun() || !at_end()) return st.bad(MG_ERR_ARG, "PNG image data: part does not end where indexed");
+    return true;
+  }
   {
     const int drop = bitcnt & 7;
     bitbuf >>= drop;
@@ -479,8 +495,18 @@ void parallel_for(size_t n, int threads, F&& fn) {
   auto work = [&]() {
     for (size_t i; (i = next.fetch_add(1)) < n;) fn(i);
   };
+  // Threads that cannot be created (a thread or process limit) leave their
+  // share to the ones running: work() takes items until none are left, so the
+  // calling thread alone still finishes everything.
   std::vector<std::thread> pool;
-  for (int k = 1; k < t; ++k) pool.emplace_back(work);
+  pool.reserve((size_t)t - 1);
+  for (int k = 1; k < t; ++k) {
+    try {
+      pool.emplace_back(work);
+    } catch (const std::exception&) {
+      break;
+    }
+  }
   work();
   for (auto& th : pool) th.join();
 }
@@ -685,7 +711,8 @@ bool inflate_indexed(const std::vector<uint8_t>& z, const uint8_t* idx, size_t i
   parallel_for(count, 0, [&](size_t i) {
     Status st;
     if (!ok.load(std::memory_order_relaxed)) return;
-    if (!inflate_zlib(z.data() + zo[i], zo[i + 1] - zo[i], raw + ro[i], ro[i + 1] - ro[i], st, nullptr, true)) {
+    if (!inflate_zlib(z.data() + zo[i], zo[i + 1] - zo[i], raw + ro[i], ro[i + 1] - ro[i], st, nullptr,
+                      i + 1 == count ? kFinalPart : kInnerPart)) {
       ok.store(false);
       return;
     }

@@ -238,9 +238,9 @@ const LabConsts& host_lab_consts() {
   return h.c;
 }
 
-void upload_lab_consts(cudaStream_t stream) {
+cudaError_t upload_lab_consts(cudaStream_t stream) {
   static HostLabConsts h;
-  cudaMemcpyToSymbolAsync(c_lab, &h.c, sizeof(LabConsts), 0, cudaMemcpyHostToDevice, stream);
+  return cudaMemcpyToSymbolAsync(c_lab, &h.c, sizeof(LabConsts), 0, cudaMemcpyHostToDevice, stream);
 }
 
 int launch_region_stats(const uint8_t* base, const CellGeom* geom, const Region* regions, int n_regions,
@@ -307,11 +307,13 @@ extern "C" int mg_cells_lab_noalloc(const uint8_t* d_img, int w, int h, int64_t 
   {
     // First call on a device: resolve the array's device address (the host-side
     // symbol is only a stand-in) and upload the Lab constants to that device.
+    // The address is kept only once both have succeeded, so a failed first
+    // call is retried in full by the next one.
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     if (!g_noalloc_ptr[dev]) {
       void* p = nullptr;
       MG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_sums));
-      upload_lab_consts(0);
+      MG_CUDA(upload_lab_consts(0));
       MG_CUDA(cudaDeviceSynchronize());
       g_noalloc_ptr[dev] = static_cast<RegionSums*>(p);
     }

@@ -67,7 +67,7 @@ struct CellGeom {
 int launch_region_stats(const uint8_t* base, const CellGeom* geom, const Region* regions, int n_regions,
                         int64_t max_region_px, float4* out_lab, uchar4* out_rgb, RegionSums* scratch,
                         int want_lab, cudaStream_t stream);
-void upload_lab_consts(cudaStream_t stream);
+cudaError_t upload_lab_consts(cudaStream_t stream);
 
 // Copy n items of `bytes` each from device-readable addresses src[i] to
 // dst + i*bytes (16-byte vector copies when aligned).

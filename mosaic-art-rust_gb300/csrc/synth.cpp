@@ -39,11 +39,21 @@ void parallel_rows(int n, int threads, F fn) {
     return;
   }
   threads = std::min(threads, n);
+  auto rows = [=, &fn](int t) {
+    for (int i = t; i < n; i += threads) fn(i);
+  };
+  // A thread that cannot be created (a thread or process limit) leaves its
+  // rows, and those of the threads after it, to the calling thread.
   std::vector<std::thread> pool;
-  for (int t = 0; t < threads; ++t)
-    pool.emplace_back([=, &fn]() {
-      for (int i = t; i < n; i += threads) fn(i);
-    });
+  int t = 0;
+  for (; t < threads; ++t) {
+    try {
+      pool.emplace_back(rows, t);
+    } catch (const std::exception&) {
+      break;
+    }
+  }
+  for (; t < threads; ++t) rows(t);
   for (auto& th : pool) th.join();
 }
 

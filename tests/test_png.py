@@ -459,3 +459,100 @@ def test_indexed_parts_decode_in_parallel_and_fall_back(capi):
             bent = _with_chunk_body(data, b"mgIX", fn)
             assert np.array_equal(capi.png_decode(bent), img)
         check_rows(data, img)
+
+
+def _indexed_file(segments: list[bytes], w: int, h: int, parts: list[bytes]) -> bytes:
+    """An RGB8 PNG whose zlib stream is the given raw-deflate parts (one per
+    segment of the filtered data) with an mgIX index of where each starts."""
+    raw = b"".join(segments)
+    z = b"\x78\xda" + b"".join(parts) + struct.pack(">I", zlib.adler32(raw) & 0xFFFFFFFF)
+    idx, zo, ro = struct.pack(">I", len(parts)), 2, 0
+    for seg, part in zip(segments, parts):
+        idx += struct.pack(">QQ", zo, ro)
+        zo, ro = zo + len(part), ro + len(seg)
+    return (SIG + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0)) + chunk(b"mgIX", idx) +
+            chunk(b"IDAT", z) + chunk(b"IEND", b""))
+
+
+def _runs_before_cuts(w: int, h: int, cuts: list[int], rng) -> bytes:
+    """Filtered RGB8 data (filter type None) whose bytes before each cut repeat a
+    13-byte pattern, so a deflate part ending at the cut ends in a long match at
+    distance 13."""
+    raw = bytearray(rng.integers(0, 256, h * (3 * w + 1)).astype(np.uint8).tobytes())
+    pat = bytes(rng.integers(0, 256, 13).astype(np.uint8))
+    for c in cuts:
+        raw[c - 700:c] = (pat * 60)[:700]
+    raw[::3 * w + 1] = bytes(h)  # filter bytes
+    return bytes(raw)
+
+
+def _pixels(raw: bytes, w: int, h: int) -> np.ndarray:
+    return np.frombuffer(raw, np.uint8).reshape(h, 3 * w + 1)[:, 1:].reshape(h, w, 3)
+
+
+def test_indexed_parts_ending_in_long_matches(capi):
+    """Each part of an indexed file (here compressed by zlib with a full flush
+    between parts, so parts share no back-references) ends in a long match at a
+    distance of at least 8.  The parts inflate on separate threads into
+    adjacent ranges of one buffer, so a part must not write past its own end:
+    the decoded image equals the serial decode of the same stream, every time."""
+    w, h = 700, 520
+    rng = np.random.default_rng(12)
+    total = h * (3 * w + 1)
+    cuts = list(range(65533, total, 65533))
+    raw = _runs_before_cuts(w, h, cuts, rng)
+    bounds = [0] + cuts + [total]
+    segments = [raw[a:b] for a, b in zip(bounds[:-1], bounds[1:])]
+    c = zlib.compressobj(9, zlib.DEFLATED, -15)
+    parts = [c.compress(s) + c.flush(zlib.Z_FULL_FLUSH) for s in segments[:-1]]
+    parts.append(c.compress(segments[-1]) + c.flush(zlib.Z_FINISH))
+    want = _pixels(raw, w, h)
+    data = _indexed_file(segments, w, h, parts)
+    serial = _with_chunk_body(data, b"mgIX", lambda b: b"\x00" * len(b))
+    assert np.array_equal(capi.png_decode(serial), want)
+    for _ in range(8):
+        assert np.array_equal(capi.png_decode(data), want)
+
+
+def _stored(seg: bytes, final: bool) -> bytes:
+    """seg as raw-deflate stored blocks (<= 65535 bytes each); the last block
+    carries BFINAL when `final`."""
+    out = bytearray()
+    for i in range(0, max(len(seg), 1), 65535):
+        piece = seg[i:i + 65535]
+        last = final and i + 65535 >= len(seg)
+        out += bytes([1 if last else 0]) + struct.pack("<HH", len(piece), len(piece) ^ 0xFFFF) + piece
+    return bytes(out)
+
+
+def test_indexed_parts_must_agree_with_the_serial_stream(capi):
+    """An index cannot make the decoder accept a stream that the serial inflate
+    rejects, nor decode one differently: a file whose inner part carries BFINAL
+    (the serial inflate stops there, short of the image) fails; with a part
+    boundary moved, the image is the same (through the serial inflate when a
+    part no longer ends exactly where the index says)."""
+    w, h = 700, 520
+    rng = np.random.default_rng(13)
+    total = h * (3 * w + 1)
+    raw = bytearray(rng.integers(0, 256, total).astype(np.uint8).tobytes())
+    raw[::3 * w + 1] = bytes(h)
+    raw = bytes(raw)
+    bounds = [0, 300000, 700000, total]
+    segments = [raw[a:b] for a, b in zip(bounds[:-1], bounds[1:])]
+    good = [_stored(s, i == len(segments) - 1) for i, s in enumerate(segments)]
+    assert np.array_equal(capi.png_decode(_indexed_file(segments, w, h, good)), _pixels(raw, w, h))
+    early_final = [_stored(s, i >= 1) for i, s in enumerate(segments)]
+    bad = _indexed_file(segments, w, h, early_final)
+    with pytest.raises(RuntimeError):
+        capi.png_decode(bad)
+
+    def move_part1(by):
+        return lambda b: b[:4 + 16] + struct.pack(">Q", struct.unpack(">Q", b[4 + 16:4 + 24])[0] + by) + b[4 + 24:]
+
+    # part 0 followed by an empty stored block: moved back over it, part 1
+    # starts with that block (the same stream either way); moved forward, part 0
+    # runs into part 1's data and the serial inflate decides
+    padded = [good[0] + b"\x00\x00\x00\xff\xff"] + good[1:]
+    data = _indexed_file(segments, w, h, padded)
+    for by in (-5, 5, 1):
+        assert np.array_equal(capi.png_decode(_with_chunk_body(data, b"mgIX", move_part1(by))), _pixels(raw, w, h))
