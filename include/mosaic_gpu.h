@@ -76,9 +76,10 @@ int mg_cells_lab(mg_ctx* ctx, const uint8_t* img, int w, int h, int64_t stride, 
  * device-accessible: d_img (stride bytes per row), d_lab4 (gw*gh x 4 floats:
  * L, a, b, 0; 16-byte aligned), d_rgb4 (nullable, gw*gh x 4 bytes: R, G, B, 0).
  * Work is queued on `stream` (a cudaStream_t, NULL = default stream) and no
- * memory is allocated: the per-cell sums live in a fixed device array the
- * library reserves on each GPU that loads it (1.5 MB), so at most 32768 cells
- * per call (MG_ERR_ARG beyond).  The first call on a device resolves that
+ * memory is allocated: a cell is reduced by one warp, or, from 8192 pixels
+ * per cell, by several warps whose partial sums meet in a fixed device array
+ * the library reserves on each GPU that loads it (1.5 MB), so at most 32768
+ * cells per call (MG_ERR_ARG beyond).  The first call on a device resolves that
  * array's address and uploads constants (it synchronises the device), so make
  * it before any stream capture.  All calls share the array: calls whose work
  * overlaps on the GPU (other streams, other threads) race and must be ordered

@@ -10,8 +10,8 @@
 // of the chain kernel (k_anneal.cu: one CTA per chain) and one best-chain
 // selection per mosaic.  Each walk and chain is the single-mosaic code, so
 // batched results equal the one-mosaic-per-launch results bit for bit.
-#include "mg_internal.h"
 #include "composite.cuh"
+#include "lab_reduce.cuh"
 
 namespace mg {
 namespace {
@@ -26,22 +26,41 @@ __device__ __forceinline__ int find_mosaic(const BatchMosaic* __restrict__ mos, 
   return lo;
 }
 
-// One warp per (padded) cell of any mosaic: exact fixed-point Lab sums and u32
-// RGB sums over the cell's pixels, reduced by shuffles.  Padding cells get 0.
+constexpr int kCellBaseSmem = 1024;  // mosaics whose first cells the cell kernel keeps in shared memory
+
+// One warp per (padded) cell of any mosaic: the cell's rows through
+// lab_reduce.cuh (exact fixed-point Lab and integer RGB sums, reduced by
+// shuffles), means written by lane 0.  Padding cells get 0.  Each CTA loads the
+// transfer table and (for batches of up to 1024 mosaics) the mosaics' first
+// cell indices into shared memory once, so finding a cell's mosaic is a
+// binary search on chip.
 template <int kWarps>
 __global__ void __launch_bounds__(32 * kWarps) batch_cells_kernel(const BatchMosaic* __restrict__ mos, int nm,
                                                                   int total_cells, const LabConsts* __restrict__ C,
                                                                   float4* __restrict__ lab_out,
                                                                   uchar4* __restrict__ rgb_out) {
   __shared__ float s_lut[256];
-  __shared__ float s_ms[9];
+  __shared__ int s_base[kCellBaseSmem];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) s_lut[i] = C->lut[i];
-  if (threadIdx.x < 9) s_ms[threadIdx.x] = C->ms[threadIdx.x];
+  const bool base_in_smem = nm <= kCellBaseSmem;
+  if (base_in_smem)
+    for (int i = threadIdx.x; i < nm; i += blockDim.x) s_base[i] = mos[i].cell_base;
   __syncthreads();
-  const float eps = C->eps, k1 = C->k1, k2 = C->k2;
+  const LabK K = make_lab_k(C->ms, C->eps, C->k1, C->k2);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int cell = blockIdx.x * kWarps + warp; cell < total_cells; cell += gridDim.x * kWarps) {
-    const int m = find_mosaic(mos, nm, cell);
+    int m;
+    if (base_in_smem) {
+      int lo = 0, hi = nm - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_base[mid] <= cell) lo = mid;
+        else hi = mid - 1;
+      }
+      m = lo;
+    } else {
+      m = find_mosaic(mos, nm, cell);
+    }
     const BatchMosaic& M = mos[m];
     const int local = cell - M.cell_base;
     if (local >= M.n) {
@@ -53,65 +72,14 @@ __global__ void __launch_bounds__(32 * kWarps) batch_cells_kernel(const BatchMos
     }
     const int cy = local / M.gw, cx = local - cy * M.gw;
     const uint8_t* base = M.target + (int64_t)cy * M.ch * M.stride + 3ll * cx * M.cw;
-    const int npx = M.cw * M.ch;
-    long long aL = 0, aA = 0, aB = 0;
-    unsigned sr = 0, sg = 0, sb = 0;
-    auto pixel = [&](uint32_t r8, uint32_t g8, uint32_t b8) {
-      sr += r8;
-      sg += g8;
-      sb += b8;
-      float L, A, B;
-      lab_pixel(s_lut, s_ms, eps, k1, k2, r8, g8, b8, L, A, B);
-      aL += lab_quant(L);
-      aA += lab_quant(A);
-      aB += lab_quant(B);
-    };
-    if ((M.cw & 3) == 0 && (M.stride & 3) == 0 && ((uintptr_t)base & 3) == 0) {
-      // four pixels of a cell row as three 32-bit words (exact integer sums: order-free)
-      const int gpr = M.cw >> 2, ng = gpr * M.ch;
-      int gx = lane % gpr, y = lane / gpr;
-      const int dgx = 32 % gpr, dgy = 32 / gpr;
-      for (int q = lane; q < ng; q += 32) {
-        const uint32_t* p = reinterpret_cast<const uint32_t*>(base + (int64_t)y * M.stride + 12 * gx);
-        const uint32_t w0 = p[0], w1 = p[1], w2 = p[2];
-        pixel(w0 & 0xFFu, (w0 >> 8) & 0xFFu, (w0 >> 16) & 0xFFu);
-        pixel(w0 >> 24, w1 & 0xFFu, (w1 >> 8) & 0xFFu);
-        pixel((w1 >> 16) & 0xFFu, w1 >> 24, w2 & 0xFFu);
-        pixel((w2 >> 8) & 0xFFu, (w2 >> 16) & 0xFFu, w2 >> 24);
-        gx += dgx;
-        y += dgy;
-        if (gx >= gpr) {
-          gx -= gpr;
-          ++y;
-        }
-      }
-    } else {
-      int x = lane % M.cw, y = lane / M.cw;
-      const int dx = 32 % M.cw, dy = 32 / M.cw;
-      for (int i = lane; i < npx; i += 32) {
-        const uint8_t* px = base + (int64_t)y * M.stride + 3 * x;
-        pixel(px[0], px[1], px[2]);
-        x += dx;
-        y += dy;
-        if (x >= M.cw) {
-          x -= M.cw;
-          ++y;
-        }
-      }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      aL += __shfl_xor_sync(0xffffffffu, aL, o);
-      aA += __shfl_xor_sync(0xffffffffu, aA, o);
-      aB += __shfl_xor_sync(0xffffffffu, aB, o);
-      sr += __shfl_xor_sync(0xffffffffu, sr, o);
-      sg += __shfl_xor_sync(0xffffffffu, sg, o);
-      sb += __shfl_xor_sync(0xffffffffu, sb, o);
-    }
+    LabAcc acc;
+    reduce_rows<true>(base, M.cw, M.stride, 0, M.ch, lane, s_lut, K, acc);
+    const LabSums t = warp_sums<true>(acc);
     if (lane == 0) {
-      lab_out[cell] = make_float4(lab_mean(aL, npx), lab_mean(aA, npx), lab_mean(aB, npx), 0.0f);
-      rgb_out[cell] = make_uchar4((unsigned char)(sr / (unsigned)npx), (unsigned char)(sg / (unsigned)npx),
-                                  (unsigned char)(sb / (unsigned)npx), 0);
+      const long long npx = (long long)M.cw * M.ch;
+      const unsigned long long n = (unsigned long long)npx;
+      lab_out[cell] = make_float4(lab_mean(t.L, npx), lab_mean(t.A, npx), lab_mean(t.B, npx), 0.0f);
+      rgb_out[cell] = make_uchar4((unsigned char)(t.R / n), (unsigned char)(t.G / n), (unsigned char)(t.Bc / n), 0);
     }
   }
 }

@@ -6,18 +6,18 @@
 // truncating division), main.rs:495-496 / 537-541 (cells of w/gw x h/gh at
 // (x*cw, y*ch), remainder ignored).
 //
-// Design: one CTA per (region, row chunk).  Each thread converts pixels to Lab
-// with the table-driven FP32 arithmetic of mg_math.h and accumulates the
-// fixed-point Lab (int64) and RGB (u32) in registers; warp shuffles and one
-// shared-memory pass reduce the CTA, and six 64-bit atomics add it to the
-// region's sums.  Integer sums are exact, so the result does not depend on the
-// CTA count or order.  A second tiny kernel divides.
+// Design: one warp per (region, chunk of rows); the per-pixel work is
+// lab_reduce.cuh (packed FP32x2 Lab of pixel pairs from 48-byte loads,
+// fixed-point sums).  A region that fits one unit (a target cell) is reduced
+// and divided by its warp; larger ones (materials) add each chunk's sums to
+// the region's with 64-bit atomics and a second tiny kernel divides.  Integer
+// sums are exact, so the result does not depend on the split.
 #include <cmath>
 #include <mutex>
 
 #include <algorithm>
 
-#include "mg_internal.h"
+#include "lab_reduce.cuh"
 
 namespace mg {
 
@@ -63,122 +63,70 @@ struct HostLabConsts {
 };
 
 constexpr int kStatThreads = 256;
+constexpr int kStatWarps = kStatThreads / 32;
+constexpr int64_t kUnitPx = 4096;  // pixels per warp unit when a region is split into row chunks
 
+// One warp per unit = (region, chunk of its rows).  With one chunk per region
+// the unit's warp writes the region's means itself; with several, it adds its
+// sums to the region's (zeroed) RegionSums with six 64-bit atomics and
+// region_finalize_kernel divides.  The CTA loads the transfer table once and
+// its warps take units round robin.
 template <bool kCells, bool kLab>
 __global__ void __launch_bounds__(kStatThreads) region_stats_kernel(const uint8_t* __restrict__ base, CellGeom geom,
-                                                                    const Region* __restrict__ regions, int chunks,
-                                                                    RegionSums* __restrict__ sums) {
+                                                                    const Region* __restrict__ regions, int n_regions,
+                                                                    int chunks, RegionSums* __restrict__ sums,
+                                                                    float4* __restrict__ out_lab,
+                                                                    uchar4* __restrict__ out_rgb) {
   __shared__ float s_lut[256];
-  __shared__ float s_ms[9];
-  __shared__ long long s_lab[kStatThreads / 32][3];
-  __shared__ unsigned long long s_rgb[kStatThreads / 32][3];
-
-  const int r = blockIdx.x / chunks;
-  const int chunk = blockIdx.x - r * chunks;
-  int64_t off, stride;
-  int w, h;
-  if (kCells) {
-    const int cx = r % geom.gw, cy = r / geom.gw;
-    w = geom.cw;
-    h = geom.ch;
-    stride = geom.stride;
-    off = (int64_t)cy * geom.ch * stride + 3ll * cx * geom.cw;
-  } else {
-    const Region reg = regions[r];
-    off = reg.offset;
-    w = reg.w;
-    h = reg.h;
-    stride = reg.stride;
-  }
   if (kLab) {
     for (int i = threadIdx.x; i < 256; i += blockDim.x) s_lut[i] = c_lab.lut[i];
-    if (threadIdx.x < 9) s_ms[threadIdx.x] = c_lab.ms[threadIdx.x];
     __syncthreads();
   }
-  const float eps = c_lab.eps, k1 = c_lab.k1, k2 = c_lab.k2;
-
-  const int y0 = (int)((int64_t)chunk * h / chunks), y1 = (int)((int64_t)(chunk + 1) * h / chunks);
-  long long aL = 0, aA = 0, aB = 0;
-  unsigned int sr = 0, sg = 0, sb = 0;
-  auto pixel = [&](uint32_t r8, uint32_t g8, uint32_t b8) {
-    sr += r8;
-    sg += g8;
-    sb += b8;
-    if (kLab) {
-      float L, A, B;
-      lab_pixel(s_lut, s_ms, eps, k1, k2, r8, g8, b8, L, A, B);
-      aL += lab_quant(L);
-      aA += lab_quant(A);
-      aB += lab_quant(B);
-    }
-  };
-  const uint8_t* img = base + off;
-  if ((w & 3) == 0 && (stride & 3) == 0 && ((uintptr_t)img & 3) == 0) {
-    // Four pixels of a row as three 32-bit words (fewer, wider loads: the
-    // regions may sit in pinned host memory read over the CPU-GPU link).  The
-    // sums are exact integers, so the order of the pixels does not matter.
-    const int gpr = w >> 2;
-    const int64_t ng = (int64_t)(y1 - y0) * gpr;
-    int gx = threadIdx.x % gpr, y = y0 + threadIdx.x / gpr;
-    const int dgx = kStatThreads % gpr, dgy = kStatThreads / gpr;
-    for (int64_t q = threadIdx.x; q < ng; q += kStatThreads) {
-      const uint32_t* p = reinterpret_cast<const uint32_t*>(img + (int64_t)y * stride + 12 * gx);
-      const uint32_t w0 = p[0], w1 = p[1], w2 = p[2];
-      pixel(w0 & 0xFFu, (w0 >> 8) & 0xFFu, (w0 >> 16) & 0xFFu);
-      pixel(w0 >> 24, w1 & 0xFFu, (w1 >> 8) & 0xFFu);
-      pixel((w1 >> 16) & 0xFFu, w1 >> 24, w2 & 0xFFu);
-      pixel((w2 >> 8) & 0xFFu, (w2 >> 16) & 0xFFu, w2 >> 24);
-      gx += dgx;
-      y += dgy;
-      if (gx >= gpr) {
-        gx -= gpr;
-        ++y;
-      }
-    }
-  } else {
-    // Walk pixels i = tid, tid + T, ... of the chunk with incremental (x, y).
-    const int64_t npx = (int64_t)(y1 - y0) * w;
-    int x = threadIdx.x % w, y = y0 + threadIdx.x / w;
-    const int dx = kStatThreads % w, dy = kStatThreads / w;
-    for (int64_t i = threadIdx.x; i < npx; i += kStatThreads) {
-      const uint8_t* p = img + (int64_t)y * stride + 3 * x;
-      pixel(p[0], p[1], p[2]);
-      x += dx;
-      y += dy;
-      if (x >= w) {
-        x -= w;
-        ++y;
-      }
-    }
-  }
-  unsigned long long ur = sr, ug = sg, ub = sb;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    if (kLab) {
-      aL += __shfl_xor_sync(0xffffffffu, aL, o);
-      aA += __shfl_xor_sync(0xffffffffu, aA, o);
-      aB += __shfl_xor_sync(0xffffffffu, aB, o);
-    }
-    ur += __shfl_xor_sync(0xffffffffu, ur, o);
-    ug += __shfl_xor_sync(0xffffffffu, ug, o);
-    ub += __shfl_xor_sync(0xffffffffu, ub, o);
-  }
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) {
-    s_lab[warp][0] = aL; s_lab[warp][1] = aA; s_lab[warp][2] = aB;
-    s_rgb[warp][0] = ur; s_rgb[warp][1] = ug; s_rgb[warp][2] = ub;
-  }
-  __syncthreads();
-  if (threadIdx.x < 6) {
-    const int c = threadIdx.x % 3;
-    if (threadIdx.x < 3) {
-      long long t = 0;
-      for (int i = 0; i < kStatThreads / 32; ++i) t += s_lab[i][c];
-      if (kLab) atomicAdd(reinterpret_cast<unsigned long long*>(&sums[r].lab[c]), (unsigned long long)t);
+  const LabK K = make_lab_k(c_lab.ms, c_lab.eps, c_lab.k1, c_lab.k2);
+  const int lane = threadIdx.x & 31;
+  const int64_t units = (int64_t)n_regions * chunks;
+  for (int64_t u = (int64_t)blockIdx.x * kStatWarps + (threadIdx.x >> 5); u < units;
+       u += (int64_t)gridDim.x * kStatWarps) {
+    const int r = (int)(u / chunks);
+    const int chunk = (int)(u - (int64_t)r * chunks);
+    int64_t off, stride;
+    int w, h;
+    if (kCells) {
+      const int cx = r % geom.gw, cy = r / geom.gw;
+      w = geom.cw;
+      h = geom.ch;
+      stride = geom.stride;
+      off = (int64_t)cy * geom.ch * stride + 3ll * cx * geom.cw;
     } else {
-      unsigned long long t = 0;
-      for (int i = 0; i < kStatThreads / 32; ++i) t += s_rgb[i][c];
-      atomicAdd(&sums[r].rgb[c], t);
+      const Region reg = regions[r];
+      off = reg.offset;
+      w = reg.w;
+      h = reg.h;
+      stride = reg.stride;
+    }
+    const int y0 = (int)((int64_t)chunk * h / chunks), y1 = (int)((int64_t)(chunk + 1) * h / chunks);
+    LabAcc acc;
+    reduce_rows<kLab>(base + off, w, stride, y0, y1, lane, s_lut, K, acc);
+    const LabSums t = warp_sums<kLab>(acc);
+    if (lane == 0) {
+      if (chunks == 1) {
+        const long long npx = (long long)w * h;
+        if (kLab && out_lab)
+          out_lab[r] = make_float4(lab_mean(t.L, npx), lab_mean(t.A, npx), lab_mean(t.B, npx), 0.0f);
+        if (out_rgb) {
+          const unsigned long long n = (unsigned long long)npx;
+          out_rgb[r] = make_uchar4((unsigned char)(t.R / n), (unsigned char)(t.G / n), (unsigned char)(t.Bc / n), 0);
+        }
+      } else {
+        if (kLab) {
+          atomicAdd(reinterpret_cast<unsigned long long*>(&sums[r].lab[0]), (unsigned long long)t.L);
+          atomicAdd(reinterpret_cast<unsigned long long*>(&sums[r].lab[1]), (unsigned long long)t.A);
+          atomicAdd(reinterpret_cast<unsigned long long*>(&sums[r].lab[2]), (unsigned long long)t.B);
+        }
+        atomicAdd(&sums[r].rgb[0], t.R);
+        atomicAdd(&sums[r].rgb[1], t.G);
+        atomicAdd(&sums[r].rgb[2], t.Bc);
+      }
     }
   }
 }
@@ -247,25 +195,35 @@ int launch_region_stats(const uint8_t* base, const CellGeom* geom, const Region*
                         int64_t max_region_px, float4* out_lab, uchar4* out_rgb, RegionSums* scratch, int want_lab,
                         cudaStream_t stream) {
   if (n_regions <= 0) return MG_OK;
-  MG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(RegionSums) * (size_t)n_regions, stream));
-  // Split large regions over several CTAs so that small palettes still fill the GPU.
-  int chunks = (int)std::min<int64_t>(64, std::max<int64_t>(1, max_region_px / 8192));
-  if ((int64_t)n_regions * chunks > (1ll << 30)) return fail(MG_ERR_ARG, "too many regions");
-  const unsigned grid = (unsigned)(n_regions * chunks);
+  // Regions above 2 units split into row chunks of about kUnitPx pixels, so
+  // that a few large materials still spread over the GPU; smaller ones (target
+  // cells) are one warp each and need no scratch.
+  const int chunks = (int)std::min<int64_t>(64, std::max<int64_t>(1, max_region_px / kUnitPx));
+  const int64_t units = (int64_t)n_regions * chunks;
+  if (units > (1ll << 40)) return fail(MG_ERR_ARG, "too many regions");
+  if (chunks > 1) MG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(RegionSums) * (size_t)n_regions, stream));
+  int dev = 0, sms = 0;
+  MG_CUDA(cudaGetDevice(&dev));
+  MG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((units + kStatWarps - 1) / kStatWarps,
+                                                                         (int64_t)sms * 16));
   CellGeom g{};
   if (geom) g = *geom;
+  float4* lab = want_lab ? out_lab : nullptr;
   if (geom) {
-    if (want_lab) region_stats_kernel<true, true><<<grid, kStatThreads, 0, stream>>>(base, g, nullptr, chunks, scratch);
-    else region_stats_kernel<true, false><<<grid, kStatThreads, 0, stream>>>(base, g, nullptr, chunks, scratch);
-    region_finalize_kernel<true><<<(n_regions + 255) / 256, 256, 0, stream>>>(g, nullptr, n_regions, scratch,
-                                                                             want_lab ? out_lab : nullptr, out_rgb);
+    if (want_lab) region_stats_kernel<true, true><<<grid, kStatThreads, 0, stream>>>(base, g, nullptr, n_regions, chunks, scratch, lab, out_rgb);
+    else region_stats_kernel<true, false><<<grid, kStatThreads, 0, stream>>>(base, g, nullptr, n_regions, chunks, scratch, lab, out_rgb);
+    if (chunks > 1)
+      region_finalize_kernel<true><<<(n_regions + 255) / 256, 256, 0, stream>>>(g, nullptr, n_regions, scratch, lab,
+                                                                               out_rgb);
   } else {
-    if (want_lab) region_stats_kernel<false, true><<<grid, kStatThreads, 0, stream>>>(base, g, regions, chunks, scratch);
-    else region_stats_kernel<false, false><<<grid, kStatThreads, 0, stream>>>(base, g, regions, chunks, scratch);
-    region_finalize_kernel<false><<<(n_regions + 255) / 256, 256, 0, stream>>>(g, regions, n_regions, scratch,
-                                                                              want_lab ? out_lab : nullptr, out_rgb);
+    if (want_lab) region_stats_kernel<false, true><<<grid, kStatThreads, 0, stream>>>(base, g, regions, n_regions, chunks, scratch, lab, out_rgb);
+    else region_stats_kernel<false, false><<<grid, kStatThreads, 0, stream>>>(base, g, regions, n_regions, chunks, scratch, lab, out_rgb);
+    if (chunks > 1)
+      region_finalize_kernel<false><<<(n_regions + 255) / 256, 256, 0, stream>>>(g, regions, n_regions, scratch, lab,
+                                                                                out_rgb);
   }
-  g_launches += 2;
+  g_launches += chunks > 1 ? 2 : 1;
   MG_CUDA(cudaGetLastError());
   return MG_OK;
 }

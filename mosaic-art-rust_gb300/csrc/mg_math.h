@@ -141,14 +141,16 @@ MG_HD float exp_spec(float x) {
 }
 
 // --------------------------------------------------------------------------
-// Cube root on (216/24389, ~1.1]: bit-level first guess for t^(-1/3), three
-// Newton steps r += r/3 (1 - t r^3), y = t r^2, one Newton polish of y.
-// Max error 0.73 ulp against FP64 cbrt on that interval.
+// Cube root on (216/24389, ~1.1]: bit-level first guess for t^(-1/3) (within
+// 3.3%), two Newton steps r += r/3 (1 - t r^3) (relative error then below
+// 1e-5), y = t r^2, one Newton polish of y.  Max error 0.77 ulp against FP64
+// cbrt on that interval (every float checked), mean error -0.004 ulp.
 // --------------------------------------------------------------------------
+constexpr int kCbrtNewton = 2;
 MG_HD float cbrt_spec(float t) {
   float r = u2f(0x54A2FA8Cu - f2u(t) / 3u);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
+  for (int k = 0; k < kCbrtNewton; ++k) {
     float r2 = MG_MUL(r, r);
     float r3 = MG_MUL(r2, r);
     float e = MG_FMA(-t, r3, 1.0f);
@@ -201,6 +203,61 @@ MG_HD long long lab_quant(float v) {
 #else
   return (long long)std::llrintf(v * kLabQ);
 #endif
+}
+
+// The quantised Lab of one pixel as the reduction kernels compute it:
+// lab_quant of each lab_pixel component, rearranged without changing a
+// result.  The 2^20 scale is folded into the L, a, b constants (scaling by a
+// power of two commutes with rounding), and the clamps are left out: for all
+// 2^24 sRGB8 colours a and b stay inside [-128, 127] and L inside [0, 100]
+// except for black, whose L of -6e-8 quantises to 0 as the clamped value
+// does.  The kernels evaluate this on pairs of pixels with packed FP32x2
+// arithmetic (each component rounded as here).  The cube root is cbrt_spec
+// with the seed's division by 3 as a multiply-high (div3_u31: equal for
+// inputs below 2^31, and t >= 0 here).
+constexpr float kLabQL = 121634816.0f;   // 116 * 2^20
+constexpr float kLabQL0 = -16777216.0f;  // -16 * 2^20
+constexpr float kLabQA = 524288000.0f;   // 500 * 2^20
+constexpr float kLabQB = 209715200.0f;   // 200 * 2^20
+MG_HD uint32_t div3_u31(uint32_t x) {  // x / 3 for x < 2^31
+#if defined(__CUDA_ARCH__)
+  return __umulhi(x, 0x55555556u);
+#else
+  return (uint32_t)(((uint64_t)x * 0x55555556u) >> 32);
+#endif
+}
+MG_HD int quant_rn(float v) {
+#if defined(__CUDA_ARCH__)
+  return __float2int_rn(v);
+#else
+  return (int)std::lrintf(v);
+#endif
+}
+MG_HD void lab_pixel_q(const float* lut, const float* ms, float eps, float k1, float k2, uint32_t r8, uint32_t g8,
+                       uint32_t b8, int& qL, int& qA, int& qB) {
+  float R = lut[r8], G = lut[g8], Bl = lut[b8];
+  float t[3];
+  for (int i = 0; i < 3; ++i) t[i] = MG_FMA(ms[3 * i + 2], Bl, MG_FMA(ms[3 * i + 1], G, MG_MUL(ms[3 * i], R)));
+  float f[3];
+  for (int i = 0; i < 3; ++i) {
+    float r = u2f(0x54A2FA8Cu - div3_u31(f2u(t[i])));
+    for (int k = 0; k < kCbrtNewton; ++k) {
+      float r2 = MG_MUL(r, r);
+      float r3 = MG_MUL(r2, r);
+      float e = MG_FMA(-t[i], r3, 1.0f);
+      r = MG_FMA(MG_MUL(r, 1.0f / 3.0f), e, r);
+    }
+    float rr = MG_MUL(r, r);
+    float y = MG_MUL(t[i], rr);
+    float y2 = MG_MUL(y, y);
+    float res = MG_FMA(-y2, y, t[i]);
+    float c = MG_FMA(res, MG_MUL(rr, 1.0f / 3.0f), y);
+    float l = MG_FMA(k1, t[i], k2);
+    f[i] = t[i] > eps ? c : l;
+  }
+  qL = quant_rn(MG_FMA(kLabQL, f[1], kLabQL0));
+  qA = quant_rn(MG_MUL(MG_ADD(f[0], -f[1]), kLabQA));
+  qB = quant_rn(MG_MUL(MG_ADD(f[1], -f[2]), kLabQB));
 }
 
 // Sum (fixed point) / pixel count -> mean, in FP32.

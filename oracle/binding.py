@@ -27,7 +27,7 @@ class OracleJob(C.Structure):
                 ("max_usage", C.c_int), ("weight", C.c_float), ("color_strength", C.c_float),
                 ("enable_opt", C.c_int), ("iters", C.c_long), ("t0", C.c_float), ("decay", C.c_float),
                 ("chains", C.c_int), ("seed", C.c_uint64), ("stream", C.c_uint32), ("threads", C.c_int),
-                ("gui_scoring", C.c_int)]
+                ("gui_scoring", C.c_int), ("ref_arith", C.c_int)]
 
 
 class OracleOut(C.Structure):
@@ -42,6 +42,8 @@ _SIGS = [
     ("orc_lab_mean_f64", None, [_u8p, C.c_int, C.c_int, C.c_long, _f64p]),
     ("orc_lab_mean_reffold", None, [_u8p, C.c_int, C.c_int, C.c_long, _f32p]),
     ("orc_lab_pixel_spec", None, [C.c_int, C.c_int, C.c_int, _f32p]),
+    ("orc_lab_consts", None, [_f32p, _f32p, _f32p]),
+    ("orc_lab_pixels_q", None, [_u8p, C.c_long, _i32p]),
     ("orc_lab_mean_spec", None, [_u8p, C.c_int, C.c_int, C.c_long, _f32p]),
     ("orc_avg_rgb", None, [_u8p, C.c_int, C.c_int, C.c_long, _u8p]),
     ("orc_cells", C.c_int, [_u8p, C.c_int, C.c_int, C.c_long, C.c_int, C.c_int, _f32p, _u8p]),
@@ -60,11 +62,14 @@ _SIGS = [
     ("orc_exp", C.c_float, [C.c_float]),
     ("orc_anneal", None, [_f32p, C.c_int, _i32p, C.c_int, C.c_int, C.c_long, C.c_float, C.c_float, C.c_uint64,
                           C.c_uint32, C.c_uint32, C.c_int, _f32p, _i64p]),
+    ("orc_anneal_ex", None, [_f32p, C.c_int, _i32p, C.c_int, C.c_int, C.c_long, C.c_float, C.c_float, C.c_uint64,
+                             C.c_uint32, C.c_uint32, C.c_int, C.c_int, _f32p, _i64p]),
     ("orc_rgb_to_hsv", None, [C.c_float, C.c_float, C.c_float, _f32p]),
     ("orc_hsv_to_rgb", None, [C.c_float, C.c_float, C.c_float, _f32p]),
     ("orc_adjustment_new", None, [C.c_float, C.c_float, C.c_float, C.c_float, _f32p]),
     ("orc_optimal_adjustment", None, [_u8p, _u8p, C.c_float, _f32p]),
     ("orc_adjust_pixel", None, [_f32p, _u8p, _u8p]),
+    ("orc_adjust_pixels", None, [_f32p, _u8p, C.c_long, _u8p]),
     ("orc_composite", C.c_int, [_i32p, C.c_int, C.c_int, _u8p, C.c_int, C.c_int, _u8p, _u8p, C.c_float, _u8p]),
     ("orc_generate", C.c_int, [C.POINTER(OracleJob), C.POINTER(OracleOut)]),
 ]
@@ -197,14 +202,17 @@ def penalty(pal, grid, cand, x, y, weight):
     return lib().orc_penalty(p(pal, C.c_float), pal.shape[0], cand, x, y, p(g, C.c_int32), gw, gh, weight)
 
 
-def anneal(pal, grid, iters, t0=100.0, decay=0.99995, seed=0x5EED5EED5EED, stream=0, chain=0, greedy_only=False):
+def anneal(pal, grid, iters, t0=100.0, decay=0.99995, seed=0x5EED5EED5EED, stream=0, chain=0, greedy_only=False,
+           libm_exp=False):
+    """One annealing chain from `grid` (libm_exp: acceptance by the C library's
+    expf instead of the defined exp)."""
     pal = np.ascontiguousarray(pal, np.float32).reshape(-1, 3)
     g = np.ascontiguousarray(grid, np.int32).copy()
     gh, gw = g.shape if g.size else (0, 0)
     res = np.zeros(3, np.float32)
     cnt = np.zeros(3, np.int64)
-    lib().orc_anneal(p(pal, C.c_float), pal.shape[0], p(g, C.c_int32), gw, gh, iters, t0, decay, seed, stream, chain,
-                     1 if greedy_only else 0, p(res, C.c_float), p(cnt, C.c_int64))
+    lib().orc_anneal_ex(p(pal, C.c_float), pal.shape[0], p(g, C.c_int32), gw, gh, iters, t0, decay, seed, stream,
+                        chain, 1 if greedy_only else 0, 1 if libm_exp else 0, p(res, C.c_float), p(cnt, C.c_int64))
     return g, res, cnt
 
 
@@ -243,9 +251,11 @@ def composite(grid, thumbs, cell_rgb, thumb_rgb, strength):
     return out
 
 
-def generate(inp, threads: int = 1, want_image: bool = True, stream: int = 0, gui: bool = False):
+def generate(inp, threads: int = 1, want_image: bool = True, stream: int = 0, gui: bool = False,
+             ref_arith: bool = False):
     """Run the whole job on the CPU from mosaic_gpu.job.Inputs (Philox stream id
-    `stream`; gui: the GUI generator's greedy scoring)."""
+    `stream`; gui: the GUI generator's greedy scoring; ref_arith: Lab by the
+    reference's FP32 fold and acceptance by libm expf)."""
     cfg = inp.cfg
     tw, th = inp.tile
     n = len(inp.mats)
@@ -268,6 +278,7 @@ def generate(inp, threads: int = 1, want_image: bool = True, stream: int = 0, gu
     job.iters, job.t0, job.decay = cfg.iterations, 100.0, 0.99995
     job.chains, job.seed, job.stream, job.threads = cfg.chains, cfg.seed, stream, threads
     job.gui_scoring = 1 if gui else 0
+    job.ref_arith = 1 if ref_arith else 0
     N = cfg.grid_w * cfg.grid_h
     grid = np.zeros(N, np.int32)
     image = np.zeros((cfg.grid_h * th, cfg.grid_w * tw, 3), np.uint8) if want_image else None

@@ -124,11 +124,12 @@ const SpecConsts& spec() {
 }
 
 // Cube root on (216/24389, ~1.1], the build's own definition (identical op
-// sequence in the CUDA library): bit-level initial guess for t^(-1/3), three
+// sequence in the CUDA library): bit-level initial guess for t^(-1/3), two
 // Newton steps r += r/3 * (1 - t r^3), y = t r^2, one Newton polish of y.
+// Max error 0.77 ulp against FP64 cbrt on that interval.
 float cbrt_spec(float t) {
   float r = u2f(0x54A2FA8Cu - f2u(t) / 3u);
-  for (int k = 0; k < 3; ++k) {
+  for (int k = 0; k < 2; ++k) {
     float r2 = r * r;
     float r3 = r2 * r;
     float e = std::fmaf(-t, r3, 1.0f);
@@ -316,6 +317,28 @@ void orc_lab_mean_reffold(const uint8_t* rgb, int w, int h, long stride, float o
 }
 
 void orc_lab_pixel_spec(int r, int g, int b, float out[3]) { lab_pixel_spec(r, g, b, out); }
+
+// The constants of the defined conversion: transfer table, white-normalised
+// RGB -> XYZ matrix (row major), and eps, kappa / 116, 16 / 116.
+void orc_lab_consts(float lut[256], float ms[9], float k[3]) {
+  const SpecConsts& S = spec();
+  std::memcpy(lut, S.lut, sizeof(float) * 256);
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) ms[3 * r + c] = S.ms[r][c];
+  k[0] = S.eps;
+  k[1] = S.k1;
+  k[2] = S.k2;
+}
+
+// The fixed-point summands of n pixels (L, a, b of each, scaled by 2^20 and
+// rounded as orc_lab_mean_spec sums them).
+void orc_lab_pixels_q(const uint8_t* rgb, long n, int32_t* q) {
+  for (long i = 0; i < n; ++i) {
+    float l[3];
+    lab_pixel_spec(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2], l);
+    for (int c = 0; c < 3; ++c) q[3 * i + c] = (int32_t)quantize(l[c]);
+  }
+}
 
 // lib.rs:94-119 in the build's defined arithmetic (FP32 per pixel, exact
 // fixed-point sum, one FP32 division).  The CUDA reduction must equal this.
@@ -570,9 +593,11 @@ float orc_exp(float x) { return exp_spec(x); }
 // uniform (word0 >> 8) * 2^-24 (rand's f32 construction).  An iteration that
 // draws pos1 == pos2 or an empty cell is skipped without cooling, as in the
 // reference.
-void orc_anneal(const float* pal, int p, int32_t* grid, int gw, int gh, long iters, float t0, float decay,
-                uint64_t seed, uint32_t stream, uint32_t chain, int greedy_only, float res[3],
-                int64_t counts[3]) {
+// libm_exp: the acceptance test with the C library's expf (what Rust's
+// f32::exp calls, optimizer.rs:81) instead of the defined exp_spec.
+void orc_anneal_ex(const float* pal, int p, int32_t* grid, int gw, int gh, long iters, float t0, float decay,
+                   uint64_t seed, uint32_t stream, uint32_t chain, int greedy_only, int libm_exp, float res[3],
+                   int64_t counts[3]) {
   res[0] = res[1] = res[2] = 0.0f;
   counts[0] = counts[1] = counts[2] = 0;
   if (gh == 0 || gw == 0) return;
@@ -601,7 +626,8 @@ void orc_anneal(const float* pal, int p, int32_t* grid, int gw, int gh, long ite
       uint32_t u[4];
       philox4x32_10(ctr2, key, u);
       float uf = (float)(u[0] >> 8) * 5.9604644775390625e-08f;
-      accept = uf < exp_spec(-delta / temp);
+      const float arg = -delta / temp;
+      accept = uf < (libm_exp ? std::exp(arg) : exp_spec(arg));
     }
     if (accept) {
       std::swap(grid[y1 * gw + x1], grid[y2 * gw + x2]);
@@ -621,6 +647,12 @@ void orc_anneal(const float* pal, int p, int32_t* grid, int gw, int gh, long ite
   counts[0] = accepted;
   counts[1] = greedy_only ? accepted : improved;
   counts[2] = cooled;
+}
+
+void orc_anneal(const float* pal, int p, int32_t* grid, int gw, int gh, long iters, float t0, float decay,
+                uint64_t seed, uint32_t stream, uint32_t chain, int greedy_only, float res[3],
+                int64_t counts[3]) {
+  orc_anneal_ex(pal, p, grid, gw, gh, iters, t0, decay, seed, stream, chain, greedy_only, 0, res, counts);
 }
 
 // palette 0.7.6 Hsv::from_color(Rgb) -- hexcone, hue in raw degrees (may be
@@ -715,6 +747,11 @@ void orc_adjust_pixel(const float adj[4], const uint8_t in[3], uint8_t out[3]) {
   for (int i = 0; i < 3; ++i) out[i] = as_u8(rclamp(f[i] * 255.0f, 0.0f, 255.0f));
 }
 
+// orc_adjust_pixel of n pixels.
+void orc_adjust_pixels(const float adj[4], const uint8_t* in, long n, uint8_t* out) {
+  for (long i = 0; i < n; ++i) orc_adjust_pixel(adj, in + 3 * i, out + 3 * i);
+}
+
 // main.rs:548-592 (first composite) and main.rs:627-664 (rebuild after the
 // optimiser): per cell, the material's thumbnail, colour-adjusted when the
 // strength is positive, written at (x*tw, y*th).  Cells without a tile stay 0.
@@ -754,10 +791,16 @@ int orc_generate(const orc_job* J, orc_out* O) {
   std::vector<int> sel(std::max(J->n_mats, 1));
   int P = orc_select_palette(J->mat_w, J->mat_h, J->n_mats, target_aspect, J->aspect_tol,
                              J->max_materials, sel.data());
+  // ref_arith: Lab as lib.rs:99-118 folds it (per-pixel FP32 conversion, a
+  // sequential FP32 sum, one division) instead of the defined fixed-point mean
+  auto lab_mean = [&](const uint8_t* img, int w, int h, long stride, float* out) {
+    if (J->ref_arith) orc_lab_mean_reffold(img, w, h, stride, out);
+    else orc_lab_mean_spec(img, w, h, stride, out);
+  };
   std::vector<float> pal(3 * (size_t)std::max(P, 1));
   parallel_for(P, J->threads, [&](int i) {
     int m = sel[i];
-    orc_lab_mean_spec(J->mats + J->mat_off[m], J->mat_w[m], J->mat_h[m], 3L * J->mat_w[m], pal.data() + 3 * i);
+    lab_mean(J->mats + J->mat_off[m], J->mat_w[m], J->mat_h[m], 3L * J->mat_w[m], pal.data() + 3 * i);
   });
   std::vector<float> cell_lab(3 * (size_t)N);
   std::vector<uint8_t> cell_rgb(3 * (size_t)N);
@@ -766,7 +809,7 @@ int orc_generate(const orc_job* J, orc_out* O) {
     for (int x = 0; x < J->gw; ++x) {
       const uint8_t* base = J->target + (long)y * ch * J->tstride + 3L * x * cw;
       int c = y * J->gw + x;
-      orc_lab_mean_spec(base, cw, ch, J->tstride, cell_lab.data() + 3 * c);
+      lab_mean(base, cw, ch, J->tstride, cell_lab.data() + 3 * c);
       orc_avg_rgb(base, cw, ch, J->tstride, cell_rgb.data() + 3 * c);
     }
   });
@@ -785,8 +828,8 @@ int orc_generate(const orc_job* J, orc_out* O) {
     std::vector<float> res(3 * K);
     parallel_for(K, J->threads, [&](int c) {
       int64_t cnt[3];
-      orc_anneal(pal.data(), P, g[c].data(), J->gw, J->gh, J->iters, J->t0, J->decay, J->seed, J->stream,
-                 (uint32_t)c, 0, res.data() + 3 * c, cnt);
+      orc_anneal_ex(pal.data(), P, g[c].data(), J->gw, J->gh, J->iters, J->t0, J->decay, J->seed, J->stream,
+                    (uint32_t)c, 0, J->ref_arith, res.data() + 3 * c, cnt);
     });
     best_chain = 0;
     for (int c = 1; c < K; ++c)

@@ -31,6 +31,8 @@ void  orc_lab_pixel_f64(int r, int g, int b, double out[3]);
 void  orc_lab_mean_f64(const uint8_t* rgb, int w, int h, long stride, double out[3]);
 void  orc_lab_mean_reffold(const uint8_t* rgb, int w, int h, long stride, float out[3]);
 void  orc_lab_pixel_spec(int r, int g, int b, float out[3]);
+void  orc_lab_consts(float lut[256], float ms[9], float k[3]);
+void  orc_lab_pixels_q(const uint8_t* rgb, long n, int32_t* q);
 void  orc_lab_mean_spec(const uint8_t* rgb, int w, int h, long stride, float out[3]);
 void  orc_avg_rgb(const uint8_t* rgb, int w, int h, long stride, uint8_t out[3]);
 int   orc_cells(const uint8_t* img, int w, int h, long stride, int gw, int gh,
@@ -74,8 +76,12 @@ void  orc_adjustment_new(float br, float co, float hue, float sat, float out[4])
 void  orc_optimal_adjustment(const uint8_t tile[3], const uint8_t target[3], float strength,
                              float out[4]);
 void  orc_adjust_pixel(const float adj[4], const uint8_t in[3], uint8_t out[3]);
+void  orc_adjust_pixels(const float adj[4], const uint8_t* in, long n, uint8_t* out);
 
 /* ---- composite (main.rs:583-592, 627-664) -------------------------------- */
+void  orc_anneal_ex(const float* pal, int p, int32_t* grid, int gw, int gh, long iters, float t0, float decay,
+                    uint64_t seed, uint32_t stream, uint32_t chain, int greedy_only, int libm_exp, float res[3],
+                    int64_t counts[3]);
 int   orc_composite(const int32_t* grid, int gw, int gh, const uint8_t* thumbs, int tw, int th,
                     const uint8_t* cell_avg_rgb, const uint8_t* thumb_avg_rgb,
                     float strength, uint8_t* out);
@@ -94,6 +100,8 @@ typedef struct orc_job {
   int enable_opt; long iters; float t0, decay; int chains; uint64_t seed; uint32_t stream;
   int threads;
   int gui_scoring;  /* 1: the GUI generator's scoring (orc_place_greedy_gui) */
+  int ref_arith;    /* 1: Lab by the reference's FP32 fold (orc_lab_mean_reffold) and
+                       annealing acceptance by libm expf, instead of the defined arithmetic */
 } orc_job;
 
 typedef struct orc_out {

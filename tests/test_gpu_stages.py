@@ -36,6 +36,40 @@ def test_cells_lab_bit_exact(ctx, orc, w, h, gw, gh):
         assert np.linalg.norm(lab[c].astype(np.float64) - ref) <= LAB_TOL_DE
 
 
+def _every_colour():
+    """A 4096 x 4096 image holding each sRGB8 colour once, in an order that
+    mixes all three channels inside every 16 x 16 block."""
+    i = np.arange(1 << 24, dtype=np.uint32)
+    j = (i * np.uint32(2654435761)) & np.uint32(0xFFFFFF)  # odd multiplier: a permutation of 0..2^24-1
+    rgb = np.stack([(j >> 16) & 0xFF, (j >> 8) & 0xFF, j & 0xFF], -1).astype(np.uint8)
+    return rgb.reshape(4096, 4096, 3)
+
+
+@pytest.mark.parametrize("cell", [1, 4, 8, 16, 12])
+def test_cells_lab_every_colour(ctx, orc, cell):
+    """Every sRGB8 colour through the cell reduction: 1-pixel cells take the
+    pixel-pair path (each cell one pixel, so each colour's Lab is checked on
+    its own), 4-, 8- and 16-pixel cells the 12-, 24- and 48-byte vector paths,
+    12-pixel cells the 12-byte path with 36-byte cell offsets.  Every cell's
+    Lab equals the oracle's fixed-point mean of its pixels bit for bit."""
+    import ctypes as C
+
+    img = _every_colour()
+    g = 4096 // cell
+    q = np.empty((1 << 24, 3), np.int32)
+    orc.lib().orc_lab_pixels_q(img.ctypes.data_as(C.POINTER(C.c_uint8)), 1 << 24,
+                               q.ctypes.data_as(C.POINTER(C.c_int32)))
+    sums = q.reshape(4096, 4096, 3)[:g * cell, :g * cell].astype(np.int64)
+    sums = sums.reshape(g, cell, g, cell, 3).sum(axis=(1, 3)).reshape(-1, 3)
+    n = np.float32(cell * cell)
+    want = (sums.astype(np.float32) / n) * np.float32(2.0 ** -20)
+    lab, rgb = ctx.cells_lab(img, g, g) if cell * g == 4096 else ctx.cells_lab(
+        np.ascontiguousarray(img[:g * cell, :g * cell]), g, g)
+    assert np.array_equal(lab.view(np.uint32), want.view(np.uint32))
+    px = img[:g * cell, :g * cell].reshape(g, cell, g, cell, 3).astype(np.uint64).sum(axis=(1, 3)).reshape(-1, 3)
+    assert np.array_equal(rgb, (px // np.uint64(cell * cell)).astype(np.uint8))
+
+
 def test_images_lab_bit_exact(ctx, orc):
     rng = np.random.default_rng(1)
     imgs = [rng.integers(0, 256, (h, w, 3), dtype=np.uint8) for (w, h) in

@@ -54,6 +54,32 @@ def test_lab_pixel_exhaustive_grey_and_primaries(orc):
     assert worst < 1e-4, worst
 
 
+def test_kernel_lab_arithmetic_equals_the_oracle_for_every_colour(orc):
+    """The reduction kernels compute each pixel's fixed-point Lab summands as
+    mg_math.h's lab_pixel_q (clamps left out, the 2^20 scale folded into the
+    constants, the cube root's division by 3 as a multiply-high), two pixels at
+    a time in packed FP32x2 arithmetic.  For all 2^24 sRGB8 colours that equals
+    the oracle's defined Lab, clamped and quantised (tests/cpp/lab_equiv.cpp)."""
+    import shutil
+    import subprocess
+    import tempfile
+    from pathlib import Path
+
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    repo = Path(__file__).resolve().parents[1]
+    build = repo / "oracle" / "build"
+    with tempfile.TemporaryDirectory() as d:
+        exe = Path(d) / "lab_equiv"
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math",
+               str(repo / "tests" / "cpp" / "lab_equiv.cpp"), f"-L{build}", "-loracle", f"-Wl,-rpath,{build}",
+               "-o", str(exe)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "differing 0" in r.stdout, r.stdout + r.stderr
+
+
 # ---- main.rs:866-889 calculate_average_rgb -----------------------------------------------
 def test_avg_rgb_red(orc):
     assert tuple(orc.avg_rgb(solid(10, 10, (255, 0, 0)))) == (255, 0, 0)

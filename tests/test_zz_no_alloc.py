@@ -37,13 +37,15 @@ def test_noalloc_matches_allocating_entry_point_twice(ctx):
     lib = _capi.load()
     img_a = synth.target(640, 480, 5, seed=1234, stream=3)
     img_b = synth.target(640, 480, 9, seed=98765, stream=4)
-    gw, gh = 40, 30
-    for img in (img_a, img_b):  # two calls in a row, different inputs
-        rc, lab4, rgb4 = _noalloc(lib, torch, img, gw, gh)
-        assert rc == _capi.MG_OK, lib.mg_last_error()
-        ref_lab, ref_rgb = ctx.cells_lab(img, gw, gh)
-        assert np.array_equal(lab4[:, :3].view(np.uint32), ref_lab.view(np.uint32))
-        assert np.array_equal(rgb4[:, :3], ref_rgb)
+    # 16x16-pixel cells are one warp each; 160x160-pixel cells (25 600 pixels)
+    # are split over several warps whose sums meet in the library's array
+    for gw, gh in ((40, 30), (4, 3)):
+        for img in (img_a, img_b):  # two calls in a row, different inputs
+            rc, lab4, rgb4 = _noalloc(lib, torch, img, gw, gh)
+            assert rc == _capi.MG_OK, lib.mg_last_error()
+            ref_lab, ref_rgb = ctx.cells_lab(img, gw, gh)
+            assert np.array_equal(lab4[:, :3].view(np.uint32), ref_lab.view(np.uint32))
+            assert np.array_equal(rgb4[:, :3], ref_rgb)
 
 
 def test_noalloc_rejects_grids_beyond_its_limit(ctx):
