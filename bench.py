@@ -12,10 +12,24 @@ greedy placement, the annealing chains and the colour-adjusted composite.
 
   value  tiles placed per second with the inputs resident in device memory
          (mg_plan_run), device time per step from CUDA events on the library's
-         stream, L2 flushed (512 MB write) between steps.
+         stream, L2 flushed (512 MB write) between steps.  The K timed steps
+         are repeated in passes until about a second of load has run, so the
+         clock sampler sees the clocks under load; every pass is timed.
   e2e    the same metric through mg_generate from pinned host buffers: host
          wall time per call, including the uploads and the download of the
          output image and grid.
+
+With one GPU the same line also carries the benchmark spec's two systems patterns
+and the large single mosaic, each measured in this run on the current build:
+  batched  256 uneven mosaics over one resident 10 000-material palette
+           (mosaics/s, against the same mosaics one single-mosaic batch after
+           another, the plain path)
+  served   Poisson arrivals at 50, 200 and 800 req/s over a resident
+           20 000-material palette (p50/p99, saturated mosaics/s, against one
+           request per batch and one batch in flight, the plain path)
+  large    7680x5760 target, 5000 materials, 179x134 cells, 64 chains x
+           100 000 iterations (tiles/s; the Lab reductions' and composite's
+           GB/s; k-nearest candidates per second)
 
 --impl reference times the CPU restatement of the reference's path (the
 reference crate itself cannot be built here: no Rust toolchain) on the host
@@ -56,6 +70,8 @@ def parse_args():
     ap.add_argument("--served-scale", type=float, default=1.0, help="shrinks the cell range (served)")
     ap.add_argument("--served-arena-gb", type=int, default=8, help="pinned output arena (served)")
     ap.add_argument("--batched-mosaics", type=int, default=256, help="mosaics in the batch (batched; fewer for profiling)")
+    ap.add_argument("--min-timed-s", type=float, default=1.0, help="repeat the K timed steps until this much load ran")
+    ap.add_argument("--no-patterns", action="store_true", help="leave the batched/served/large sub-records out")
     return ap.parse_args()
 
 
@@ -126,6 +142,15 @@ def workload_inputs(name: str, rank: int, allocator=None):
     if rank:
         cfg = job.scaled(cfg, seed=cfg.seed + 7919 * rank)
     return job.make_inputs(cfg, allocator)
+
+
+def bench_config(cfg, palette_in: int, palette: int, tile, world: int) -> dict:
+    """The workload as both arms name it (same keys, same values)."""
+    return {"workload": cfg.name, "cells": cfg.grid_w * cfg.grid_h, "palette_in": palette_in, "palette": palette,
+            "grid": f"{cfg.grid_w}x{cfg.grid_h}", "chains": cfg.chains, "iterations": cfg.iterations,
+            "tile": f"{tile[0]}x{tile[1]}", "max_usage": cfg.max_usage, "adjacency_weight": cfg.weight,
+            "color_strength": cfg.color_strength, "l2": "flushed (512 MB write) between steps",
+            "parallelism": f"replicas x{world}"}
 
 
 def algorithmic(inp, palette_size: int, sel_px: int):
@@ -239,8 +264,9 @@ def run_reference(args, rank, world):
     inp = workload_inputs(args.workload, 0)
     cores = os.cpu_count() or 1
     n = inp.cfg.grid_w * inp.cfg.grid_h
-    for _ in range(args.warmup):
-        ob.generate(inp, threads=cores)
+    palette = None
+    for _ in range(max(args.warmup, 1)):
+        palette = ob.generate(inp, threads=cores)["p"]
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
@@ -251,8 +277,7 @@ def run_reference(args, rank, world):
     line = {"metric": METRIC, "value": value, "unit": "tiles/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "cells": n, "palette": 1500, "grid": "80x60",
-                       "chains": inp.cfg.chains, "iterations": inp.cfg.iterations},
+            "config": bench_config(inp.cfg, len(inp.mats), int(palette), inp.tile, world),
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "tiles/s", "cores": cores, "kind": "port",
                              "sample": f"each step one full {args.workload} job on the C++ restatement of the "
@@ -300,29 +325,43 @@ def run_ours(args, rank, world, local):
                                 cfg.max_materials or n_m, sel)
     assert cnt == P
     sel_px = int(sum(int(inp.mats.w[i]) * int(inp.mats.h[i]) for i in sel[:P]))
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    stage_ms = np.zeros((args.steps, 8))
     clocks = ClockSampler(local)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
+
+    def timed_pass():
+        """Exactly K steps between a barrier + synchronize on both sides."""
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        st = np.zeros((args.steps, 8))
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(i & 0xFF)          # L2 flush between steps, outside the events
+                starts[i].record(stream)
+            plan.run()
+            with torch.cuda.stream(stream):
+                ends[i].record(stream)
+            st[i] = plan.stage_ms()
+        torch.cuda.synchronize()
+        return [s.elapsed_time(e) for s, e in zip(starts, ends)], st
+
     clocks.start()
     wall0 = time.perf_counter()
     launches0 = lib.mg_kernel_launches()
-    for i in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(i & 0xFF)          # L2 flush between steps, outside the events
-            starts[i].record(stream)
-        plan.run()
-        with torch.cuda.stream(stream):
-            ends[i].record(stream)
-        stage_ms[i] = plan.stage_ms()
-    torch.cuda.synchronize()
+    step_times, stage_rows, passes = [], [], 0
+    while True:  # K steps per pass; passes until about a second of load has run
+        t, st = timed_pass()
+        step_times += t
+        stage_rows.append(st)
+        passes += 1
+        if time.perf_counter() - wall0 >= args.min_timed_s or passes >= 1000:
+            break
     wall = time.perf_counter() - wall0
     launches = int(lib.mg_kernel_launches() - launches0)
     clk = clocks.stop()
-    step_ms = float(np.mean([s.elapsed_time(e) for s, e in zip(starts, ends)]))
+    stage_ms = np.concatenate(stage_rows)
+    step_ms = float(np.mean(step_times))
     if dist:
         t = torch.tensor([step_ms], device=torch.device("cuda", local))
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -371,13 +410,13 @@ def run_ours(args, rank, world, local):
         "metric": METRIC, "value": value, "unit": "tiles/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "cells": N, "palette_in": len(inp.mats), "palette": P,
-                   "grid": f"{cfg.grid_w}x{cfg.grid_h}", "chains": cfg.chains, "iterations": cfg.iterations,
-                   "tile": f"{tw}x{th}", "l2": "flushed (512 MB write) between steps",
-                   "parallelism": f"replicas x{world}"},
+        "config": bench_config(cfg, len(inp.mats), P, (tw, th), world),
+        "timed_passes": {"passes": passes, "steps_per_pass": args.steps,
+                         "ms_per_step_per_pass": [round(float(np.mean(step_times[i * args.steps:(i + 1) * args.steps])), 4)
+                                                  for i in range(passes)][:20]},
         "e2e": {"value": world * N / (e2e_ms / 1000.0), "unit": "tiles/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "matches_device_run": same},
-        "gpu_launches": launches,
+        "gpu_launches": launches // passes,
         "roofline": {"bound": "hbm", "kernel": KERNEL_OF_STAGE[dom_name], "stage": dom_name,
                      "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / peaks["hbm_gbs"], 6), "peak_source": peak_kind,
@@ -400,15 +439,36 @@ def run_ours(args, rank, world, local):
         line["cpu_baseline"] = cpu_baseline(inp)
     if rank == 0 and world == 1:
         line["file_ends"] = file_ends(inp.target)
+    plan.close()
+    del flush
+    if rank == 0 and world == 1 and not args.no_patterns and args.workload == WORKLOAD:
+        # the benchmark spec's systems patterns and the large mosaic, on this GPU, in this run
+        for key, fn in (("batched", lambda: measure_batched(args, 0, 1, local, ctx)),
+                        ("served", lambda: measure_served(args, 0, 1, local, ctx)),
+                        ("large", lambda: measure_large(args, local, ctx))):
+            try:
+                line[key] = fn()
+            except Exception as e:  # a sub-record never costs the headline line
+                line[key] = {"error": f"{type(e).__name__}: {str(e)[:300]}"}
+            torch.cuda.empty_cache()
     if rank == 0:
         print(json.dumps(line), flush=True)
-    plan.close()
     ctx.close()
     if dist:
         dist.destroy_process_group()
 
 
 def run_batched(args, rank, world, local):
+    from mosaic_gpu import _capi as capi
+
+    ctx = capi.Context(local)
+    line = measure_batched(args, rank, world, local, ctx)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def measure_batched(args, rank, world, local, ctx):
     """256 uneven mosaics over one resident 10 000-material palette: the batched
     pipeline (cell statistics and k-nearest over every cell, every walk in one
     launch, every chain in one launch, adjustment and composite; graph replay)
@@ -423,7 +483,6 @@ def run_batched(args, rank, world, local):
     from mosaic_gpu import job
 
     lib = capi.load()
-    ctx = capi.Context(local)
     t0 = time.perf_counter()
     specs, mats, thumbs = job.batched_workload(n=args.batched_mosaics, seed=20251203 + 7919 * rank,
                                                allocator=lib.mg_host_alloc)
@@ -516,11 +575,9 @@ def run_batched(args, rank, world, local):
             "e2e": {"value": n / e2e_s, "unit": "mosaics/s", "ms_per_step": 1000 * e2e_s,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clk}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     batch.close()
     pal.close()
-    ctx.close()
+    return line
 
 
 class _Arena:
@@ -537,6 +594,7 @@ class _Arena:
         addr = lib.mg_host_alloc(nbytes)
         if not addr:
             raise MemoryError(f"pinned arena of {nbytes} bytes")
+        self.lib, self.addr = lib, addr
         self.buf = np.ctypeslib.as_array(C.cast(addr, C.POINTER(C.c_uint8)), shape=(nbytes,))
         self.n, self.head = nbytes, 0
         self.live = deque()
@@ -562,6 +620,12 @@ class _Arena:
             self.live.append((start, start + size))
             self.head = start + size
             return self.buf[start:start + size]
+
+    def close(self):
+        self.buf = None
+        if self.addr:
+            self.lib.mg_host_free(self.addr)
+            self.addr = None
 
     def release(self):
         with self.cv:
@@ -625,6 +689,16 @@ def _serve(server, pool, stream, arrivals, arena, tile, keep=()):
 
 
 def run_served(args, rank, world, local):
+    from mosaic_gpu import _capi as capi
+
+    ctx = capi.Context(local)
+    line = measure_served(args, rank, world, local, ctx)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def measure_served(args, rank, world, local, ctx):
     """The served stream: Poisson arrivals of mixed-size requests (cells
     log-uniform 500..50 000 at 4:3, 24 px per cell, max usage 5, weight 0.25,
     colour 0.4, 2000 iterations x 4 chains) over one resident palette of 20 000
@@ -641,7 +715,6 @@ def run_served(args, rank, world, local):
     from mosaic_gpu import job
 
     lib = capi.load()
-    ctx = capi.Context(local)
     seed = 20251203 + 7919 * rank
     t0 = time.perf_counter()
     pool, mats, thumbs = job.served_workload(n_targets=args.served_pool, seed=seed, allocator=lib.mg_host_alloc,
@@ -724,9 +797,142 @@ def run_served(args, rank, world, local):
             "e2e": {"value": value, "unit": "mosaics/s", "ms_per_step": 1000.0 * sat_n / value,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clk, "cpu_baseline": cpu}
+    pal.close()
+    arena.close()
+    return line
+
+
+def measure_large(args, local, ctx, steps: int = 3):
+    """The large single mosaic at full size (7680x5760 target, 128 blobs; 5000
+    materials 128x128; 179x134 cells; max usage 8; 64 chains x 100 000
+    iterations; 32x32 tiles): the device-resident plan timed per stage with CUDA
+    events (L2 flushed between steps), and the figures that configuration is
+    quoted on -- GB/s of the two Lab reductions and of the composite, and
+    k-nearest candidates (cells x palette) per second.  The cell reduction runs
+    beside the material reduction inside the plan, so it is also timed alone
+    here on the resident target (mg_cells_lab_noalloc on the same stream)."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from mosaic_gpu import _capi as capi
+    from mosaic_gpu import job
+
+    lib = capi.load()
+    dev = torch.device("cuda", local)
+    t0 = time.perf_counter()
+    inp = workload_inputs("large", 0, allocator=lib.mg_host_alloc)
+    gen_s = time.perf_counter() - t0
+    cfg = inp.cfg
+    N = cfg.grid_w * cfg.grid_h
+    holder = job.RequestHolder(inp)
+    plan = job.Plan(ctx, holder)
+    stream = torch.cuda.ExternalStream(lib.mg_ctx_stream(ctx.h), device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(3):
+        plan.run()
+    capi.check(lib.mg_ctx_sync(ctx.h))
+    res, grid, image = plan.read()
+    P = res.palette_size
+    sel_px = int(sum(int(w) * int(h) for w, h in zip(inp.mats.w, inp.mats.h)))  # 1:1 materials: all kept
+    clocks = ClockSampler(local)
+    clocks.start()
+    times, stages = [], []
+    for i in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xFF)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+        plan.run()
+        with torch.cuda.stream(stream):
+            b.record(stream)
+        stages.append(plan.stage_ms())
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    # the cell reduction alone, device-resident target
+    cw, ch = cfg.target_w // cfg.grid_w, cfg.target_h // cfg.grid_h
+    d_img = torch.from_numpy(np.ascontiguousarray(inp.target)).to(dev)
+    d_lab = torch.empty((N, 4), dtype=torch.float32, device=dev)
+    d_rgb = torch.empty((N, 4), dtype=torch.uint8, device=dev)
+    cell_ms = []
+    with torch.cuda.stream(stream):
+        for i in range(4):
+            flush.fill_(i & 0xFF)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            capi.check(lib.mg_cells_lab_noalloc(C.c_void_p(d_img.data_ptr()), cfg.target_w, cfg.target_h,
+                                                3 * cfg.target_w, cfg.grid_w, cfg.grid_h,
+                                                C.c_void_p(d_lab.data_ptr()), C.c_void_p(d_rgb.data_ptr()),
+                                                C.c_void_p(lib.mg_ctx_stream(ctx.h))))
+            b.record(stream)
+            torch.cuda.synchronize()
+            if i:
+                cell_ms.append(a.elapsed_time(b))
+    clk = clocks.stop()
+    # end to end from pinned host buffers
+    out_img = np.ctypeslib.as_array(C.cast(lib.mg_host_alloc(image.nbytes), C.POINTER(C.c_uint8)),
+                                    shape=(image.nbytes,)).reshape(image.shape)
+    out_grid = np.zeros(N, np.int32)
+    job.generate(ctx, holder, out_img, out_grid)
+    e2e = []
+    for _ in range(2):
+        t1 = time.perf_counter()
+        _, g2, im2 = job.generate(ctx, holder, out_img, out_grid)
+        e2e.append(time.perf_counter() - t1)
+    same = bool(np.array_equal(g2, grid) and np.array_equal(im2, image))
+    plan.close()
+    peaks, peak_kind = read_peaks()
+    hbm = peaks["hbm_gbs"]
+    st = np.mean(stages, axis=0)
+    step_ms = float(np.mean(times))
+    alg = algorithmic(inp, P, sel_px)
+    cell_bytes = 3 * cw * ch * N + 20 * N
+    cms = float(np.mean(cell_ms))
+
+    def gbs(nbytes, ms):
+        v = nbytes / (ms / 1000.0) / 1e9
+        return {"gbs": round(v, 1), "frac_of_measured_hbm": round(v / hbm, 4), "ms": round(ms, 4), "bytes": int(nbytes)}
+
+    tw, th = inp.tile
+    out = {"metric": METRIC, "value": N / (step_ms / 1000.0), "unit": "tiles/s", "ms_per_step": step_ms,
+           "steps": steps, "config": bench_config(cfg, len(inp.mats), P, (tw, th), 1),
+           "stages_ms": {k: round(float(v), 4) for k, v in zip(STAGES + ["total"], st)},
+           "material_lab": gbs(alg["palette_lab"], float(st[0])),
+           "cell_lab": {**gbs(cell_bytes, cms), "what": "cell reduction alone on the resident target (it overlaps "
+                                                      "the material reduction inside the step)"},
+           "composite": gbs(alg["composite"], float(st[6])),
+           "similarity": gbs(alg["similarity"], float(st[1])),
+           "nearest": {"candidates_per_s": N * P / (float(st[3]) / 1000.0), "ms": round(float(st[3]), 4),
+                       "what": "cells x palette per second of the k-nearest stage (the bucket-grid search "
+                               "computes far fewer distances than that)"},
+           "greedy_us_per_cell": round(1000.0 * float(st[4]) / N, 4),
+           "anneal_proposals_per_s": cfg.chains * cfg.iterations / (float(st[5]) / 1000.0),
+           "e2e": {"value": N / float(np.mean(e2e)), "unit": "tiles/s", "ms_per_step": 1000.0 * float(np.mean(e2e)),
+                   "h2d_bytes_per_step": int(inp.target.nbytes + 3 * sel_px + P * tw * th * 3),
+                   "d2h_bytes_per_step": int(out_img.nbytes + out_grid.nbytes), "matches_device_run": same},
+           "peak_source": peak_kind, "input_generation_s": round(gen_s, 2), "clocks": clk}
+    if not args.no_cpu_baseline:
+        import oracle.binding as ob
+
+        cores = os.cpu_count() or 1
+        tc = time.perf_counter()
+        ob.generate(inp, threads=cores)
+        dt = time.perf_counter() - tc
+        out["cpu_baseline"] = {"value": N / dt, "unit": "tiles/s", "cores": cores, "kind": "port",
+                               "sample": "one full large job on the C++ restatement of the reference path"}
+    return out
+
+
+def run_large(args, rank, world, local):
+    from mosaic_gpu import _capi as capi
+
+    ctx = capi.Context(local)
+    line = measure_large(args, local, ctx, steps=args.steps)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    pal.close()
     ctx.close()
 
 
@@ -739,6 +945,8 @@ def main():
         run_batched(args, rank, world, local)
     elif args.workload == "served":
         run_served(args, rank, world, local)
+    elif args.workload == "large-figures":
+        run_large(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 
