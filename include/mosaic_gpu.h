@@ -170,6 +170,19 @@ int mg_ctx_set_nearest_method(mg_ctx* ctx, int method);
 #define MG_SCORING_GUI 1
 int mg_ctx_set_scoring(mg_ctx* ctx, int scoring);
 
+/* No counterpart in the reference (which has no device waits): fault
+ * injection for tests of the timeout path.  Every wait inside this library's
+ * kernels is bounded; a wait that runs out makes the kernel give up, and the
+ * call reports MG_ERR_TIMEOUT ("a bounded wait inside a kernel ran out")
+ * instead of hanging the GPU.  After this call the next `walks` greedy walks
+ * on this context in the three-CTA form (mg_place_greedy, mg_generate,
+ * mg_plan_run; rows of at least 8 cells, palettes of at most 65535) run with
+ * their candidate records withheld and a short wait limit, so the walker's
+ * wait for its first record runs out within about a millisecond: the call
+ * returns MG_ERR_TIMEOUT, the walk's grid is left empty (-1), and the context
+ * and its plans stay usable.  0 cancels. */
+int mg_ctx_inject_walk_timeout(mg_ctx* ctx, int walks);
+
 /* ---- adjacency ------------------------------------------------------------------ */
 /* adjacency.rs:63-88 calculate_penalty for n (candidate, x, y) triples
  * (cxy: n*3 ints) against one grid; out: n floats (weighted). */

@@ -287,6 +287,13 @@ int mg_ctx_set_nearest_method(mg_ctx* ctx, int method) {
   return MG_OK;
 }
 
+int mg_ctx_inject_walk_timeout(mg_ctx* ctx, int walks) {
+  if (!ctx) return fail(MG_ERR_ARG, "null context");
+  if (walks < 0) return fail(MG_ERR_ARG, "negative walk count");
+  ctx->inject_walk_timeouts = walks;
+  return MG_OK;
+}
+
 int mg_ctx_set_scoring(mg_ctx* ctx, int scoring) {
   if (!ctx) return fail(MG_ERR_ARG, "null context");
   if (scoring != MG_SCORING_CLI && scoring != MG_SCORING_GUI) return fail(MG_ERR_ARG, "unknown scoring");
@@ -577,8 +584,10 @@ int mg_place_greedy(mg_ctx* ctx, const float* palette_lab, int p, const float* c
   GreedyJob job{ctx->out0.as<uint32_t>(), ctx->out1.as<float>(), d_grid, gw, gh, k,
                 (uint32_t)cfg->max_usage_per_image, cfg->adjacency_penalty_weight, d_resets, nullptr};
   MG_CHECK(upload(ctx, ctx->regions, &job, sizeof(job)));
+  const bool inject = ctx->inject_walk_timeouts > 0;
+  if (inject) --ctx->inject_walk_timeouts;
   MG_CHECK(launch_greedy(ctx->in0.as<float4>(), p, ctx->regions.as<GreedyJob>(), 1, k, gw, n,
-                         ctx->sums.as<uint32_t>(), ctx->err.as<uint32_t>(), ctx->stream));
+                         ctx->sums.as<uint32_t>(), ctx->err.as<uint32_t>(), ctx->stream, false, inject));
   MG_CUDA(cudaMemcpyAsync(grid_out, d_grid, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
   int resets = 0;
   MG_CUDA(cudaMemcpyAsync(&resets, d_resets, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1051,8 +1060,10 @@ int plan_run(mg_plan* pl) {
   MG_CUDA(cudaEventRecord(pl->ev[4], s));
   // [4] greedy placement
   if (P > 0) {
+    const bool inject = pl->ctx->inject_walk_timeouts > 0;
+    if (inject) --pl->ctx->inject_walk_timeouts;
     MG_CHECK(launch_greedy(pl->pal_lab.as<float4>(), P, pl->greedy_job.as<GreedyJob>(), 1, pl->k, pl->gw, N,
-                           pl->usage.as<uint32_t>(), pl->err.as<uint32_t>(), s));
+                           pl->usage.as<uint32_t>(), pl->err.as<uint32_t>(), s, false, inject));
   } else {
     MG_CUDA(cudaMemsetAsync(pl->grid_greedy.p, 0xFF, sizeof(int32_t) * N, s));
   }
@@ -1143,7 +1154,10 @@ int plan_read(mg_plan* pl, mg_result* res) {
     MG_CUDA(cudaMemset(ctx->err.p, 0, 4));
     return fail(MG_ERR_TIMEOUT, "a bounded wait inside a kernel ran out");
   }
-  if (h_words[1]) return fail(MG_ERR_TIMEOUT, "a bounded wait inside a kernel ran out");
+  if (h_words[1]) {
+    MG_CUDA(cudaMemset(pl->err.p, 0, 4));  // reported once; the plan can run again
+    return fail(MG_ERR_TIMEOUT, "a bounded wait inside a kernel ran out");
+  }
   resets = (int)h_words[0];
   if (pl->run_sa) {
     bc = (int)h_words[3];

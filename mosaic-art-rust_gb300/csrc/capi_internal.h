@@ -13,6 +13,7 @@ struct mg_ctx {
   mg_plan* gen_plan = nullptr;
   int nearest_method = mg::kNearestAuto;  // MG_NEAREST_*
   int scoring = 0;                        // MG_SCORING_*
+  int inject_walk_timeouts = 0;           // mg_ctx_inject_walk_timeout: walks left to fail on purpose
   mg::LabIndex nn_index;                  // grid of the last single-call palette
 };
 

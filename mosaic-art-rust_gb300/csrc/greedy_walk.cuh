@@ -290,8 +290,11 @@ __device__ __forceinline__ void greedy_walk(const float4* __restrict__ pal, int 
     y = yn;
   }
   if (aborted) {
-    // Give in-flight copies a bounded chance to land before the CTA exits.
+    // Give in-flight copies a bounded chance to land before the CTA exits, and
+    // leave every cell empty so the stages after the walk read no stale index.
     for (int b = 0; b < kStageBufs; ++b) mbar_wait_bounded(&bars[b], 0, 1u << 16);
+    for (int i = lane; i < n; i += 32) J.grid[i] = -1;
+    if (lane == 0 && J.n_resets) *J.n_resets = 0;
     return;
   }
   __syncwarp();

@@ -66,7 +66,8 @@ constexpr int kWarps = 32;                  // per CTA
 constexpr int kScoutCtas = 2;               // CTAs 1..kScoutCtas of the cluster
 constexpr int kScouts = kWarps * kScoutCtas;  // every warp of the scout CTAs
 constexpr uint32_t kInvalidEpoch = 0xFFFFFFFFu;
-constexpr uint32_t kWalkPolls = 1u << 24;
+constexpr uint32_t kWalkPolls = 1u << 24;      // the walker's bounded wait for a record
+constexpr uint32_t kInjectedWalkPolls = 1u << 12;  // ... when a timeout is injected (well under a millisecond)
 constexpr uint32_t kScoutPolls = 1u << 22;  // polls of about 1 us each
 constexpr int kScoutLead = 80;             // records built at most this many cells ahead
 constexpr int kCostChunk = 2048;  // cells per pass of the final cost sum
@@ -389,9 +390,11 @@ __device__ inline WalkerLayout walker_layout(uint8_t* smem, int gw, int n, int p
 // (The layout is recomputed here rather than passed by reference: a struct
 // whose address escapes would turn the walker's shared-memory pointers into
 // generic ones.)
+// withhold: build the records but never publish them (an injected fault: the
+// walker's wait for the first record then runs out).
 template <bool kWindow, bool kRing>
 __device__ bool scout_cells(int s, const GreedyJob& J, const float4* __restrict__ pal, int p, uint8_t* smem,
-                            ScoutStage& S, int R, uint32_t* err) {
+                            ScoutStage& S, int R, uint32_t* err, bool withhold) {
   const int lane = threadIdx.x & 31;
   const int gw = J.gw, k = J.k, n = gw * J.gh;
   const WalkerLayout L = walker_layout(smem, gw, n, p, R, kRing);
@@ -531,14 +534,15 @@ __device__ bool scout_cells(int s, const GreedyJob& J, const float4* __restrict_
     }
     fence_cluster();
     __syncwarp();
-    if (lane == 0) st_release_cluster(r_seq + 4u * slot, (uint32_t)(c + 1));
+    if (lane == 0 && !withhold) st_release_cluster(r_seq + 4u * slot, (uint32_t)(c + 1));
   }
   return true;
 }
 
 template <bool kLabSmem, bool kRing>
 __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps * 32)
-    greedy_pair_kernel(const float4* __restrict__ pal, int p, const GreedyJob* __restrict__ jobs, uint32_t* err) {
+    greedy_pair_kernel(const float4* __restrict__ pal, int p, const GreedyJob* __restrict__ jobs, uint32_t* err,
+                       uint32_t walk_polls, uint32_t withhold) {
   extern __shared__ __align__(128) uint8_t smem[];
   const GreedyJob J = jobs[blockIdx.x / (1 + kScoutCtas)];
   const uint32_t rank = cluster_ctarank();
@@ -564,7 +568,8 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
     // ---- the scouts, then (CTA 1) the final cost of the walk
     ScoutStage* stage = reinterpret_cast<ScoutStage*>(smem);
     float* terms = reinterpret_cast<float*>(smem + (size_t)kWarps * sizeof(ScoutStage));
-    bool ok = scout_cells<!kLabSmem, kRing>((int)(rank - 1) * kWarps + warp, J, pal, p, smem, stage[warp], R, err);
+    bool ok = scout_cells<!kLabSmem, kRing>((int)(rank - 1) * kWarps + warp, J, pal, p, smem, stage[warp], R, err,
+                                            withhold != 0u);
     if (rank > 1) {
       cluster_sync_all();
       return;
@@ -669,7 +674,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
       }
       if (c < ready_until) return true;
       if (!block) return false;
-      if (++polls > kWalkPolls || ld_volatile_u32(&ctrl[kAbort])) {
+      if (++polls > walk_polls || ld_volatile_u32(&ctrl[kAbort])) {
         aborted = true;
         return false;
       }
@@ -871,6 +876,9 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
       atomicOr(err, kErrTimeout);
       *reinterpret_cast<volatile uint32_t*>(&ctrl[kAbort]) = 1u;
     }
+    // every cell empty, so the stages after the walk read no stale index
+    for (int i = lane; i < n; i += 32) J.grid[i] = -1;
+    if (lane == 0 && J.n_resets) *J.n_resets = 0;
   } else {
     // the placed grid in global memory (every lane's stores visible) before the
     // completion the scout CTA waits for
@@ -899,7 +907,8 @@ bool greedy_scouted_fits(int gw, int n, int p) {
 }
 
 int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_jobs, int k, int max_gw,
-                  int max_cells, uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream, bool one_warp) {
+                  int max_cells, uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream, bool one_warp,
+                  bool inject_timeout) {
   if (n_jobs <= 0) return MG_OK;
   if (k < 1 || k > 100) return fail(MG_ERR_ARG, "candidate count must be in 1..100");
   constexpr size_t kMaxSmem = 220 * 1024;
@@ -929,10 +938,15 @@ int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_job
       const bool lab_smem = form == 0 || form == 2, ring = form >= 2;
       const size_t bytes = pair_smem_bytes(max_gw, max_cells, p, lab_smem, ring);
       const unsigned grid = (1 + kScoutCtas) * n_jobs;
-      if (form == 0) greedy_pair_kernel<true, false><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
-      else if (form == 1) greedy_pair_kernel<false, false><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
-      else if (form == 2) greedy_pair_kernel<true, true><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
-      else greedy_pair_kernel<false, true><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err);
+      const uint32_t polls = inject_timeout ? kInjectedWalkPolls : kWalkPolls, hold = inject_timeout ? 1u : 0u;
+      if (form == 0)
+        greedy_pair_kernel<true, false><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err, polls, hold);
+      else if (form == 1)
+        greedy_pair_kernel<false, false><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err, polls, hold);
+      else if (form == 2)
+        greedy_pair_kernel<true, true><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err, polls, hold);
+      else
+        greedy_pair_kernel<false, true><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err, polls, hold);
       g_launches += 1;
       MG_CUDA(cudaGetLastError());
       return MG_OK;

@@ -122,9 +122,13 @@ struct GreedyJob {
 };
 // Candidate arrays must hold ceil(N/16)*16 rows (the walk streams 16 rows per copy).
 // one_warp: every job walks in the one-warp form (else the three-CTA form when
-// every job allows it).
+// every job allows it).  inject_timeout (three-CTA form only): the scouts
+// withhold their records and the walker waits at most a few thousand polls,
+// so its bounded wait runs out -- an injected fault for tests.  A walk that
+// gives up sets kErrTimeout in *err and leaves every cell of its grid empty.
 int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_jobs, int k, int max_gw,
-                  int max_cells, uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream, bool one_warp = false);
+                  int max_cells, uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream, bool one_warp = false,
+                  bool inject_timeout = false);
 inline size_t padded_cells(int n) { return ((size_t)n + 15) / 16 * 16; }
 // Whether a mosaic of gw x (n / gw) cells over a palette of p walks in the
 // three-CTA form (else one warp).

@@ -131,6 +131,7 @@ SIGNATURES = [
     ("mg_ctx_sync", C.c_int, [C.c_void_p]),
     ("mg_ctx_stream", C.c_void_p, [C.c_void_p]),
     ("mg_ctx_set_nearest_method", C.c_int, [C.c_void_p, C.c_int]),
+    ("mg_ctx_inject_walk_timeout", C.c_int, [C.c_void_p, C.c_int]),
     ("mg_ctx_set_scoring", C.c_int, [C.c_void_p, C.c_int]),
     ("mg_host_alloc", C.c_void_p, [C.c_size_t]),
     ("mg_host_free", None, [C.c_void_p]),

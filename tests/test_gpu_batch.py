@@ -97,9 +97,10 @@ def test_batch_against_oracle(ctx, orc):
         cfg = job.JobConfig("b", w, h, 0, len(mats), 24, 0, gw, gh, kw.get("max_usage", 3), kw.get("weight", 0.25),
                             kw.get("strength", 0.4), kw.get("iterations", 1000), kw.get("chains", 1), TILE, TILE,
                             enable_optimization=kw.get("enable_opt", True), seed=20251203)
-        ref = orc.generate(job.Inputs(cfg, tgts[i], mats, thumbs), threads=8) if i == 2 else None
-        if ref is not None:
-            assert np.array_equal(grids[i], ref["grid"]) and np.array_equal(images[i], ref["image"])
+        ref = orc.generate(job.Inputs(cfg, tgts[i], mats, thumbs), threads=8, stream=i)  # request i: Philox stream i
+        assert np.array_equal(grids[i], ref["grid"]), i
+        assert np.array_equal(images[i], ref["image"]), i
+        assert results[i].best_chain == ref["best_chain"] and results[i].final_cost == ref["final_cost"], i
     pal.close()
 
 

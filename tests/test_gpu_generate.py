@@ -45,6 +45,32 @@ def test_generate_scaled_workloads(ctx, orc, cfg_kw):
     _compare(ctx, orc, _small(name, **cfg_kw))
 
 
+def test_generate_full_large_workload(ctx, orc):
+    """The large single mosaic at full size: 7680x5760 target (128 blobs), 5000
+    materials of 128x128, 179x134 = 23 986 cells of 42x42 pixels, max usage 8,
+    64 chains x 100 000 iterations, 32x32 output tiles (5728x4288 image).  The
+    grid and the winning chain bit-exact, every chain's final cost equal to the
+    CPU replay of its Philox stream, pixels within 1 LSB."""
+    import os
+
+    from mosaic_gpu import job
+
+    cfg = job.WORKLOADS["large"]
+    inp, res, grid, image, ref = _compare(ctx, orc, cfg, threads=os.cpu_count() or 8)
+    assert grid.shape == (134, 179) and image.shape == (4288, 5728, 3)
+    assert res.palette_size == 5000
+    assert np.float32(res.best_cost) == np.float32(ref["best_cost"])
+    # every chain (not only the winner): the 64 chains run again from the greedy grid
+    # through mg_optimize; each chain's initial, final and best cost equal the oracle's
+    g, best, per, chain_grids = ctx.optimize(ref["pal_lab"], ref["greedy_grid"], cfg.iterations, chains=cfg.chains,
+                                             seed=cfg.seed, stream=0)
+    # no square material passes the 4:3 filter, so every one is kept in input order (main.rs:215-253):
+    # palette indices are material indices
+    assert best.best_chain == ref["best_chain"] and np.array_equal(g, ref["grid"])
+    got = np.array([[r.initial_cost, r.final_cost, r.best_cost] for r in per], np.float32)
+    assert np.array_equal(got.view(np.uint32), ref["chain_res"][:cfg.chains].view(np.uint32))
+
+
 def test_generate_edge_cases(ctx, orc):
     # every material rejected (max_materials 0) -> nothing placed, black output
     cfg = _small("small", target_w=64, target_h=48, n_materials=10, material_side=16, grid_w=8, grid_h=6,

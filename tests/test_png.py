@@ -11,6 +11,7 @@ rounded).  Files the library writes are inflated here with zlib and checked
 row by row against the image they encode (check_rows).  Defective files must
 fail with MG_ERR_ARG, never crash.
 """
+import os
 import struct
 import zlib
 from pathlib import Path
@@ -354,12 +355,13 @@ def test_batch_decode(capi):
 @pytest.mark.parametrize("name", ["examples/mosaic.png", "docs/public/hero-image.png"])
 def test_reference_example_images(capi, name):
     """The PNG files shipped with mosaic-art-rust (an RGBA mosaic the tool made,
-    3840x2160, and an RGB image in 32 IDAT chunks), where the source tree is
-    present: decoded, then checked row by row against the files' own filtered
-    data as zlib inflates it."""
-    path = Path("/root/reference") / name
-    if not path.exists():
-        pytest.skip("mosaic-art-rust source tree not present")
+    3840x2160, and an RGB image in 32 IDAT chunks), when MOSAIC_ART_RUST_SRC
+    names a copy of its source tree: decoded, then checked row by row against
+    the files' own filtered data as zlib inflates it."""
+    root = os.environ.get("MOSAIC_ART_RUST_SRC")
+    if not root or not (Path(root) / name).exists():
+        pytest.skip("set MOSAIC_ART_RUST_SRC to a mosaic-art-rust source tree to check its example images")
+    path = Path(root) / name
     data = path.read_bytes()
     rgb = capi.png_decode(data)
     check_rows(data, rgb)
