@@ -376,10 +376,12 @@ int mg_batch_read(mg_batch* batch, int i, mg_result* res);
 /* [0] cell statistics, [1] k-nearest, [2] walks + chains, [3] adjust +
  * composite, [4] total; ms of the last run. */
 int mg_batch_stage_ms(mg_batch* batch, float* ms, int cap);
-/* The launch shapes the autotuner picked (nearest_chunk 0: the palette's
- * bucket grid serves the k-nearest search, which has no chunk size;
- * workers_per_cta is 0: every chain runs as one CTA of the chain kernel). */
-int mg_batch_tuning(mg_batch* batch, int* cells_per_cta, int* nearest_chunk, int* workers_per_cta);
+/* The launch shapes the autotuner picked: cells per CTA of the cell
+ * statistics, and the palette chunk of the k-nearest scan (0: the palette's
+ * bucket grid serves the search, which has no chunk size).  Chains are not a
+ * tuned shape: each annealing chain is one 4-warp CTA and an SM runs as many
+ * chain CTAs as fit, so putting several chains in one CTA would serialise them. */
+int mg_batch_tuning(mg_batch* batch, int* cells_per_cta, int* nearest_chunk);
 int mg_batch_launches(mg_batch* batch);
 int mg_batch_destroy(mg_batch* batch);
 /* One batch from host buffers to host buffers (targets in pinned host memory

@@ -631,11 +631,10 @@ int mg_batch_stage_ms(mg_batch* b, float* ms, int cap) {
   return nout;
 }
 
-int mg_batch_tuning(mg_batch* b, int* cells_per_cta, int* nearest_chunk, int* workers_per_cta) {
+int mg_batch_tuning(mg_batch* b, int* cells_per_cta, int* nearest_chunk) {
   if (!b) return fail(MG_ERR_ARG, "null batch");
   if (cells_per_cta) *cells_per_cta = b->cells_warps;
   if (nearest_chunk) *nearest_chunk = b->pal->index.g > 0 ? 0 : b->nn_chunk;
-  if (workers_per_cta) *workers_per_cta = 0;  // chains run one CTA each, no persistent workers
   return b->tuned ? MG_OK : fail(MG_ERR_STATE, "batch has not run");
 }
 

@@ -111,7 +111,7 @@ SIGNATURES = [
     ("mg_batch_run", C.c_int, [C.c_void_p]),
     ("mg_batch_read", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     ("mg_batch_stage_ms", C.c_int, [C.c_void_p, _f32p, C.c_int]),
-    ("mg_batch_tuning", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("mg_batch_tuning", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("mg_batch_launches", C.c_int, [C.c_void_p]),
     ("mg_batch_destroy", C.c_int, [C.c_void_p]),
     ("mg_generate_batch", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Mosaic), C.c_int, C.c_void_p]),

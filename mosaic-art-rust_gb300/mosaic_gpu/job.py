@@ -279,9 +279,9 @@ class Batch:
         return ms[:max(n, 0)]
 
     def tuning(self):
-        a, b, c = C.c_int(), C.c_int(), C.c_int()
-        capi.check(self.ctx.lib.mg_batch_tuning(self.h, C.byref(a), C.byref(b), C.byref(c)))
-        return {"cells_per_cta": a.value, "nearest_chunk": b.value, "workers_per_cta": c.value}
+        a, b = C.c_int(), C.c_int()
+        capi.check(self.ctx.lib.mg_batch_tuning(self.h, C.byref(a), C.byref(b)))
+        return {"cells_per_cta": a.value, "nearest_chunk": b.value}
 
     def launches(self) -> int:
         return int(self.ctx.lib.mg_batch_launches(self.h))

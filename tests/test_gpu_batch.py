@@ -74,7 +74,6 @@ def test_batch_equals_single_mosaic_path(ctx):
             assert r.n_resets == res.n_resets and r.palette_size == res.palette_size
     tune = batch.tuning()
     assert tune["cells_per_cta"] in (4, 8) and tune["nearest_chunk"] in (0, 1024, 2048, 4096)
-    assert tune["workers_per_cta"] == 0
     assert len(batch.stage_ms()) == 5 and batch.launches() > 0
     # one-shot batch from host buffers
     results, grids, images = job.generate_batch(ctx, pal, reqs)
