@@ -5,7 +5,10 @@
 //
 // The brightness/contrast step of adjust_pixel is a function of one byte, so
 // the CTA tabulates it for the tile's adjustment (256 entries) and each pixel
-// looks its three channels up; the HSV part (adjust_from_bc) stays per pixel.
+// looks its three channels up; the HSV part stays per pixel, as adjust_unit
+// (mg_math.h: adjust_from_bc rearranged for channels in [0, 1] without
+// changing a result -- fewer comparisons, selects and clamps, the division by
+// 60 as a multiply and one correction, the output a truncating conversion).
 // With tile widths a multiple of 4, four pixels of a tile row are 12 bytes,
 // 4-byte aligned in the thumbnail and in the output, and move as three 32-bit
 // words.
@@ -44,7 +47,7 @@ __device__ __forceinline__ void composite_tile(const uint8_t* __restrict__ src, 
         for (int px = 0; px < 4; ++px) {
           const int b0 = 3 * px, b1 = b0 + 1, b2 = b0 + 2;
           uint8_t o0, o1, o2;
-          adjust_from_bc(a, s_bc[byte_of(w[b0 >> 2], b0 & 3)], s_bc[byte_of(w[b1 >> 2], b1 & 3)],
+          adjust_unit(a, s_bc[byte_of(w[b0 >> 2], b0 & 3)], s_bc[byte_of(w[b1 >> 2], b1 & 3)],
                          s_bc[byte_of(w[b2 >> 2], b2 & 3)], o0, o1, o2);
           o[b0 >> 2] |= (uint32_t)o0 << (8 * (b0 & 3));
           o[b1 >> 2] |= (uint32_t)o1 << (8 * (b1 & 3));
@@ -70,7 +73,7 @@ __device__ __forceinline__ void composite_tile(const uint8_t* __restrict__ src, 
       o0 = s[0];
       o1 = s[1];
       o2 = s[2];
-      if (adjust) adjust_from_bc(a, s_bc[o0], s_bc[o1], s_bc[o2], o0, o1, o2);
+      if (adjust) adjust_unit(a, s_bc[o0], s_bc[o1], s_bc[o2], o0, o1, o2);
     }
     d[0] = o0;
     d[1] = o1;

@@ -401,6 +401,76 @@ MG_HD void adjust_from_bc(const Adjust& a, float c0, float c1, float c2, uint8_t
   o2 = as_u8(rclamp(MG_MUL(c2, 255.0f), 0.0f, 255.0f));
 }
 
+// x / 60, correctly rounded, as a multiply and one FMA correction: equal to
+// the division for every float in [0x1p-120, 360] (checked exhaustively); the
+// division itself below that.
+MG_HD float div60(float x) {
+  if (x < 0x1p-120f) return MG_DIV(x, 60.0f);
+  const float q = MG_MUL(x, 1.0f / 60.0f);
+  return MG_FMA(MG_FMA(-q, 60.0f, x), 1.0f / 60.0f, q);
+}
+
+// adjust_from_bc for channels in [0, 1] (the brightness/contrast table's
+// values: clamped, possibly -0), rearranged without changing a result:
+//  - rgb_to_hsv's clamps cannot bind: channels >= 0 (or -0, which the max
+//    with 0 keeps), the value is the largest channel <= 1, the saturation
+//    d / max is in [0, 1] as d = fl(max - min) <= max;
+//  - the hue reaching hsv_to_rgb is in [-0, 360] (fmod_360 of the shifted hue,
+//    then + 360 below zero), so its normalisation is the hue itself inside
+//    (0, 360) and 0 at the ends (0 - 0 * 360, -0 - (-0) * 360, 360 - 360);
+//  - pos / 60 through div60;
+//  - the sector tests h in [i, i + 1) become the truncated index of h >= 0
+//    (index 6 for h = 6 takes the last sector's branch, as before);
+//  - each channel red + m is >= 0 (red in {c, x, 0}, x = c (1 - t) with t in
+//    [0, 1], m = v - c >= 0 as c = v s <= v), so only the clamp at 1 can bind;
+//  - the output v * 255 of a channel in [-0, 1] lies in [0, 255] and is never
+//    NaN, so `as u8` is a truncating conversion.
+MG_HD uint32_t unit_to_u8(float v) {
+#if defined(__CUDA_ARCH__)
+  return __float2uint_rz(__fmul_rn(v, 255.0f));
+#else
+  return (uint32_t)(v * 255.0f);
+#endif
+}
+MG_HD float min1(float v) { return v > 1.0f ? 1.0f : v; }
+MG_HD void adjust_unit(const Adjust& a, float c0, float c1, float c2, uint8_t& o0, uint8_t& o1, uint8_t& o2) {
+  if (a.hue_shift != 0.0f || a.saturation != 1.0f) {
+    float mx, mn, sep, coeff;
+    if (c0 > c1) { mx = c0; mn = c1; sep = MG_SUB(c1, c2); coeff = 0.0f; }
+    else { mx = c1; mn = c0; sep = MG_SUB(c2, c0); coeff = 2.0f; }
+    if (c2 > mx) { mx = c2; sep = MG_SUB(c0, c1); coeff = 4.0f; }
+    else if (c2 < mn) { mn = c2; }
+    float hh = 0.0f, s = 0.0f;
+    if (mx != mn) {
+      const float d = MG_SUB(mx, mn);
+      hh = MG_MUL(MG_ADD(MG_DIV(sep, d), coeff), 60.0f);
+      s = MG_DIV(d, mx);
+    }
+    float rem = fmod_360(MG_ADD(hh, a.hue_shift));
+    if (rem < 0.0f) rem = MG_ADD(rem, 360.0f);
+    const float pos = (rem > 0.0f && rem < 360.0f) ? rem : 0.0f;
+    const float ss = rclamp(MG_MUL(s, a.saturation), 0.0f, 1.0f);
+    const float v = mx;
+    const float c = MG_MUL(v, ss);
+    const float h = div60(pos);
+    const float hm2 = MG_SUB(h, MG_MUL(MG_FLOOR(MG_MUL(h, 0.5f)), 2.0f));
+    float t = MG_SUB(hm2, 1.0f);
+    t = t < 0.0f ? -t : t;
+    const float x = MG_MUL(c, MG_SUB(1.0f, t));
+    const float m = MG_SUB(v, c);
+    const uint32_t bit = 1u << (uint32_t)(int)h;  // h in [0, 6]
+    const float red = (bit & 0x12u) ? x : ((bit & 0x0Cu) ? 0.0f : c);
+    const float green = (bit & 0x09u) ? x : ((bit & 0x06u) ? c : 0.0f);
+    const float blue = (bit & 0x03u) ? 0.0f : ((bit & 0x18u) ? c : x);
+    c0 = min1(MG_ADD(red, m));
+    c1 = min1(MG_ADD(green, m));
+    c2 = min1(MG_ADD(blue, m));
+  }
+  o0 = (uint8_t)unit_to_u8(c0);
+  o1 = (uint8_t)unit_to_u8(c1);
+  o2 = (uint8_t)unit_to_u8(c2);
+}
+
 // color_adjustment.rs:53-87 adjust_pixel.  r, g, b are the channels as v/255.
 MG_HD void adjust_pixel(const Adjust& a, float r, float g, float b, uint8_t& o0, uint8_t& o1, uint8_t& o2) {
   adjust_from_bc(a, brightness_contrast(r, a.brightness, a.contrast), brightness_contrast(g, a.brightness, a.contrast),

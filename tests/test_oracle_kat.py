@@ -80,6 +80,31 @@ def test_kernel_lab_arithmetic_equals_the_oracle_for_every_colour(orc):
     assert r.returncode == 0 and "differing 0" in r.stdout, r.stdout + r.stderr
 
 
+def test_composite_adjustment_equals_the_definition_for_every_colour():
+    """The composite adjusts each pixel with mg_math.h's adjust_unit: the
+    definition adjust_from_bc (which the oracle restates) rearranged for
+    channels in [0, 1].  For twelve tile adjustments (hue shifts of both signs
+    and the clamps' ends, saturation 0..2, brightness and contrast changes)
+    and all 2^24 byte triples through each one's brightness/contrast table,
+    the two give the same output bytes (tests/cpp/adjust_equiv.cpp)."""
+    import shutil
+    import subprocess
+    import tempfile
+    from pathlib import Path
+
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    repo = Path(__file__).resolve().parents[1]
+    with tempfile.TemporaryDirectory() as d:
+        exe = Path(d) / "adjust_equiv"
+        r = subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math",
+                            str(repo / "tests" / "cpp" / "adjust_equiv.cpp"), "-o", str(exe)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "differing 0" in r.stdout, r.stdout + r.stderr
+
+
 # ---- main.rs:866-889 calculate_average_rgb -----------------------------------------------
 def test_avg_rgb_red(orc):
     assert tuple(orc.avg_rgb(solid(10, 10, (255, 0, 0)))) == (255, 0, 0)
