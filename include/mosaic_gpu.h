@@ -86,6 +86,21 @@ int mg_cells_lab(mg_ctx* ctx, const uint8_t* img, int w, int h, int64_t stride, 
  * by the caller.  Results equal mg_cells_lab's bit for bit. */
 int mg_cells_lab_noalloc(const uint8_t* d_img, int w, int h, int64_t stride, int gw, int gh, float* d_lab4,
                          uint8_t* d_rgb4, void* stream);
+/* How missing thumbnails are made on the device (mg_request / mg_palette_desc
+ * with thumbnails NULL, and mg_resize).  MG_THUMB_LANCZOS3 (the default) is
+ * main.rs:710-738 resize_image: fast_image_resize's default, a Lanczos3
+ * convolution, here as the published convolution resampler it follows (taps
+ * at pixel centres, support 3 x the downscale factor, weights normalised and
+ * rounded to 22-bit fixed point, a horizontal then a vertical pass through an
+ * 8-bit intermediate; exact integer arithmetic).  MG_THUMB_AREA: the mean of
+ * each output pixel's source box, rounded.  Applies to plans, mg_generate
+ * calls and palettes set up on the context afterwards. */
+#define MG_THUMB_LANCZOS3 0
+#define MG_THUMB_AREA 1
+int mg_ctx_set_thumbnail_filter(mg_ctx* ctx, int filter);
+/* main.rs:710-738 resize_image: one RGB8 image (stride bytes per row, 0 ->
+ * 3*w) to dw x dh with the context's thumbnail filter; out: dh x dw x 3. */
+int mg_resize(mg_ctx* ctx, const uint8_t* rgb, int w, int h, int64_t stride, int dw, int dh, uint8_t* out);
 /* main.rs:193-208, 244-253 (process_tile -> calculate_average_lab for each
  * material) in one launch.  lab_out: n*3; avg_rgb_out (nullable): n*3. */
 int mg_images_lab(mg_ctx* ctx, const uint8_t* const* imgs, const int* w, const int* h,
@@ -263,7 +278,8 @@ typedef struct mg_request {
   const int* material_h;
   const int64_t* material_stride;  /* nullable -> 3*w */
   const uint8_t* thumbnails;       /* nullable: n_materials x tile_h x tile_w x 3, the resized tiles
-                                      (main.rs:549); NULL -> area-average resize on the device */
+                                      (main.rs:549); NULL -> resized on the device with the
+                                      context's thumbnail filter (Lanczos3 by default) */
   int tile_w, tile_h;              /* output tile size; 0 -> cell size (main.rs:495-496) */
   int grid_w, grid_h;              /* main.rs:37-43 */
   int max_materials;               /* main.rs:45-47 */
@@ -331,7 +347,7 @@ typedef struct mg_palette_desc {
   const int* material_w;
   const int* material_h;
   const int64_t* material_stride;  /* nullable -> 3*w */
-  const uint8_t* thumbnails;       /* nullable: n x tile_h x tile_w x 3; NULL -> area-average resize */
+  const uint8_t* thumbnails;       /* nullable: n x tile_h x tile_w x 3; NULL -> the context's thumbnail filter */
   int tile_w, tile_h;              /* output tile size of every mosaic using the palette (> 0) */
   float target_aspect;             /* load_tiles selection (main.rs:166-261) for this target aspect */
   float aspect_tolerance;

@@ -72,6 +72,8 @@ struct mg_plan {
       cand_dist, grid_greedy, resets, init_cost, greedy_job, chain_grids, chain_res, anneal_job, final_grid,
       finals_ptr, best_chain, adj, out, sums, cell_sums, err, usage, gather_src;
   LabIndex index;  // bucket grid over pal_lab for the k-nearest search (when large)
+  ResizePlan resize;  // Lanczos3 tables of the selected materials (thumbnails made on the device)
+  int thumb_filter = MG_THUMB_LANCZOS3;
   // pinned host staging of the small read-backs (grid, counters, chain results)
   void* h_read = nullptr;
   size_t h_read_cap = 0;
@@ -263,6 +265,7 @@ int mg_ctx_destroy(mg_ctx* ctx) {
                     &ctx->err, &ctx->lab_consts})
     b->release();
   ctx->nn_index.release();
+  ctx->resize.release();
   if (ctx->side) {
     cudaStreamSynchronize(ctx->side);
     cudaStreamDestroy(ctx->side);
@@ -285,6 +288,39 @@ int mg_ctx_set_nearest_method(mg_ctx* ctx, int method) {
     return fail(MG_ERR_ARG, "unknown nearest method");
   ctx->nearest_method = method;
   return MG_OK;
+}
+
+int mg_ctx_set_thumbnail_filter(mg_ctx* ctx, int filter) {
+  if (!ctx) return fail(MG_ERR_ARG, "null context");
+  if (filter != MG_THUMB_LANCZOS3 && filter != MG_THUMB_AREA) return fail(MG_ERR_ARG, "unknown thumbnail filter");
+  ctx->thumb_filter = filter;
+  return MG_OK;
+}
+
+int mg_resize(mg_ctx* ctx, const uint8_t* rgb, int w, int h, int64_t stride, int dw, int dh, uint8_t* out) {
+  MG_CHECK(check_ctx(ctx));
+  if (stride == 0) stride = 3ll * w;
+  if (!valid_image(rgb, w, h, stride) || !out || dw <= 0 || dh <= 0) return fail(MG_ERR_ARG, "invalid image or size");
+  const void* dev = device_view_or_device(rgb);
+  const uint8_t* src = static_cast<const uint8_t*>(dev);
+  if (!dev) {
+    MG_CHECK(ctx->in2.ensure((size_t)stride * (h - 1) + 3ull * w));
+    MG_CUDA(cudaMemcpy2DAsync(ctx->in2.p, (size_t)stride, rgb, (size_t)stride, 3ull * w, (size_t)h,
+                              cudaMemcpyHostToDevice, ctx->stream));
+    src = ctx->in2.as<uint8_t>();
+  }
+  const size_t bytes = 3ull * dw * dh;
+  MG_CHECK(ctx->out2.ensure(bytes));
+  const Region r{0, w, h, stride};
+  if (ctx->thumb_filter == MG_THUMB_LANCZOS3) {
+    MG_CHECK(ctx->resize.build(&r, 1, dw, dh, ctx->stream));
+    MG_CHECK(launch_resize(src, ctx->resize, ctx->out2.as<uint8_t>(), ctx->stream));
+  } else {
+    MG_CHECK(upload(ctx, ctx->regions, &r, sizeof(r)));
+    MG_CHECK(launch_thumbnails(src, ctx->regions.as<Region>(), 1, dw, dh, ctx->out2.as<uint8_t>(), ctx->stream));
+  }
+  MG_CUDA(cudaMemcpyAsync(out, ctx->out2.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return finish(ctx);
 }
 
 int mg_ctx_inject_walk_timeout(mg_ctx* ctx, int walks) {
@@ -797,6 +833,7 @@ void plan_release(mg_plan* pl) {
                     &pl->err})
     b->release();
   pl->index.release();
+  pl->resize.release();
   if (pl->events)
     for (auto& e : pl->ev) cudaEventDestroy(e);
   if (pl->download_done) {
@@ -930,6 +967,9 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r, bool zero_copy) {
   const size_t tb = 3ull * pl->tw * pl->th;
   MG_CHECK(pl->thumbs.ensure(tb * std::max(P, 1)));
   pl->device_thumbs = r->thumbnails == nullptr;
+  pl->thumb_filter = ctx->thumb_filter;
+  if (pl->device_thumbs && pl->thumb_filter == MG_THUMB_LANCZOS3)
+    MG_CHECK(pl->resize.build(pl->h_regions.data(), P, pl->tw, pl->th, s));
   if (!pl->device_thumbs) {
     const void* thdev = pl->zero_copy && P > 0 ? device_view(r->thumbnails) : nullptr;
     if (thdev) {
@@ -1029,7 +1069,9 @@ int plan_run(mg_plan* pl) {
   MG_CUDA(cudaEventRecord(pl->ev[8], s2));
   // [0] palette ingestion: thumbnails (when not given), material Lab, thumbnail means
   if (P > 0) {
-    if (pl->device_thumbs)
+    if (pl->device_thumbs && pl->thumb_filter == MG_THUMB_LANCZOS3)
+      MG_CHECK(launch_resize(nullptr, pl->resize, pl->thumbs.as<uint8_t>(), s));
+    else if (pl->device_thumbs)
       MG_CHECK(launch_thumbnails(nullptr, pl->regions.as<Region>(), P, pl->tw, pl->th,
                                  pl->thumbs.as<uint8_t>(), s));
     int64_t maxpx = 0;

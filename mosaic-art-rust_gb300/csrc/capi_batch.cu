@@ -30,6 +30,7 @@ struct mg_palette {
   std::vector<Region> h_regions;
   DevBuf mats, regions, thumbs, thumb_regions, pal_lab, thumb_rgb, sim, sums;
   LabIndex index;  // bucket grid over pal_lab for the k-nearest search (when large)
+  ResizePlan resize;  // Lanczos3 tables when the thumbnails are made on the device
   bool has_sim = false;
   size_t device_bytes = 0;
 };
@@ -108,6 +109,9 @@ int palette_setup(mg_palette* pl, mg_ctx* ctx, const mg_palette_desc* d) {
     for (int i = 0; i < P; ++i)
       MG_CUDA(cudaMemcpyAsync(pl->thumbs.as<uint8_t>() + tb * i, d->thumbnails + tb * pl->selected[i], tb,
                               cudaMemcpyHostToDevice, s));
+  } else if (P > 0 && ctx->thumb_filter == MG_THUMB_LANCZOS3) {
+    MG_CHECK(pl->resize.build(pl->h_regions.data(), P, pl->tw, pl->th, s));
+    MG_CHECK(launch_resize(pl->mats.as<uint8_t>(), pl->resize, pl->thumbs.as<uint8_t>(), s));
   } else if (P > 0) {
     MG_CHECK(launch_thumbnails(pl->mats.as<uint8_t>(), pl->regions.as<Region>(), P, pl->tw, pl->th,
                                pl->thumbs.as<uint8_t>(), s));
@@ -572,6 +576,7 @@ int mg_palette_destroy(mg_palette* pal) {
   release({&pal->mats, &pal->regions, &pal->thumbs, &pal->thumb_regions, &pal->pal_lab, &pal->thumb_rgb, &pal->sim,
            &pal->sums});
   pal->index.release();
+  pal->resize.release();
   delete pal;
   return MG_OK;
 }

@@ -14,6 +14,8 @@ struct mg_ctx {
   int nearest_method = mg::kNearestAuto;  // MG_NEAREST_*
   int scoring = 0;                        // MG_SCORING_*
   int inject_walk_timeouts = 0;           // mg_ctx_inject_walk_timeout: walks left to fail on purpose
+  int thumb_filter = 0;                   // MG_THUMB_*: how missing thumbnails are made
+  mg::ResizePlan resize;                  // mg_resize's tables
   mg::LabIndex nn_index;                  // grid of the last single-call palette
 };
 

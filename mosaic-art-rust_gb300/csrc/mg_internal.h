@@ -73,6 +73,22 @@ cudaError_t upload_lab_consts(cudaStream_t stream);
 // dst + i*bytes (16-byte vector copies when aligned).
 int launch_gather(const int64_t* src, int n, size_t bytes, uint8_t* dst, cudaStream_t stream);
 
+// Lanczos3 thumbnails of regions at tw x th (k_resize.cu): ResizePlan::build
+// makes the weight tables of the regions' sizes on the host and uploads them
+// (once per palette or plan); launch_resize runs the two passes.
+struct ResizeImage {
+  int64_t offset, stride;
+  int32_t w, h;
+  int32_t htab, vtab;  // table offsets; -1: the dimension keeps its size
+};
+struct ResizePlan {
+  DevBuf tabs, images, inter;
+  int n = 0, tw = 0, th = 0, max_h = 0;
+  int build(const Region* regions, int n_images, int tw, int th, cudaStream_t s);
+  void release();
+};
+int launch_resize(const uint8_t* base, const ResizePlan& rp, uint8_t* out, cudaStream_t stream);
+
 // Area-average thumbnails of regions at tw x th.
 int launch_thumbnails(const uint8_t* base, const Region* regions, int n, int tw, int th, uint8_t* out,
                       cudaStream_t stream);

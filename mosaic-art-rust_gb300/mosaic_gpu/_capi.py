@@ -15,6 +15,7 @@ import numpy as np
 from .build import BUILD
 
 MG_OK, MG_ERR_ARG, MG_ERR_OOM, MG_ERR_CUDA, MG_ERR_TIMEOUT, MG_ERR_BUDGET, MG_ERR_STATE = range(7)
+MG_THUMB_LANCZOS3, MG_THUMB_AREA = 0, 1
 MG_SIM_FULL, MG_SIM_TRIANGULAR = 0, 1
 MG_NEAREST_AUTO, MG_NEAREST_SCAN, MG_NEAREST_GRID = 0, 1, 2
 MG_SCORING_CLI, MG_SCORING_GUI = 0, 1
@@ -131,6 +132,8 @@ SIGNATURES = [
     ("mg_ctx_sync", C.c_int, [C.c_void_p]),
     ("mg_ctx_stream", C.c_void_p, [C.c_void_p]),
     ("mg_ctx_set_nearest_method", C.c_int, [C.c_void_p, C.c_int]),
+    ("mg_ctx_set_thumbnail_filter", C.c_int, [C.c_void_p, C.c_int]),
+    ("mg_resize", C.c_int, [C.c_void_p, _u8p, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_int, _u8p]),
     ("mg_ctx_inject_walk_timeout", C.c_int, [C.c_void_p, C.c_int]),
     ("mg_ctx_set_scoring", C.c_int, [C.c_void_p, C.c_int]),
     ("mg_host_alloc", C.c_void_p, [C.c_size_t]),
@@ -261,6 +264,14 @@ class Context:
         check(self.lib.mg_cells_lab(self.h, ptr(img, C.c_uint8), w, h, img.strides[0], gw, gh,
                                     ptr(lab, C.c_float), ptr(rgb, C.c_uint8)))
         return lab, rgb
+
+    def resize(self, img: np.ndarray, dw: int, dh: int) -> np.ndarray:
+        """main.rs:710-738 resize_image on the device (the context's thumbnail filter)."""
+        img = np.ascontiguousarray(img, dtype=np.uint8)
+        h, w = img.shape[:2]
+        out = np.zeros((dh, dw, 3), np.uint8)
+        check(self.lib.mg_resize(self.h, ptr(img, C.c_uint8), w, h, img.strides[0], dw, dh, ptr(out, C.c_uint8)))
+        return out
 
     def images_lab(self, imgs: list[np.ndarray]):
         n = len(imgs)

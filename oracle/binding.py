@@ -46,6 +46,7 @@ _SIGS = [
     ("orc_lab_pixels_q", None, [_u8p, C.c_long, _i32p]),
     ("orc_lab_mean_spec", None, [_u8p, C.c_int, C.c_int, C.c_long, _f32p]),
     ("orc_avg_rgb", None, [_u8p, C.c_int, C.c_int, C.c_long, _u8p]),
+    ("orc_resize_lanczos3", None, [_u8p, C.c_int, C.c_int, C.c_long, C.c_int, C.c_int, _u8p]),
     ("orc_cells", C.c_int, [_u8p, C.c_int, C.c_int, C.c_long, C.c_int, C.c_int, _f32p, _u8p]),
     ("orc_is_aspect_ratio_match", C.c_int, [C.c_float, C.c_float, C.c_float]),
     ("orc_select_palette", C.c_int, [_ip, _ip, C.c_int, C.c_float, C.c_float, C.c_int, _ip]),
@@ -214,6 +215,15 @@ def anneal(pal, grid, iters, t0=100.0, decay=0.99995, seed=0x5EED5EED5EED, strea
     lib().orc_anneal_ex(p(pal, C.c_float), pal.shape[0], p(g, C.c_int32), gw, gh, iters, t0, decay, seed, stream,
                         chain, 1 if greedy_only else 0, 1 if libm_exp else 0, p(res, C.c_float), p(cnt, C.c_int64))
     return g, res, cnt
+
+
+def resize_lanczos3(img, dw: int, dh: int):
+    """main.rs:710-738 resize_image (fast_image_resize's default Lanczos3, restated)."""
+    img = np.ascontiguousarray(img, np.uint8)
+    h, w = img.shape[:2]
+    out = np.zeros((dh, dw, 3), np.uint8)
+    lib().orc_resize_lanczos3(p(img, C.c_uint8), w, h, img.strides[0], dw, dh, p(out, C.c_uint8))
+    return out
 
 
 def optimal_adjustment(tile_rgb, target_rgb, strength):

@@ -355,6 +355,89 @@ void orc_lab_mean_spec(const uint8_t* rgb, int w, int h, long stride, float out[
   for (int c = 0; c < 3; ++c) out[c] = ((float)s[c] / n) * kInvQ;
 }
 
+// main.rs:710-738 resize_image: fast_image_resize's default Lanczos3
+// convolution, restated from the published resampler it follows (Pillow's
+// ImagingResample): per output coordinate of a dimension in -> out, taps at
+// pixel centres over a support of 3 * max(in / out, 1), lanczos3 weights
+// normalised to sum 1 and rounded half away from zero to 22-bit fixed point;
+// the horizontal pass into an 8-bit image first, then the vertical pass; a
+// dimension that keeps its size is copied.
+namespace {
+double resize_sinc(double x) {
+  if (x == 0.0) return 1.0;
+  x = x * M_PI;
+  return std::sin(x) / x;
+}
+double resize_lanczos3(double x) {
+  if (x < -3.0 || x >= 3.0) return 0.0;
+  return resize_sinc(x) * resize_sinc(x / 3.0);
+}
+struct Taps {
+  std::vector<int> first, count;
+  std::vector<std::vector<int32_t>> k;
+};
+Taps resize_taps(int in, int out) {
+  Taps T;
+  const double scale = (double)in / (double)out;
+  const double fs = std::max(scale, 1.0);
+  const double support = 3.0 * fs;
+  for (int o = 0; o < out; ++o) {
+    const double centre = (o + 0.5) * scale;
+    const int lo = std::max(0, (int)(centre - support + 0.5));
+    const int hi = std::min(in, (int)(centre + support + 0.5));
+    std::vector<double> w;
+    double sum = 0.0;
+    for (int i = lo; i < hi; ++i) {
+      w.push_back(resize_lanczos3((i - centre + 0.5) / fs));
+      sum += w.back();
+    }
+    std::vector<int32_t> q;
+    for (double v : w) {
+      if (sum != 0.0) v /= sum;
+      q.push_back((int32_t)(v < 0.0 ? v * 4194304.0 - 0.5 : v * 4194304.0 + 0.5));
+    }
+    T.first.push_back(lo);
+    T.count.push_back(hi - lo);
+    T.k.push_back(q);
+  }
+  return T;
+}
+uint8_t resize_clip(int32_t acc) {
+  const int32_t v = acc >> 22;
+  return (uint8_t)(v < 0 ? 0 : (v > 255 ? 255 : v));
+}
+}  // namespace
+
+void orc_resize_lanczos3(const uint8_t* rgb, int w, int h, long stride, int dw, int dh, uint8_t* out) {
+  // horizontal: h rows of dw pixels
+  std::vector<uint8_t> mid((size_t)h * dw * 3);
+  if (dw == w) {
+    for (int y = 0; y < h; ++y) std::memcpy(&mid[(size_t)y * dw * 3], rgb + (long)y * stride, (size_t)w * 3);
+  } else {
+    const Taps T = resize_taps(w, dw);
+    for (int y = 0; y < h; ++y)
+      for (int x = 0; x < dw; ++x)
+        for (int c = 0; c < 3; ++c) {
+          int32_t acc = 1 << 21;
+          for (int t = 0; t < T.count[x]; ++t) acc += T.k[x][t] * rgb[(long)y * stride + 3L * (T.first[x] + t) + c];
+          mid[((size_t)y * dw + x) * 3 + c] = resize_clip(acc);
+        }
+  }
+  // vertical: dh rows
+  if (dh == h) {
+    std::memcpy(out, mid.data(), mid.size());
+    return;
+  }
+  const Taps T = resize_taps(h, dh);
+  for (int y = 0; y < dh; ++y)
+    for (int x = 0; x < dw; ++x)
+      for (int c = 0; c < 3; ++c) {
+        int32_t acc = 1 << 21;
+        for (int t = 0; t < T.count[y]; ++t) acc += T.k[y][t] * mid[((size_t)(T.first[y] + t) * dw + x) * 3 + c];
+        out[((size_t)y * dw + x) * 3 + c] = resize_clip(acc);
+      }
+}
+
 // main.rs:687-708 calculate_average_rgb: u64 sums, truncating division.
 void orc_avg_rgb(const uint8_t* rgb, int w, int h, long stride, uint8_t out[3]) {
   uint64_t s[3] = {0, 0, 0};

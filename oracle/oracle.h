@@ -35,6 +35,7 @@ void  orc_lab_consts(float lut[256], float ms[9], float k[3]);
 void  orc_lab_pixels_q(const uint8_t* rgb, long n, int32_t* q);
 void  orc_lab_mean_spec(const uint8_t* rgb, int w, int h, long stride, float out[3]);
 void  orc_avg_rgb(const uint8_t* rgb, int w, int h, long stride, uint8_t out[3]);
+void  orc_resize_lanczos3(const uint8_t* rgb, int w, int h, long stride, int dw, int dh, uint8_t* out);
 int   orc_cells(const uint8_t* img, int w, int h, long stride, int gw, int gh,
                 float* lab_out, uint8_t* avg_rgb_out);
 int   orc_is_aspect_ratio_match(float img_aspect, float target_aspect, float tol);

@@ -113,10 +113,16 @@ def test_device_thumbnails_equal_host_thumbnails(ctx, orc):
 
     cfg = _small("recommended", target_w=240, target_h=180, n_materials=60, material_side=40, grid_w=10, grid_h=9,
                  tile_w=9, tile_h=7, iterations=200, chains=2)
-    inp = job.make_inputs(cfg)
+    from mosaic_gpu import _capi
+
+    inp = job.make_inputs(cfg)  # host thumbnails: the area rule of the synthetic generator
     res_a, grid_a, img_a = job.generate(ctx, job.RequestHolder(inp))
     inp_dev = job.Inputs(cfg, inp.target, inp.mats, None)
-    res_b, grid_b, img_b = job.generate(ctx, job.RequestHolder(inp_dev))
+    assert ctx.lib.mg_ctx_set_thumbnail_filter(ctx.h, _capi.MG_THUMB_AREA) == _capi.MG_OK
+    try:
+        res_b, grid_b, img_b = job.generate(ctx, job.RequestHolder(inp_dev))
+    finally:
+        ctx.lib.mg_ctx_set_thumbnail_filter(ctx.h, _capi.MG_THUMB_LANCZOS3)
     assert np.array_equal(grid_a, grid_b) and np.array_equal(img_a, img_b)
 
 
