@@ -145,6 +145,27 @@ size_t mg_png_encode_bound(int w, int h);
 int mg_png_encode(const uint8_t* rgb, int w, int h, int64_t stride, int level, int threads, uint8_t* out,
                   size_t cap, size_t* len);
 
+/* main.rs:172-185, 492, 548: load_tiles also takes jpg/jpeg materials, opened
+ * by image::open (zune-jpeg 0.4.18).  This library's own decoder (ITU-T T.81,
+ * JFIF): sequential Huffman JPEG with 8-bit samples (baseline and extended),
+ * grey or YCbCr with sampling factors 1 or 2, restart intervals; progressive,
+ * lossless and arithmetic-coded files fail with MG_ERR_ARG.  The inverse DCT
+ * is the FP32 separable form of T.81 A.3.3, chroma is upsampled by
+ * replication and converted with the JFIF equations, so pixels may differ
+ * from zune-jpeg's by a few levels (not pinned: that crate cannot run here).
+ * Same conventions as the PNG calls: no context, any thread, RGB8 out. */
+int mg_jpeg_info(const uint8_t* data, size_t n, int* w, int* h);
+int mg_jpeg_decode(const uint8_t* data, size_t n, uint8_t* out, int64_t stride);
+/* PNG or JPEG, told apart by the file's signature (image::open's format
+ * detection for the two formats read here). */
+int mg_image_info(const uint8_t* data, size_t n, int* w, int* h);
+int mg_image_decode(const uint8_t* data, size_t n, uint8_t* out, int64_t stride);
+/* A material folder of PNG and JPEG files on up to `threads` host threads
+ * (<= 0: one per hardware thread); status (nullable) receives each file's
+ * code; returns the first failure's code (its message names the file). */
+int mg_image_decode_batch(const uint8_t* const* data, const size_t* n, int count, uint8_t* const* out,
+                          const int64_t* stride, int threads, int* status);
+
 /* ---- similarity database --------------------------------------------------------- */
 /* similarity.rs:69-82 build_similarities (+ similarity.rs:141-146
  * calculate_lab_distance) on the device.  layout MG_SIM_FULL or

@@ -1,0 +1,602 @@
+// io_jpeg.cpp -- JPEG files at the input end of the path (host code), and
+// decoding by file signature.
+//
+// Reference: main.rs:172-185 load_tiles accepts png, jpg, jpeg and webp
+// materials and main.rs:492 / 548 open them with image::open (+ to_rgb8);
+// for JPEG that is zune-jpeg 0.4.18 behind image 0.25.6.  This decoder is the
+// library's own, from ITU-T T.81 (the JPEG standard) and JFIF 1.02:
+//   * sequential DCT with Huffman coding, 8-bit samples (SOF0 baseline, SOF1
+//     extended); progressive (SOF2), lossless and arithmetic-coded files are
+//     refused with MG_ERR_ARG;
+//   * one component (grey, replicated to RGB) or three (YCbCr per JFIF);
+//     sampling factors 1 or 2 in each direction; interleaved and
+//     one-component scans; 8- and 16-bit quantisation tables; restart
+//     intervals;
+//   * the inverse DCT is the separable 8-point form of T.81 A.3.3 in FP32
+//     with a cosine table computed in FP64; chroma is upsampled by
+//     replication; YCbCr -> RGB with the JFIF equations; each sample rounded
+//     to nearest and clamped.
+// zune-jpeg's own integer IDCT, its upsampling filter and its colour
+// conversion are not pinned (the crate is not here to run): decoded pixels
+// may differ from the reference's by a few levels; the tests hold this
+// decoder to +-1 of a float64 restatement of the same steps and to the exact
+// pixels of files whose content survives the codec unchanged.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/mosaic_gpu.h"
+
+namespace mg {
+void set_error(const std::string& msg);
+}
+
+namespace {
+
+struct Err {
+  int code = MG_OK;
+  std::string msg;
+  bool bad(const std::string& m) {
+    code = MG_ERR_ARG;
+    msg = "JPEG: " + m;
+    return false;
+  }
+};
+
+const uint8_t kZigzag[64] = {0,  1,  8,  16, 9,  2,  3,  10, 17, 24, 32, 25, 18, 11, 4,  5,
+                             12, 19, 26, 33, 40, 48, 41, 34, 27, 20, 13, 6,  7,  14, 21, 28,
+                             35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51,
+                             58, 59, 52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63};
+
+// A Huffman table (T.81 C / F.2.2.3): canonical codes from the code-length
+// counts; decoding with a 9-bit lookup and the canonical limits beyond it.
+struct Huff {
+  static constexpr int kFast = 9;
+  uint16_t fast[1 << kFast];  // (length << 8 | symbol) + 1, 0: longer than kFast bits
+  int maxcode[18];
+  int valptr[17];
+  int mincode[17];
+  uint8_t vals[256];
+  bool present = false;
+  bool build(const uint8_t counts[16], const uint8_t* symbols, int nsym) {
+    std::memset(fast, 0, sizeof(fast));
+    int code = 0, k = 0;
+    for (int len = 1; len <= 16; ++len) {
+      valptr[len] = k;
+      mincode[len] = code;
+      code += counts[len - 1];
+      k += counts[len - 1];
+      if (code > (1 << len)) return false;  // over-subscribed
+      maxcode[len] = counts[len - 1] ? code - 1 : -1;
+      code <<= 1;
+    }
+    maxcode[17] = 0x7FFFFFFF;
+    if (k != nsym) return false;
+    std::memcpy(vals, symbols, (size_t)nsym);
+    // fast table
+    code = 0;
+    k = 0;
+    for (int len = 1; len <= kFast; ++len) {
+      for (int i = 0; i < counts[len - 1]; ++i, ++k, ++code) {
+        const int shift = kFast - len;
+        for (int j = 0; j < (1 << shift); ++j) fast[(code << shift) | j] = (uint16_t)(((len << 8) | vals[k]) + 1);
+      }
+      code <<= 1;
+    }
+    present = true;
+    return true;
+  }
+};
+
+// Entropy-coded data: bits MSB first, 0xFF 0x00 stuffing removed; a marker
+// ends the data (later reads give zero bits and flag an overrun).
+struct Bits {
+  const uint8_t* p;
+  const uint8_t* end;
+  uint64_t buf = 0;
+  int cnt = 0;
+  bool hit_marker = false;
+  int marker = 0;
+  int overrun = 0;  // bits fed past the data
+  void fill() {
+    while (cnt <= 56) {
+      int b = 0;
+      if (!hit_marker && p < end) {
+        b = *p;
+        if (b == 0xFF) {
+          const int nxt = p + 1 < end ? p[1] : -1;
+          if (nxt == 0x00) {
+            p += 2;
+          } else {
+            hit_marker = true;
+            marker = nxt;
+            b = 0;
+            overrun += 8;
+          }
+        } else {
+          ++p;
+        }
+      } else {
+        overrun += 8;
+      }
+      buf |= (uint64_t)b << (56 - cnt);
+      cnt += 8;
+    }
+  }
+  uint32_t get(int n) {  // n <= 16
+    if (n == 0) return 0;
+    if (cnt < n) fill();
+    const uint32_t v = (uint32_t)(buf >> (64 - n));
+    buf <<= n;
+    cnt -= n;
+    return v;
+  }
+  int decode(const Huff& h) {
+    if (cnt < 16) fill();
+    const uint16_t e = h.fast[buf >> (64 - Huff::kFast)];
+    if (e) {
+      const int len = (e - 1) >> 8;
+      buf <<= len;
+      cnt -= len;
+      return (e - 1) & 0xFF;
+    }
+    for (int len = Huff::kFast + 1; len <= 16; ++len) {
+      const int code = (int)(buf >> (64 - len));
+      if (code <= h.maxcode[len]) {
+        buf <<= len;
+        cnt -= len;
+        return h.vals[h.valptr[len] + code - h.mincode[len]];
+      }
+    }
+    return -1;
+  }
+  // bits consumed beyond the real data (zeros fed after a marker or the end)
+  bool past_end() const { return overrun > cnt; }
+  // At a restart boundary: drop the padding bits and step over marker RSTn
+  // (the reader stops at a marker without consuming it).
+  bool restart(int expect) {
+    buf = 0;
+    cnt = 0;
+    overrun = 0;
+    hit_marker = false;
+    const uint8_t* q = p;
+    while (q + 1 < end && !(q[0] == 0xFF && q[1] != 0x00 && q[1] != 0xFF)) ++q;
+    if (q + 1 >= end || q[1] != 0xD0 + expect) return false;
+    p = q + 2;
+    return true;
+  }
+};
+
+inline int extend(uint32_t v, int s) { return s == 0 ? 0 : (v < (1u << (s - 1)) ? (int)v - (1 << s) + 1 : (int)v); }
+
+struct Component {
+  int id = 0, h = 1, v = 1, tq = 0;
+  int td = 0, ta = 0;      // Huffman tables of the current scan
+  int bw = 0, bh = 0;      // blocks across / down, padded to whole MCUs
+  int pred = 0;            // DC prediction
+  std::vector<int16_t> coef;  // bw * bh blocks x 64, natural order, quantised
+};
+
+struct Decoder {
+  const uint8_t* d;
+  size_t n;
+  Err& err;
+  int width = 0, height = 0, ncomp = 0, hmax = 1, vmax = 1, mcux = 0, mcuy = 0;
+  bool have_frame = false;
+  int restart = 0;
+  uint16_t qt[4][64];
+  bool qt_set[4] = {false, false, false, false};
+  Huff dc[4], ac[4];
+  Component comp[3];
+  Decoder(const uint8_t* data, size_t size, Err& e) : d(data), n(size), err(e) {}
+
+  bool header_only(int* w, int* h) {
+    size_t pos = 0;
+    if (n < 4 || d[0] != 0xFF || d[1] != 0xD8) return err.bad("not a JPEG file");
+    pos = 2;
+    while (pos + 4 <= n) {
+      if (d[pos] != 0xFF) return err.bad("marker expected");
+      const int m = d[pos + 1];
+      if (m == 0xFF) {
+        ++pos;
+        continue;
+      }
+      const size_t len = (size_t)d[pos + 2] << 8 | d[pos + 3];
+      if (len < 2 || pos + 2 + len > n) return err.bad("segment runs past the end of the file");
+      if (m == 0xC0 || m == 0xC1 || m == 0xC2 || m == 0xC3) {
+        if (len < 8) return err.bad("short frame header");
+        *h = d[pos + 5] << 8 | d[pos + 6];
+        *w = d[pos + 7] << 8 | d[pos + 8];
+        if (*w <= 0 || *h <= 0) return err.bad("empty image (or a height given later by DNL, not supported)");
+        return true;
+      }
+      pos += 2 + len;
+    }
+    return err.bad("no frame header");
+  }
+
+  bool frame(const uint8_t* s, size_t len, int m) {
+    if (m == 0xC2 || m == 0xC6 || m == 0xCA || m == 0xCE) return err.bad("progressive JPEG is not supported");
+    if (m != 0xC0 && m != 0xC1) return err.bad("lossless, hierarchical or arithmetic-coded JPEG is not supported");
+    if (have_frame) return err.bad("second frame header");
+    if (len < 6) return err.bad("short frame header");
+    if (s[0] != 8) return err.bad("only 8-bit samples are supported");
+    height = s[1] << 8 | s[2];
+    width = s[3] << 8 | s[4];
+    ncomp = s[5];
+    if (width <= 0 || height <= 0) return err.bad("empty image (or a height given later by DNL, not supported)");
+    if (ncomp != 1 && ncomp != 3) return err.bad("only grey and three-component images are supported");
+    if (len < 6 + 3 * (size_t)ncomp) return err.bad("short frame header");
+    if ((int64_t)width * height > (1ll << 28)) return err.bad("image too large");
+    hmax = vmax = 1;
+    for (int i = 0; i < ncomp; ++i) {
+      Component& c = comp[i];
+      c.id = s[6 + 3 * i];
+      c.h = s[7 + 3 * i] >> 4;
+      c.v = s[7 + 3 * i] & 15;
+      c.tq = s[8 + 3 * i];
+      if (c.h < 1 || c.h > 2 || c.v < 1 || c.v > 2) return err.bad("sampling factors other than 1 and 2");
+      if (c.tq > 3) return err.bad("bad quantisation table index");
+      hmax = std::max(hmax, c.h);
+      vmax = std::max(vmax, c.v);
+    }
+    if (ncomp == 1) comp[0].h = comp[0].v = hmax = vmax = 1;  // a single component is never subsampled
+    mcux = (width + 8 * hmax - 1) / (8 * hmax);
+    mcuy = (height + 8 * vmax - 1) / (8 * vmax);
+    for (int i = 0; i < ncomp; ++i) {
+      Component& c = comp[i];
+      c.bw = mcux * c.h;
+      c.bh = mcuy * c.v;
+      c.coef.assign((size_t)c.bw * c.bh * 64, 0);
+    }
+    have_frame = true;
+    return true;
+  }
+
+  bool dqt(const uint8_t* s, size_t len) {
+    size_t i = 0;
+    while (i < len) {
+      const int pq = s[i] >> 4, tq = s[i] & 15;
+      if (tq > 3 || pq > 1) return err.bad("bad quantisation table");
+      const size_t need = 1 + 64 * (pq ? 2 : 1);
+      if (i + need > len) return err.bad("short quantisation table");
+      for (int k = 0; k < 64; ++k)
+        qt[tq][kZigzag[k]] = pq ? (uint16_t)(s[i + 1 + 2 * k] << 8 | s[i + 2 + 2 * k]) : s[i + 1 + k];
+      qt_set[tq] = true;
+      i += need;
+    }
+    return true;
+  }
+
+  bool dht(const uint8_t* s, size_t len) {
+    size_t i = 0;
+    while (i < len) {
+      if (i + 17 > len) return err.bad("short Huffman table");
+      const int tc = s[i] >> 4, th = s[i] & 15;
+      if (tc > 1 || th > 3) return err.bad("bad Huffman table");
+      int total = 0;
+      for (int k = 0; k < 16; ++k) total += s[i + 1 + k];
+      if (total > 256 || i + 17 + total > len) return err.bad("bad Huffman table");
+      if (!(tc ? ac[th] : dc[th]).build(s + i + 1, s + i + 17, total)) return err.bad("bad Huffman code lengths");
+      i += 17 + total;
+    }
+    return true;
+  }
+
+  // One block: DC difference and AC run/size codes (T.81 F.2.2), natural order.
+  bool block(Bits& b, Component& c, int16_t* out) {
+    const Huff& hd = dc[c.td];
+    const Huff& ha = ac[c.ta];
+    const int t = b.decode(hd);
+    if (t < 0 || t > 11) return err.bad("bad DC code");
+    c.pred += extend(b.get(t), t);
+    if (c.pred < -32768 || c.pred > 32767) return err.bad("DC value out of range");
+    out[0] = (int16_t)c.pred;
+    for (int k = 1; k < 64;) {
+      const int rs = b.decode(ha);
+      if (rs < 0) return err.bad("bad AC code");
+      const int r = rs >> 4, sz = rs & 15;
+      if (sz == 0) {
+        if (r == 15) {
+          k += 16;
+          continue;
+        }
+        break;  // end of block
+      }
+      k += r;
+      if (k > 63) return err.bad("AC coefficients run past the block");
+      out[kZigzag[k]] = (int16_t)extend(b.get(sz), sz);
+      ++k;
+    }
+    return true;
+  }
+
+  bool scan(const uint8_t* s, size_t len, size_t& pos) {
+    if (!have_frame) return err.bad("scan before the frame header");
+    if (len < 1) return err.bad("short scan header");
+    const int ns = s[0];
+    if (ns < 1 || ns > ncomp || len < 4 + 2 * (size_t)ns) return err.bad("bad scan header");
+    Component* sc[3];
+    for (int i = 0; i < ns; ++i) {
+      const int id = s[1 + 2 * i];
+      int j = 0;
+      while (j < ncomp && comp[j].id != id) ++j;
+      if (j == ncomp) return err.bad("scan names an unknown component");
+      sc[i] = &comp[j];
+      sc[i]->td = s[2 + 2 * i] >> 4;
+      sc[i]->ta = s[2 + 2 * i] & 15;
+      if (sc[i]->td > 3 || sc[i]->ta > 3 || !dc[sc[i]->td].present || !ac[sc[i]->ta].present)
+        return err.bad("scan uses a missing Huffman table");
+      sc[i]->pred = 0;
+    }
+    if (s[1 + 2 * ns] != 0 || s[2 + 2 * ns] != 63 || s[3 + 2 * ns] != 0)
+      return err.bad("spectral selection or successive approximation in a sequential scan");
+    // entropy-coded data
+    Bits b{d + pos, d + n};
+    int mx, my;
+    if (ns == 1) {  // one component: its own block grid (T.81 A.2.2), not padded to whole MCUs
+      mx = (int)std::ceil((double)width * sc[0]->h / hmax / 8.0);
+      my = (int)std::ceil((double)height * sc[0]->v / vmax / 8.0);
+    } else {
+      mx = mcux;
+      my = mcuy;
+    }
+    const int64_t units = (int64_t)mx * my;
+    int64_t left = restart;
+    int next_rst = 0;
+    for (int64_t u = 0; u < units; ++u) {
+      if (restart && left == 0) {
+        if (!b.restart(next_rst)) return err.bad("restart marker missing or out of order");
+        next_rst = (next_rst + 1) & 7;
+        for (int i = 0; i < ns; ++i) sc[i]->pred = 0;
+        left = restart;
+      }
+      if (ns == 1) {
+        Component& c = *sc[0];
+        const int bx = (int)(u % mx), by = (int)(u / mx);
+        if (!block(b, c, c.coef.data() + ((size_t)by * c.bw + bx) * 64)) return false;
+      } else {
+        const int ux = (int)(u % mx), uy = (int)(u / mx);
+        for (int i = 0; i < ns; ++i) {
+          Component& c = *sc[i];
+          for (int y = 0; y < c.v; ++y)
+            for (int x = 0; x < c.h; ++x) {
+              const int bx = ux * c.h + x, by = uy * c.v + y;
+              if (!block(b, c, c.coef.data() + ((size_t)by * c.bw + bx) * 64)) return false;
+            }
+        }
+      }
+      if (b.past_end()) return err.bad("entropy-coded data truncated");
+      if (restart) --left;
+    }
+    // continue after the scan's data at the next marker (RSTn and fill bytes skipped)
+    const uint8_t* q = b.p;
+    while (q + 1 < d + n && !(q[0] == 0xFF && q[1] != 0x00 && !(q[1] >= 0xD0 && q[1] <= 0xD7) && q[1] != 0xFF)) ++q;
+    pos = (size_t)(q - d);
+    return true;
+  }
+
+  bool parse() {
+    if (n < 4 || d[0] != 0xFF || d[1] != 0xD8) return err.bad("not a JPEG file");
+    size_t pos = 2;
+    bool scanned = false;
+    while (pos + 2 <= n) {
+      if (d[pos] != 0xFF) return err.bad("marker expected");
+      const int m = d[pos + 1];
+      if (m == 0xFF) {
+        ++pos;
+        continue;
+      }
+      if (m == 0xD9) break;  // EOI
+      if (m == 0xD8 || (m >= 0xD0 && m <= 0xD7) || m == 0x01) {
+        pos += 2;
+        continue;
+      }
+      if (pos + 4 > n) return err.bad("truncated segment");
+      const size_t len = (size_t)d[pos + 2] << 8 | d[pos + 3];
+      if (len < 2 || pos + 2 + len > n) return err.bad("segment runs past the end of the file");
+      const uint8_t* s = d + pos + 4;
+      const size_t sl = len - 2;
+      pos += 2 + len;
+      if (m >= 0xC0 && m <= 0xCF && m != 0xC4 && m != 0xC8 && m != 0xCC) {
+        if (!frame(s, sl, m)) return false;
+      } else if (m == 0xC4) {
+        if (!dht(s, sl)) return false;
+      } else if (m == 0xCC) {
+        return err.bad("arithmetic-coded JPEG is not supported");
+      } else if (m == 0xDB) {
+        if (!dqt(s, sl)) return false;
+      } else if (m == 0xDD) {
+        if (sl < 2) return err.bad("short restart interval");
+        restart = s[0] << 8 | s[1];
+      } else if (m == 0xDA) {
+        if (!scan(s, sl, pos)) return false;
+        scanned = true;
+      } else if (m == 0xDC) {
+        return err.bad("DNL (height defined later) is not supported");
+      }
+      // APPn, COM and the rest: skipped
+    }
+    if (!have_frame) return err.bad("no frame header");
+    if (!scanned) return err.bad("no scan");
+    for (int i = 0; i < ncomp; ++i)
+      if (!qt_set[comp[i].tq]) return err.bad("missing quantisation table");
+    return true;
+  }
+
+  // T.81 A.3.3 inverse DCT of one dequantised block, rows then columns, FP32,
+  // + 128, rounded to nearest, clamped.
+  static void idct(const int16_t* in, const uint16_t* q, uint8_t* out, int stride, const float (&cs)[8][8]) {
+    float t[64];
+    for (int u = 0; u < 64; ++u) t[u] = (float)in[u] * (float)q[u];
+    float r[64];
+    for (int y = 0; y < 8; ++y)  // 1-D over the horizontal frequency of each row
+      for (int x = 0; x < 8; ++x) {
+        float s = 0.0f;
+        for (int u = 0; u < 8; ++u) s += cs[x][u] * t[y * 8 + u];
+        r[y * 8 + x] = s;
+      }
+    for (int x = 0; x < 8; ++x)
+      for (int y = 0; y < 8; ++y) {
+        float s = 0.0f;
+        for (int v = 0; v < 8; ++v) s += cs[y][v] * r[v * 8 + x];
+        const float val = s + 128.0f;
+        const long iv = std::lrintf(val);
+        out[y * stride + x] = (uint8_t)(iv < 0 ? 0 : (iv > 255 ? 255 : iv));
+      }
+  }
+
+  bool output(uint8_t* out, int64_t stride) {
+    float cs[8][8];  // C(u)/2 cos((2x+1) u pi / 16)
+    for (int x = 0; x < 8; ++x)
+      for (int u = 0; u < 8; ++u)
+        cs[x][u] = (float)((u == 0 ? std::sqrt(0.5) : 1.0) * 0.5 * std::cos((2 * x + 1) * u * M_PI / 16.0));
+    std::vector<std::vector<uint8_t>> plane(ncomp);
+    for (int i = 0; i < ncomp; ++i) {
+      Component& c = comp[i];
+      const int pw = c.bw * 8, ph = c.bh * 8;
+      plane[i].assign((size_t)pw * ph, 0);
+      for (int by = 0; by < c.bh; ++by)
+        for (int bx = 0; bx < c.bw; ++bx)
+          idct(c.coef.data() + ((size_t)by * c.bw + bx) * 64, qt[c.tq], plane[i].data() + (size_t)by * 8 * pw + bx * 8,
+               pw, cs);
+    }
+    for (int y = 0; y < height; ++y) {
+      uint8_t* o = out + (int64_t)y * stride;
+      if (ncomp == 1) {
+        const uint8_t* p = plane[0].data() + (size_t)y * comp[0].bw * 8;
+        for (int x = 0; x < width; ++x) o[3 * x] = o[3 * x + 1] = o[3 * x + 2] = p[x];
+        continue;
+      }
+      const uint8_t* row[3];
+      int sx[3];
+      for (int i = 0; i < 3; ++i) {
+        const Component& c = comp[i];
+        const int yy = y * c.v / vmax;  // replication
+        row[i] = plane[i].data() + (size_t)yy * c.bw * 8;
+        sx[i] = hmax / c.h;
+      }
+      for (int x = 0; x < width; ++x) {
+        const float Y = row[0][x / sx[0]], cb = row[1][x / sx[1]] - 128.0f, cr = row[2][x / sx[2]] - 128.0f;
+        const float rgb[3] = {Y + 1.402f * cr, Y - 0.344136f * cb - 0.714136f * cr, Y + 1.772f * cb};
+        for (int c = 0; c < 3; ++c) {
+          const long iv = std::lrintf(rgb[c]);
+          o[3 * x + c] = (uint8_t)(iv < 0 ? 0 : (iv > 255 ? 255 : iv));
+        }
+      }
+    }
+    return true;
+  }
+};
+
+int jpeg_decode(const uint8_t* data, size_t n, uint8_t* out, int64_t stride, Err& e) {
+  if (!data || !out) return e.bad("null argument"), e.code;
+  Decoder dec(data, n, e);
+  if (!dec.parse()) return e.code;
+  if (stride < 3ll * dec.width) return e.bad("output stride below 3 * width"), e.code;
+  dec.output(out, stride);
+  return MG_OK;
+}
+
+bool is_jpeg(const uint8_t* d, size_t n) { return d && n >= 3 && d[0] == 0xFF && d[1] == 0xD8 && d[2] == 0xFF; }
+bool is_png(const uint8_t* d, size_t n) {
+  static const uint8_t sig[8] = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1A, '\n'};
+  return d && n >= 8 && std::memcmp(d, sig, 8) == 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mg_jpeg_info(const uint8_t* data, size_t n, int* w, int* h) {
+  Err e;
+  if (!data || !w || !h) {
+    mg::set_error("null argument");
+    return MG_ERR_ARG;
+  }
+  try {
+    Decoder dec(data, n, e);
+    if (!dec.header_only(w, h)) {
+      mg::set_error(e.msg);
+      return e.code;
+    }
+    return MG_OK;
+  } catch (const std::exception& x) {
+    mg::set_error(std::string("JPEG: ") + x.what());
+    return MG_ERR_OOM;
+  }
+}
+
+int mg_jpeg_decode(const uint8_t* data, size_t n, uint8_t* out, int64_t stride) {
+  Err e;
+  try {
+    const int rc = jpeg_decode(data, n, out, stride, e);
+    if (rc != MG_OK) mg::set_error(e.msg);
+    return rc;
+  } catch (const std::bad_alloc&) {
+    mg::set_error("JPEG: out of memory");
+    return MG_ERR_OOM;
+  } catch (const std::exception& x) {
+    mg::set_error(std::string("JPEG: ") + x.what());
+    return MG_ERR_ARG;
+  }
+}
+
+int mg_image_info(const uint8_t* data, size_t n, int* w, int* h) {
+  if (is_png(data, n)) return mg_png_info(data, n, w, h);
+  if (is_jpeg(data, n)) return mg_jpeg_info(data, n, w, h);
+  mg::set_error("neither a PNG nor a JPEG file");
+  return MG_ERR_ARG;
+}
+
+int mg_image_decode(const uint8_t* data, size_t n, uint8_t* out, int64_t stride) {
+  if (is_png(data, n)) return mg_png_decode(data, n, out, stride);
+  if (is_jpeg(data, n)) return mg_jpeg_decode(data, n, out, stride);
+  mg::set_error("neither a PNG nor a JPEG file");
+  return MG_ERR_ARG;
+}
+
+int mg_image_decode_batch(const uint8_t* const* data, const size_t* n, int count, uint8_t* const* out,
+                          const int64_t* stride, int threads, int* status) {
+  if (count < 0 || (count > 0 && (!data || !n || !out || !stride))) {
+    mg::set_error("invalid arguments");
+    return MG_ERR_ARG;
+  }
+  if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  threads = std::max(1, std::min(threads, count));
+  std::vector<int> st((size_t)std::max(count, 1), MG_OK);
+  std::vector<std::string> msg((size_t)std::max(count, 1));
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (int i; (i = next.fetch_add(1)) < count;) {
+      st[i] = mg_image_decode(data[i], n[i], out[i], stride[i]);
+      if (st[i] != MG_OK) msg[i] = mg_last_error();
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < threads; ++t) {
+    try {
+      pool.emplace_back(work);
+    } catch (const std::exception&) {
+      break;  // the threads running (and this one) take the rest
+    }
+  }
+  work();
+  for (auto& t : pool) t.join();
+  int first = MG_OK;
+  for (int i = 0; i < count; ++i) {
+    if (status) status[i] = st[i];
+    if (st[i] != MG_OK && first == MG_OK) {
+      first = st[i];
+      mg::set_error("file " + std::to_string(i) + ": " + msg[i]);
+    }
+  }
+  return first;
+}
+
+}  // extern "C"

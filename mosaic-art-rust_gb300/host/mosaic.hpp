@@ -14,8 +14,10 @@
 //   ColorAdjustment /
 //   calculate_optimal_adjustment            color_adjustment.rs:6-154
 //   generate_mosaic                         main.rs:105-164 + 477-685
-//   open_png / save_png                     main.rs:492, 548, 672 (image::open
+//   open_image / open_png / save_png        main.rs:492, 548, 672 (image::open
 //                                           + to_rgb8, DynamicImage::save)
+//   read_material_files                     main.rs:166-206 (load_tiles' files)
+//   generate_mosaic_files                   main.rs:105-164 + 477-685 from paths
 // plus RAII handles for the resident palette, batches and the request loop.
 //
 // Error behaviour: where the crate returns Option the mirror returns
@@ -37,6 +39,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cctype>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -130,7 +133,7 @@ struct RgbImage {
   RgbImageView view() const { return {pixels.data(), width, height, 3 * (int64_t)width}; }
 };
 
-// ---- image files: PNG at the two ends of the path --------------------------------------
+// ---- image files: PNG and JPEG at the two ends of the path --------------------------------------
 // PNG data held in memory as RGB8 (image::load_from_memory + to_rgb8).
 inline RgbImage decode_png(const uint8_t* data, size_t n) {
   RgbImage img;
@@ -139,13 +142,105 @@ inline RgbImage decode_png(const uint8_t* data, size_t n) {
   detail::check(mg_png_decode(data, n, img.pixels.data(), 3 * (int64_t)img.width));
   return img;
 }
-// main.rs:492, 548: image::open(path)?.to_rgb8() for a PNG file.
-inline RgbImage open_png(const Path& path) {
+// PNG or JPEG data held in memory, told apart by its signature.
+inline RgbImage decode_image(const uint8_t* data, size_t n) {
+  RgbImage img;
+  detail::check(mg_image_info(data, n, &img.width, &img.height));
+  img.pixels.resize((size_t)img.width * img.height * 3);
+  detail::check(mg_image_decode(data, n, img.pixels.data(), 3 * (int64_t)img.width));
+  return img;
+}
+namespace detail {
+inline std::vector<uint8_t> read_file(const Path& path) {
   std::ifstream f(path, std::ios::binary);
   if (!f) throw Error(MG_ERR_ARG, "cannot open " + path.string());
-  std::vector<uint8_t> data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  return std::vector<uint8_t>((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+}
+}  // namespace detail
+// main.rs:492, 548: image::open(path)?.to_rgb8() for a PNG or JPEG file.
+inline RgbImage open_image(const Path& path) {
+  const std::vector<uint8_t> data = detail::read_file(path);
+  return decode_image(data.data(), data.size());
+}
+// The same for a file that must be PNG.
+inline RgbImage open_png(const Path& path) {
+  const std::vector<uint8_t> data = detail::read_file(path);
   return decode_png(data.data(), data.size());
 }
+
+// The file half of main.rs:166-206 load_tiles: the regular files of `dir` with
+// a png/jpg/jpeg/webp extension (any case), decoded on up to `threads` host
+// threads (<= 0: all).  A file that cannot be read or decoded (webp among
+// them: no decoder here) is listed in `errors` and skipped, as load_tiles
+// prints and skips it.  Files are taken in path order (read_dir's order is
+// the file system's).  The aspect filter and its fallback then run on the
+// decoded images (mg_select_palette); the crate's fallback would also count
+// the skipped files among its first 2 * max_materials entries.
+struct MaterialFiles {
+  std::vector<Path> paths;
+  std::vector<RgbImage> images;
+  std::vector<std::pair<Path, std::string>> errors;
+  std::vector<RgbImageView> views() const {
+    std::vector<RgbImageView> v;
+    for (const RgbImage& i : images) v.push_back(i.view());
+    return v;
+  }
+};
+inline MaterialFiles read_material_files(const Path& dir, int threads = 0) {
+  std::vector<Path> found;
+  std::error_code ec;
+  for (std::filesystem::directory_iterator it(dir, ec), end; !ec && it != end; it.increment(ec)) {
+    if (!it->is_regular_file()) continue;
+    std::string ext = it->path().extension().string();
+    for (char& c : ext) c = (char)std::tolower((unsigned char)c);
+    if (ext == ".png" || ext == ".jpg" || ext == ".jpeg" || ext == ".webp") found.push_back(it->path());
+  }
+  if (ec) throw Error(MG_ERR_ARG, "cannot read directory " + dir.string() + ": " + ec.message());
+  std::sort(found.begin(), found.end());
+  MaterialFiles out;
+  std::vector<std::vector<uint8_t>> data;
+  std::vector<Path> readable;
+  for (const Path& p : found) {
+    std::ifstream f(p, std::ios::binary);
+    if (!f) {
+      out.errors.emplace_back(p, "cannot open");
+      continue;
+    }
+    data.emplace_back((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    readable.push_back(p);
+  }
+  const int n = (int)data.size();
+  std::vector<RgbImage> imgs((size_t)n);
+  std::vector<const uint8_t*> ptrs((size_t)n);
+  std::vector<size_t> lens((size_t)n);
+  std::vector<uint8_t*> outs((size_t)n);
+  std::vector<int64_t> strides((size_t)n);
+  std::vector<int> status((size_t)n, MG_OK);
+  uint8_t dummy[3];
+  for (int i = 0; i < n; ++i) {
+    ptrs[i] = data[i].data();
+    lens[i] = data[i].size();
+    if (mg_image_info(ptrs[i], lens[i], &imgs[i].width, &imgs[i].height) == MG_OK) {
+      imgs[i].pixels.resize((size_t)imgs[i].width * imgs[i].height * 3);
+      outs[i] = imgs[i].pixels.data();
+      strides[i] = 3 * (int64_t)imgs[i].width;
+    } else {  // the decode reports the defect for this file
+      outs[i] = dummy;
+      strides[i] = 3;
+    }
+  }
+  if (n) mg_image_decode_batch(ptrs.data(), lens.data(), n, outs.data(), strides.data(), threads, status.data());
+  for (int i = 0; i < n; ++i) {
+    if (status[i] == MG_OK) {
+      out.paths.push_back(readable[i]);
+      out.images.push_back(std::move(imgs[i]));
+    } else {
+      out.errors.emplace_back(readable[i], "not a readable PNG or JPEG image (status " + std::to_string(status[i]) + ")");
+    }
+  }
+  return out;
+}
+
 // An RGB8 image as PNG file data: level 0 stores the filtered rows, level 1
 // codes each 64 KB block with its own Huffman code; `threads` <= 0: all.
 inline std::vector<uint8_t> encode_png(const RgbImageView& img, int level = 1, int threads = 0) {
@@ -661,6 +756,32 @@ inline MosaicOutput generate_mosaic(const RgbImageView& target, const std::vecto
       const int32_t i = grid[(size_t)y * o.grid_w + x];
       if (i >= 0) out.grid[y][x] = paths[(size_t)i];
     }
+  return out;
+}
+
+// main.rs:105-164 + 477-685 from files: the target (PNG or JPEG), the
+// material folder (read_material_files on up to `threads` host threads) and,
+// when output_path is not empty, the mosaic saved there as PNG after creating
+// its parent folders (main.rs:667-672; the crate picks the format by
+// extension, and only .png is written here: any other fails with MG_ERR_ARG
+// before any work).  Files skipped while reading are listed in *skipped.
+inline MosaicOutput generate_mosaic_files(const Path& target_path, const Path& material_dir, const Path& output_path,
+                                          const MosaicOptions& o, int threads = 0,
+                                          std::vector<std::pair<Path, std::string>>* skipped = nullptr,
+                                          Context& ctx = default_context()) {
+  if (!output_path.empty()) {
+    std::string ext = output_path.extension().string();
+    for (char& c : ext) c = (char)std::tolower((unsigned char)c);
+    if (ext != ".png") throw Error(MG_ERR_ARG, "only PNG output is written: " + output_path.string());
+  }
+  const RgbImage target = open_image(target_path);
+  const MaterialFiles m = read_material_files(material_dir, threads);
+  if (skipped) *skipped = m.errors;
+  MosaicOutput out = generate_mosaic(target.view(), m.views(), m.paths, o, nullptr, ctx);
+  if (!output_path.empty()) {
+    if (output_path.has_parent_path()) std::filesystem::create_directories(output_path.parent_path());
+    save_png(out.image.view(), output_path, 1, threads);
+  }
   return out;
 }
 

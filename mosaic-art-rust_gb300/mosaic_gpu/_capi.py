@@ -147,6 +147,12 @@ SIGNATURES = [
                                 C.c_int, _f32p, _u8p]),
     ("mg_select_palette", C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_float, C.c_float,
                                     C.c_int, C.POINTER(C.c_int)]),
+    ("mg_jpeg_info", C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("mg_jpeg_decode", C.c_int, [C.c_void_p, C.c_size_t, _u8p, C.c_int64]),
+    ("mg_image_info", C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("mg_image_decode", C.c_int, [C.c_void_p, C.c_size_t, _u8p, C.c_int64]),
+    ("mg_image_decode_batch", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_size_t), C.c_int, C.POINTER(_u8p),
+                                        C.POINTER(C.c_int64), C.c_int, C.POINTER(C.c_int)]),
     ("mg_png_info", C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("mg_png_decode", C.c_int, [C.c_void_p, C.c_size_t, _u8p, C.c_int64]),
     ("mg_png_decode_batch", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_size_t), C.c_int, C.POINTER(_u8p),
@@ -421,6 +427,43 @@ def png_decode(data: bytes, out: np.ndarray | None = None) -> np.ndarray:
         raise ValueError("out must be a (h, w, 3) uint8 array with contiguous rows")
     check(load().mg_png_decode(data, len(data), ptr(out, C.c_uint8), out.strides[0]))
     return out
+
+
+def image_info(data: bytes) -> tuple[int, int]:
+    """Width and height of a PNG or JPEG file."""
+    w, h = C.c_int(), C.c_int()
+    check(load().mg_image_info(data, len(data), C.byref(w), C.byref(h)))
+    return w.value, h.value
+
+
+def image_decode(data: bytes, out: np.ndarray | None = None) -> np.ndarray:
+    """A PNG or JPEG file as an (h, w, 3) uint8 array."""
+    w, h = image_info(data)
+    if out is None:
+        out = np.empty((h, w, 3), np.uint8)
+    check(load().mg_image_decode(data, len(data), ptr(out, C.c_uint8), out.strides[0]))
+    return out
+
+
+def image_decode_batch(files: list[bytes], threads: int = 0) -> tuple[list[np.ndarray | None], list[int]]:
+    """PNG and JPEG files on up to `threads` host threads; (images, status codes)."""
+    n = len(files)
+    outs, sizes = [], []
+    for f in files:
+        try:
+            w, h = image_info(f)
+        except MosaicError:
+            w, h = 1, 1
+        outs.append(np.zeros((h, w, 3), np.uint8))
+    bufs = [C.create_string_buffer(f, len(f)) for f in files]
+    data = (C.c_void_p * max(n, 1))(*[C.cast(b, C.c_void_p) for b in bufs])
+    lens = (C.c_size_t * max(n, 1))(*[len(f) for f in files])
+    outp = (_u8p * max(n, 1))(*[ptr(o, C.c_uint8) for o in outs])
+    strides = (C.c_int64 * max(n, 1))(*[o.strides[0] for o in outs])
+    status = (C.c_int * max(n, 1))()
+    load().mg_image_decode_batch(data, lens, n, outp, strides, threads, status)
+    st = [int(status[i]) for i in range(n)]
+    return [o if s == MG_OK else None for o, s in zip(outs, st)], st
 
 
 def png_decode_batch(files: list[bytes], threads: int = 0) -> tuple[list[np.ndarray | None], list[int]]:

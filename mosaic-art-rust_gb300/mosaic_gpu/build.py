@@ -21,7 +21,7 @@ REPO = PKG_ROOT.parent
 INCLUDE = REPO / "include"
 
 CUDA_SOURCES = ["k_lab.cu", "k_resize.cu", "k_scan.cu", "k_nearest_grid.cu", "k_sim.cu", "k_greedy.cu", "k_anneal.cu", "k_composite.cu", "k_batch.cu",
-                "capi.cu", "capi_batch.cu", "capi_server.cu", "io_png.cpp"]  # io_png.cpp: host code, same library
+                "capi.cu", "capi_batch.cu", "capi_server.cu", "io_png.cpp", "io_jpeg.cpp"]  # io_png.cpp: host code, same library
 GENCODE = "arch=compute_103a,code=sm_103a"
 
 

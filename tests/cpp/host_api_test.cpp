@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <filesystem>
+#include <fstream>
 #include <string>
 #include <vector>
 
@@ -474,6 +475,124 @@ static void png_tests() {  // main.rs:1888-1912 (missing, corrupted files), 2219
   CHECK(threw);
 }
 
+// A 16x8 grey JPEG written by hand (T.81 baseline): one component, quantiser 1,
+// a DC code and an AC code of one symbol each ("0": category 0, "0": EOB), so
+// both blocks hold DC 0 alone and decode to level 128 everywhere.
+static std::vector<uint8_t> grey_jpeg() {
+  std::vector<uint8_t> j = {0xFF, 0xD8, 0xFF, 0xDB, 0x00, 0x43, 0x00};
+  j.insert(j.end(), 64, 1);
+  const uint8_t sof[] = {0xFF, 0xC0, 0x00, 0x0B, 8, 0x00, 0x08, 0x00, 0x10, 1, 1, 0x11, 0};
+  j.insert(j.end(), sof, sof + sizeof(sof));
+  const uint8_t dht_head[] = {0xFF, 0xC4, 0x00, 0x26};
+  j.insert(j.end(), dht_head, dht_head + 4);
+  for (uint8_t cls : {0x00, 0x10}) {
+    j.push_back(cls);
+    j.push_back(1);  // one code of length 1
+    j.insert(j.end(), 15, 0);
+    j.push_back(0);  // its symbol
+  }
+  const uint8_t sos[] = {0xFF, 0xDA, 0x00, 0x08, 1, 1, 0x00, 0, 63, 0, 0x0F, 0xFF, 0xD9};
+  j.insert(j.end(), sos, sos + sizeof(sos));
+  return j;
+}
+
+static void write_bytes(const Path& p, const std::vector<uint8_t>& d) {
+  std::ofstream f(p, std::ios::binary | std::ios::trunc);
+  f.write(reinterpret_cast<const char*>(d.data()), (std::streamsize)d.size());
+}
+
+static RgbImage solid_image(int w, int h, uint8_t r, uint8_t g, uint8_t b) {
+  RgbImage img;
+  img.width = w;
+  img.height = h;
+  img.pixels.resize((size_t)w * h * 3);
+  for (size_t i = 0; i < img.pixels.size(); i += 3) {
+    img.pixels[i] = r;
+    img.pixels[i + 1] = g;
+    img.pixels[i + 2] = b;
+  }
+  return img;
+}
+
+static void material_file_tests() {  // main.rs:166-206 load_tiles' files (extensions, skipped files)
+  const Path dir = tmp_file("_materials");
+  std::filesystem::remove_all(dir);
+  std::filesystem::create_directories(dir / "sub.png");  // a folder with an image extension: not a file
+  const RgbImage red = solid_image(4, 3, 255, 0, 0), blue = solid_image(5, 2, 0, 0, 255);
+  save_png(red.view(), dir / "a.png", 1, 1);
+  save_png(blue.view(), dir / "B.PNG", 0, 1);
+  write_bytes(dir / "c.JPG", grey_jpeg());
+  write_bytes(dir / "d.webp", {'R', 'I', 'F', 'F', 0, 0, 0, 0, 'W', 'E', 'B', 'P'});
+  write_bytes(dir / "e.txt", {'x'});
+  const MaterialFiles m = read_material_files(dir, 2);
+  CHECK(m.paths.size() == 3 && m.images.size() == 3);
+  if (m.paths.size() == 3) {
+    CHECK(m.paths[0].filename() == "B.PNG" && m.paths[1].filename() == "a.png" && m.paths[2].filename() == "c.JPG");
+    CHECK(m.images[0].pixels == blue.pixels && m.images[1].pixels == red.pixels);
+    const RgbImage& g = m.images[2];
+    CHECK(g.width == 16 && g.height == 8);
+    CHECK(std::all_of(g.pixels.begin(), g.pixels.end(), [](uint8_t v) { return v == 128; }));
+  }
+  CHECK(m.errors.size() == 1 && m.errors[0].first.filename() == "d.webp");
+  const RgbImage j = open_image(dir / "c.JPG");
+  CHECK(j.width == 16 && j.height == 8 && j.pixels[0] == 128);
+  bool threw = false;
+  try {
+    open_png(dir / "c.JPG");  // a JPEG is not a PNG
+  } catch (const Error& e) {
+    threw = e.code() == MG_ERR_ARG;
+  }
+  CHECK(threw);
+  threw = false;
+  try {
+    read_material_files(dir / "missing");
+  } catch (const Error& e) {
+    threw = e.code() == MG_ERR_ARG;
+  }
+  CHECK(threw);
+  std::filesystem::remove_all(dir);
+}
+
+static void generate_files_tests() {  // main.rs:105-164 + 477-685 from files
+  const Path dir = tmp_file("_gen_files");
+  std::filesystem::remove_all(dir);
+  std::filesystem::create_directories(dir / "materials");
+  uint32_t s = 21;
+  RgbImage target = solid_image(96, 72, 0, 0, 0);
+  for (size_t i = 0; i < target.pixels.size(); ++i) target.pixels[i] = (uint8_t)(lcg(s) >> 24);
+  save_png(target.view(), dir / "target.png", 1, 1);
+  for (int i = 0; i < 24; ++i) {
+    const RgbImage m = solid_image(16, 12, (uint8_t)(lcg(s) >> 24), (uint8_t)(lcg(s) >> 24), (uint8_t)(lcg(s) >> 24));
+    save_png(m.view(), dir / "materials" / ("m" + std::to_string(100 + i) + ".png"), 1, 1);
+  }
+  write_bytes(dir / "materials" / "grey.jpeg", grey_jpeg());
+  write_bytes(dir / "materials" / "broken.jpg", {0xFF, 0xD8, 0xFF});
+  MosaicOptions o;
+  o.grid_w = 12;
+  o.grid_h = 9;
+  o.max_usage_per_image = 6;
+  o.optimization_iterations = 300;
+  o.seed = 5;
+  std::vector<std::pair<Path, std::string>> skipped;
+  const Path out_path = dir / "out" / "deeper" / "mosaic.png";
+  const MosaicOutput a = generate_mosaic_files(dir / "target.png", dir / "materials", out_path, o, 2, &skipped);
+  CHECK(skipped.size() == 1 && skipped[0].first.filename() == "broken.jpg");
+  const MaterialFiles m = read_material_files(dir / "materials");
+  const RgbImage t = open_image(dir / "target.png");
+  const MosaicOutput b = generate_mosaic(t.view(), m.views(), m.paths, o);
+  CHECK(a.grid == b.grid && a.image.pixels == b.image.pixels && a.palette_size == 25);
+  const RgbImage saved = open_png(out_path);
+  CHECK(saved.width == 96 && saved.height == 72 && saved.pixels == a.image.pixels);
+  bool threw = false;
+  try {
+    generate_mosaic_files(dir / "target.png", dir / "materials", dir / "mosaic.jpg", o);
+  } catch (const Error& e) {
+    threw = e.code() == MG_ERR_ARG;
+  }
+  CHECK(threw);
+  std::filesystem::remove_all(dir);
+}
+
 int main(int argc, char** argv) {
   const bool gpu = argc > 1 && std::strcmp(argv[1], "--gpu") == 0;
   usage_tracker_tests();
@@ -484,6 +603,7 @@ int main(int argc, char** argv) {
   color_host_tests();
   result_tests();
   png_tests();
+  material_file_tests();
   if (gpu) {
     average_lab_tests();
     similarity_device_tests();
@@ -491,6 +611,7 @@ int main(int argc, char** argv) {
     optimizer_device_tests();
     color_device_tests();
     generate_tests();
+    generate_files_tests();
   } else {
     // without a GPU the mirror reports the failure as mosaic::Error
     bool threw = false;
