@@ -475,13 +475,14 @@ static void png_tests() {  // main.rs:1888-1912 (missing, corrupted files), 2219
   CHECK(threw);
 }
 
-// A 16x8 grey JPEG written by hand (T.81 baseline): one component, quantiser 1,
-// a DC code and an AC code of one symbol each ("0": category 0, "0": EOB), so
-// both blocks hold DC 0 alone and decode to level 128 everywhere.
-static std::vector<uint8_t> grey_jpeg() {
+// A w x h grey JPEG written by hand (T.81 baseline): one component, quantiser
+// 1, a DC code and an AC code of one symbol each ("0": category 0, "0": EOB),
+// so every block holds DC 0 alone and decodes to level 128 everywhere.
+static std::vector<uint8_t> grey_jpeg(int w = 16, int h = 8) {
   std::vector<uint8_t> j = {0xFF, 0xD8, 0xFF, 0xDB, 0x00, 0x43, 0x00};
   j.insert(j.end(), 64, 1);
-  const uint8_t sof[] = {0xFF, 0xC0, 0x00, 0x0B, 8, 0x00, 0x08, 0x00, 0x10, 1, 1, 0x11, 0};
+  const uint8_t sof[] = {0xFF, 0xC0, 0x00, 0x0B, 8, (uint8_t)(h >> 8), (uint8_t)h, (uint8_t)(w >> 8), (uint8_t)w,
+                         1, 1, 0x11, 0};
   j.insert(j.end(), sof, sof + sizeof(sof));
   const uint8_t dht_head[] = {0xFF, 0xC4, 0x00, 0x26};
   j.insert(j.end(), dht_head, dht_head + 4);
@@ -491,8 +492,13 @@ static std::vector<uint8_t> grey_jpeg() {
     j.insert(j.end(), 15, 0);
     j.push_back(0);  // its symbol
   }
-  const uint8_t sos[] = {0xFF, 0xDA, 0x00, 0x08, 1, 1, 0x00, 0, 63, 0, 0x0F, 0xFF, 0xD9};
+  const uint8_t sos[] = {0xFF, 0xDA, 0x00, 0x08, 1, 1, 0x00, 0, 63, 0};
   j.insert(j.end(), sos, sos + sizeof(sos));
+  const int bits = 2 * ((w + 7) / 8) * ((h + 7) / 8);  // "00" per block, then 1-bits to the byte's end
+  j.insert(j.end(), (size_t)(bits + 7) / 8, 0);
+  if (bits % 8) j.back() = (uint8_t)((1u << (8 - bits % 8)) - 1u);
+  j.push_back(0xFF);
+  j.push_back(0xD9);
   return j;
 }
 
@@ -536,6 +542,12 @@ static void material_file_tests() {  // main.rs:166-206 load_tiles' files (exten
   CHECK(m.errors.size() == 1 && m.errors[0].first.filename() == "d.webp");
   const RgbImage j = open_image(dir / "c.JPG");
   CHECK(j.width == 16 && j.height == 8 && j.pixels[0] == 128);
+  for (int h : {1, 7, 12, 17}) {  // block counts of every parity: the entropy data ends mid-byte or on a byte
+    const std::vector<uint8_t> d = grey_jpeg(24, h);
+    const RgbImage g = decode_image(d.data(), d.size());
+    CHECK(g.width == 24 && g.height == h);
+    CHECK(std::all_of(g.pixels.begin(), g.pixels.end(), [](uint8_t v) { return v == 128; }));
+  }
   bool threw = false;
   try {
     open_png(dir / "c.JPG");  // a JPEG is not a PNG
@@ -565,7 +577,7 @@ static void generate_files_tests() {  // main.rs:105-164 + 477-685 from files
     const RgbImage m = solid_image(16, 12, (uint8_t)(lcg(s) >> 24), (uint8_t)(lcg(s) >> 24), (uint8_t)(lcg(s) >> 24));
     save_png(m.view(), dir / "materials" / ("m" + std::to_string(100 + i) + ".png"), 1, 1);
   }
-  write_bytes(dir / "materials" / "grey.jpeg", grey_jpeg());
+  write_bytes(dir / "materials" / "grey.jpeg", grey_jpeg(16, 12));  // 4:3, as the target: passes the aspect filter
   write_bytes(dir / "materials" / "broken.jpg", {0xFF, 0xD8, 0xFF});
   MosaicOptions o;
   o.grid_w = 12;
@@ -580,7 +592,9 @@ static void generate_files_tests() {  // main.rs:105-164 + 477-685 from files
   const MaterialFiles m = read_material_files(dir / "materials");
   const RgbImage t = open_image(dir / "target.png");
   const MosaicOutput b = generate_mosaic(t.view(), m.views(), m.paths, o);
-  CHECK(a.grid == b.grid && a.image.pixels == b.image.pixels && a.palette_size == 25);
+  CHECK(a.palette_size == 25);  // 24 PNGs and the JPEG; the broken file skipped
+  CHECK(a.grid == b.grid);
+  CHECK(a.image.pixels == b.image.pixels);
   const RgbImage saved = open_png(out_path);
   CHECK(saved.width == 96 && saved.height == 72 && saved.pixels == a.image.pixels);
   bool threw = false;
