@@ -61,10 +61,12 @@ __global__ void __launch_bounds__(32) greedy_kernel(const float4* __restrict__ p
 // state of the walk lives in its shared memory); the other CTAs, on other
 // SMs, hold the scouts, which read the walk's state and write their records
 // through distributed shared memory, so the walker's SM runs nothing but the
-// walk.
-constexpr int kWarps = 32;                  // per CTA
-constexpr int kScoutCtas = 2;               // CTAs 1..kScoutCtas of the cluster
-constexpr int kScouts = kWarps * kScoutCtas;  // every warp of the scout CTAs
+// walk.  Two cluster shapes hold the same 64 scouts: four scout CTAs of 16
+// warps (128 registers a thread, which the walker's loop uses: a launch of a
+// few mosaics), or two of 32 warps (64 registers; a batch, whose clusters
+// then take three SMs each instead of five).
+constexpr int kScouts = 64;                 // every warp of the scout CTAs
+constexpr int kScoutWarpsMax = 32;          // per CTA, the larger shape
 constexpr uint32_t kInvalidEpoch = 0xFFFFFFFFu;
 constexpr uint32_t kWalkPolls = 1u << 24;      // the walker's bounded wait for a record
 constexpr uint32_t kInjectedWalkPolls = 1u << 12;  // ... when a timeout is injected (well under a millisecond)
@@ -85,12 +87,11 @@ enum Ctrl { kProgress = 0, kEpoch = 1, kAbort = 2 };
 // anything beyond it) lies inside the 2*weight window of entry i -- then, if
 // entry i is the first eligible one, the penalty cannot change the decision.
 // Palette indices are 16-bit (palettes of at most 65535).
-// When the palette's Lab is read from global memory the record also carries,
-// for each f entry, its distance, its weight against the cell above (0 in the
-// first row) and its Lab, and `f_next`, the distance of the first entry after
-// the list (+inf when the list holds every entry under the cap): the walker
-// then settles a cell whose penalty window holds several entries from shared
-// memory (window_cell).
+// The record also carries, for each f entry, its distance, its weight against
+// the cell above (0 in the first row) and its Lab, and `f_next`, the distance
+// of the first entry after the list (+inf when the list holds every entry
+// under the cap): the walker then settles a cell whose penalty window holds
+// several entries from shared memory (window_cell).
 struct __align__(16) CellRecord {
   uint32_t kf[32];
   uint32_t kr[32];
@@ -153,7 +154,7 @@ __host__ __device__ inline size_t walker_smem_bytes(int gw, int n, int p, bool l
 }
 // Shared memory of the scout CTA: staging per warp, then the cost terms.
 __host__ __device__ inline size_t scout_cta_smem_bytes() {
-  return (size_t)kWarps * sizeof(ScoutStage) + (size_t)kCostChunk * 8;
+  return (size_t)kScoutWarpsMax * sizeof(ScoutStage) + (size_t)kCostChunk * 8;
 }
 __host__ __device__ inline size_t pair_smem_bytes(int gw, int n, int p, bool lab_smem, bool ring) {
   const size_t a = walker_smem_bytes(gw, n, p, lab_smem, ring), b = scout_cta_smem_bytes();
@@ -392,7 +393,7 @@ __device__ inline WalkerLayout walker_layout(uint8_t* smem, int gw, int n, int p
 // generic ones.)
 // withhold: build the records but never publish them (an injected fault: the
 // walker's wait for the first record then runs out).
-template <bool kWindow, bool kRing>
+template <bool kRing>
 __device__ bool scout_cells(int s, const GreedyJob& J, const float4* __restrict__ pal, int p, uint8_t* smem,
                             ScoutStage& S, int R, uint32_t* err, bool withhold) {
   const int lane = threadIdx.x & 31;
@@ -515,7 +516,7 @@ __device__ bool scout_cells(int s, const GreedyJob& J, const float4* __restrict_
       st_cluster_v4(rr + 16u * (uint32_t)lane, v);
     }
     if (lane == 0) st_cluster_u32(rr + 256u, ep0 == ep1 ? ep0 : kInvalidEpoch);
-    if (kWindow) {
+    {
       // distance, weight against the cell above and Lab of each f entry (wgt
       // as full_cell computes it), and the distance after the list
       float d = inf, wu = 0.0f;
@@ -539,8 +540,8 @@ __device__ bool scout_cells(int s, const GreedyJob& J, const float4* __restrict_
   return true;
 }
 
-template <bool kLabSmem, bool kRing>
-__global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps * 32)
+template <bool kLabSmem, bool kRing, int kScoutCtas, int kWarps>
+__global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWarps * 32))
     greedy_pair_kernel(const float4* __restrict__ pal, int p, const GreedyJob* __restrict__ jobs, uint32_t* err,
                        uint32_t walk_polls, uint32_t withhold) {
   extern __shared__ __align__(128) uint8_t smem[];
@@ -568,8 +569,9 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
     // ---- the scouts, then (CTA 1) the final cost of the walk
     ScoutStage* stage = reinterpret_cast<ScoutStage*>(smem);
     float* terms = reinterpret_cast<float*>(smem + (size_t)kWarps * sizeof(ScoutStage));
-    bool ok = scout_cells<!kLabSmem, kRing>((int)(rank - 1) * kWarps + warp, J, pal, p, smem, stage[warp], R, err,
-                                            withhold != 0u);
+    static_assert(kScoutCtas * kWarps == kScouts, "64 scouts");
+    bool ok = scout_cells<kRing>((int)(rank - 1) * kWarps + warp, J, pal, p, smem, stage[warp], R, err,
+                                       withhold != 0u);
     if (rank > 1) {
       cluster_sync_all();
       return;
@@ -680,21 +682,19 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
       }
     }
   };
-  // The walk is a chain of dependent decisions.  Per cell, the two lowest
-  // keys among entries under the usage cap -- ignoring the left neighbour --
-  // are found first (two warp minimums that do not depend on the previous
-  // choice); the decision is then one comparison with the previous choice
-  // (the left neighbour): the first key unless its material is that
-  // neighbour's, else the second.  So the chain from one cell's choice to the
-  // next is a compare and a select.  A record's counters are read before the
-  // previous commit; the only counter that commit changed is the left
-  // neighbour's, which the comparison excludes anyway -- except at a row
-  // start (no left neighbour), which takes the uncommon path with that
-  // counter corrected.  Record reads are software-pipelined: the header of
-  // cell c + 2 and the counters of cell c + 1 are read while cell c is
+  // The walk is a chain of dependent decisions, so its speed is the latency
+  // of one decision in one warp: every warp collective and every memory wait
+  // on the path from one cell's choice to the next counts in full.  Per cell,
+  // one warp minimum over the record's entries under the usage cap, the left
+  // neighbour's material removed, gives the reference's choice.  A record's
+  // counters are read before the previous commit; the only counter that
+  // commit changed is the left neighbour's, which is removed anyway -- except
+  // at a row start (no left neighbour), where that entry counts with its
+  // counter + 1.  Record reads are software-pipelined: the counters of cell
+  // c + 1 and the header of cell c + 2 are read first while cell c is
   // decided, unconditionally (a record not yet published is read again once
-  // it is).  Everything uncommon (row starts, the full evaluation, late
-  // records and the probes for new ones) sits behind one branch.
+  // it is).  Everything uncommon (the full evaluation, windows that are not
+  // clear, late records and the probes for new ones) sits behind one branch.
   // Placements go to the shared-memory grid, which the scouts poll; the grid
   // reaches global memory once, after the walk.
   struct Head {
@@ -761,6 +761,29 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
   }
   // The common case runs in a tight inner loop of its own; a cell that needs
   // anything else leaves it, is finished below, and the inner loop resumes.
+  // Each entry's packed word (position << 27 | blocked << 26 | counter << 16 |
+  // material, ~0 unless present and under the cap) is formed when its
+  // counter arrives, with the counter as read (wb) and with one more (wp: the
+  // entry of a row start whose material the previous cell took, read before
+  // that commit).  The decision is then one warp minimum over the words with
+  // the left neighbour's material removed, and its commit is made by every
+  // lane (the same stores), so no lane waits on another before the next
+  // cell's counters are read.  The counter packs to 10 bits: an entry under
+  // the cap whose counter does not fit (caps above 1023) is marked as not
+  // clear, so a cell that would take it goes the uncommon way.
+  struct Words {
+    uint32_t ti, wb, wp;
+  };
+  auto words = [&](const Cur& r) -> Words {
+    const uint32_t base = ((r.key >> 17) << 27) | (((r.key >> 16) & 1u) << 26) | (r.key & 0xFFFFu);
+    const bool pres = r.key != 0xFFFFFFFFu;
+    Words o;
+    o.ti = r.ti;
+    o.wb = pres & (r.ui < max_usage) ? base | (min(r.ui, 1023u) << 16) | (r.ui < 1023u ? 0u : 1u << 26) : 0xFFFFFFFFu;
+    o.wp = pres & (r.ui + 1u < max_usage) ? base | (min(r.ui + 1u, 1023u) << 16) | (r.ui + 1u < 1023u ? 0u : 1u << 26)
+                                         : 0xFFFFFFFFu;
+    return o;
+  };
   int c = 0;
   while (c < n && !aborted) {
     Head h2{};
@@ -768,30 +791,33 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
     Cur nxt = cur;
     uint32_t chosen = 0xFFFFFFFFu;
     bool fast = false;
+    Words wc = words(cur);
     for (;;) {
-      // (a) the two lowest keys under the cap, left neighbour ignored
-      const bool okn = cur.ui < max_usage;  // absent entries carry ~0
-      const uint32_t b1 = __reduce_min_sync(0xffffffffu, okn ? cur.key : 0xFFFFFFFFu);
-      const uint32_t b2 = __reduce_min_sync(0xffffffffu, (okn && cur.key != b1) ? cur.key : 0xFFFFFFFFu);
-      // (b) header of cell c + 2 -- whether it is published is known from the
-      // last probe (probes happen on the uncommon path; waiting here, before
-      // this cell's commit, could wait on a scout that waits on this cell)
+      // (a) counters of cell c + 1, read before this cell's commit; header of
+      // cell c + 2 -- whether it is published is known from the last probe
+      // (probes happen on the uncommon path; waiting here, before this cell's
+      // commit, could wait on a scout that waits on this cell)
+      nxt = finish(h1);
       h2_ok = c + 2 < ready_until;
       h2 = load_head(c + 2);
-      // (c) counters of cell c + 1, read before this cell's commit
-      nxt = finish(h1);
-      // (d) this cell: the first key unless it is the left neighbour's material
-      chosen = (b1 & 0xFFFFu) != (uint32_t)last ? b1 : b2;
-      fast = x != 0 && chosen != 0xFFFFFFFFu && !(chosen & 0x10000u);  // not a row start, found, window clear
-      if (!fast || !h1_ok) break;
-      const int t = (int)(chosen & 0xFFFFu);
-      if (lane == (int)(chosen >> 17)) {
-        usage[cur.ti] = cur.ui + 1u;
-        place(c, t);
+      // (b) this cell: the first entry under the cap that is not the left
+      // neighbour's material (at a row start, that material's counter + 1)
+      const bool same = wc.ti == (uint32_t)last;
+      const uint32_t w = !same ? wc.wb : (x != 0 ? 0xFFFFFFFFu : (cur_fresh ? wc.wb : wc.wp));
+      const uint32_t b = __reduce_min_sync(0xffffffffu, w);
+      fast = (b != 0xFFFFFFFFu) & !(b & (1u << 26));
+      if (!fast || !h1_ok) {
+        // the record's key form for the uncommon path; a row start is redone there
+        chosen = b != 0xFFFFFFFFu ? (((b >> 27) << 17) | (((b >> 26) & 1u) << 16) | (b & 0xFFFFu)) : b;
+        fast = fast && x != 0;
+        break;
       }
-      __syncwarp();
+      const int t = (int)(b & 0xFFFFu);
+      usage[t] = ((b >> 16) & 1023u) + 1u;
+      place(c, t);
       last = t;
       cur = nxt;
+      wc = words(nxt);
       cur_fresh = false;
       h1 = h2;
       h1_ok = h2_ok;
@@ -825,7 +851,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __launch_bounds__(kWarps 
           done = true;
         }
       }
-      if (!kLabSmem && !done && !row_start && chosen != 0xFFFFFFFFu && (chosen & 0x10000u) &&
+      if (!done && !row_start && chosen != 0xFFFFFFFFu && (chosen & 0x10000u) &&
           rec[c & (R - 1)].epoch == epoch) {
         const int tw = window_cell(c, cur, last, y > 0);
         if (tw >= 0) {
@@ -912,17 +938,24 @@ int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_job
   if (n_jobs <= 0) return MG_OK;
   if (k < 1 || k > 100) return fail(MG_ERR_ARG, "candidate count must be in 1..100");
   constexpr size_t kMaxSmem = 220 * 1024;
-  static int configured_device = -1;
+  static int configured_device = -1, sms = 0;
   int dev = 0;
   MG_CUDA(cudaGetDevice(&dev));
   if (configured_device != dev) {
-    MG_CUDA(cudaFuncSetAttribute(greedy_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
-    MG_CUDA(cudaFuncSetAttribute(greedy_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
-    MG_CUDA(cudaFuncSetAttribute(greedy_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
-    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
-    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
-    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
-    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    const int m = (int)kMaxSmem;
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    MG_CUDA(cudaFuncSetAttribute(greedy_kernel<true, true>, a, m));
+    MG_CUDA(cudaFuncSetAttribute(greedy_kernel<false, true>, a, m));
+    MG_CUDA(cudaFuncSetAttribute(greedy_kernel<false, false>, a, m));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<true, false, 4, 16>, a, m));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<false, false, 4, 16>, a, m));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<true, true, 4, 16>, a, m));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<false, true, 4, 16>, a, m));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<true, false, 2, 32>, a, m));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<false, false, 2, 32>, a, m));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<true, true, 2, 32>, a, m));
+    MG_CUDA(cudaFuncSetAttribute(greedy_pair_kernel<false, true, 2, 32>, a, m));
+    MG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     configured_device = dev;
   }
   // The scouted walk: counters in shared memory, 16-bit palette indices, rows
@@ -937,16 +970,23 @@ int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_job
     if (form >= 0) {
       const bool lab_smem = form == 0 || form == 2, ring = form >= 2;
       const size_t bytes = pair_smem_bytes(max_gw, max_cells, p, lab_smem, ring);
-      const unsigned grid = (1 + kScoutCtas) * n_jobs;
       const uint32_t polls = inject_timeout ? kInjectedWalkPolls : kWalkPolls, hold = inject_timeout ? 1u : 0u;
-      if (form == 0)
-        greedy_pair_kernel<true, false><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err, polls, hold);
-      else if (form == 1)
-        greedy_pair_kernel<false, false><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err, polls, hold);
-      else if (form == 2)
-        greedy_pair_kernel<true, true><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err, polls, hold);
-      else
-        greedy_pair_kernel<false, true><<<grid, kWarps * 32, bytes, stream>>>(pal, p, jobs_dev, err, polls, hold);
+      // five SMs a mosaic while every cluster finds room at once, else three
+      const bool wide = 5 * n_jobs <= sms;
+      auto go = [&](auto kernel, int ctas, int threads) {
+        kernel<<<(unsigned)(ctas * n_jobs), threads, bytes, stream>>>(pal, p, jobs_dev, err, polls, hold);
+      };
+      if (wide) {
+        if (form == 0) go(greedy_pair_kernel<true, false, 4, 16>, 5, 512);
+        else if (form == 1) go(greedy_pair_kernel<false, false, 4, 16>, 5, 512);
+        else if (form == 2) go(greedy_pair_kernel<true, true, 4, 16>, 5, 512);
+        else go(greedy_pair_kernel<false, true, 4, 16>, 5, 512);
+      } else {
+        if (form == 0) go(greedy_pair_kernel<true, false, 2, 32>, 3, 1024);
+        else if (form == 1) go(greedy_pair_kernel<false, false, 2, 32>, 3, 1024);
+        else if (form == 2) go(greedy_pair_kernel<true, true, 2, 32>, 3, 1024);
+        else go(greedy_pair_kernel<false, true, 2, 32>, 3, 1024);
+      }
       g_launches += 1;
       MG_CUDA(cudaGetLastError());
       return MG_OK;
