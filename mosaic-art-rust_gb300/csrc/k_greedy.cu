@@ -71,7 +71,7 @@ constexpr uint32_t kInvalidEpoch = 0xFFFFFFFFu;
 constexpr uint32_t kWalkPolls = 1u << 24;      // the walker's bounded wait for a record
 constexpr uint32_t kInjectedWalkPolls = 1u << 12;  // ... when a timeout is injected (well under a millisecond)
 constexpr uint32_t kScoutPolls = 1u << 22;  // polls of about 1 us each
-constexpr int kScoutLead = 80;             // records built at most this many cells ahead
+constexpr int kScoutLead = 124;            // records built at most this many cells ahead (a ring of 128)
 constexpr int kCostChunk = 2048;  // cells per pass of the final cost sum
 enum Ctrl { kProgress = 0, kEpoch = 1, kAbort = 2 };
 
@@ -722,28 +722,29 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
   // list); each scores d + (w_up + w_left) * weight in full_cell's arithmetic
   // and the lowest score, then the lowest position, wins -- full_cell's
   // decision.  Commits it and returns the material; -1 when the window may
-  // reach past the list (then full_cell decides).
-  auto window_cell = [&](int cc, const Cur& cu, int left, bool has_up) -> int {
+  // reach past the list (then full_cell decides).  e0: the position of the
+  // first eligible entry (the loop's minimum).  Positions and materials come
+  // out of warp minimums over packed words (no bit scans or shuffles).
+  auto window_cell = [&](int cc, const Cur& cu, int left, bool has_up, int e0) -> int {
     const CellRecord& Rc = rec[cc & (R - 1)];
     const bool elig = cu.key != 0xFFFFFFFFu && cu.ui < max_usage && (int)cu.ti != left;
-    const unsigned em = __ballot_sync(0xffffffffu, elig);
-    if (!em) return -1;
-    const int e0 = __ffs(em) - 1;
     const float dl = Rc.wd[lane];
-    const float b0 = __fadd_rn(__shfl_sync(0xffffffffu, dl, e0), __fmul_rn(2.0f, weight));
+    const float b0 = __fadd_rn(Rc.wd[e0], __fmul_rn(2.0f, weight));
     if (!(Rc.f_next >= b0)) return -1;
     const bool in = elig && lane >= e0 && dl < b0;
-    // the left neighbour's Lab: its entry in the previous cell's list, else global memory
+    // the left neighbour's Lab: its entry in the previous cell's list, else the palette
     const CellRecord& Rp = rec[(cc - 1) & (R - 1)];
     const uint32_t pk = Rp.kf[lane];
-    const unsigned pm = __ballot_sync(0xffffffffu, pk != 0xFFFFFFFFu && (pk & 0xFFFFu) == (uint32_t)left);
-    const float4 lab_left = pm ? Rp.wl[__ffs(pm) - 1] : __ldg(pal + left);
+    const uint32_t pl =
+        __reduce_min_sync(0xffffffffu, (pk != 0xFFFFFFFFu && (pk & 0xFFFFu) == (uint32_t)left) ? (uint32_t)lane : 32u);
+    const float4 lab_left = pl < 32u ? Rp.wl[pl] : lab(left);
     float pen = has_up ? Rc.wu[lane] : 0.0f;  // 0 + w_up, exactly
     pen = __fadd_rn(pen, wgt(Rc.wl[lane], lab_left));
     const uint32_t sb = in ? __float_as_uint(__fadd_rn(dl, __fmul_rn(pen, weight))) : 0xFFFFFFFFu;
     const uint32_t mn = __reduce_min_sync(0xffffffffu, sb);
-    const int win = mn == 0xFFFFFFFFu ? e0 : __ffs(__ballot_sync(0xffffffffu, sb == mn)) - 1;
-    const int tw = (int)__shfl_sync(0xffffffffu, cu.ti, win);
+    const bool wins = mn == 0xFFFFFFFFu ? lane == e0 : (in && sb == mn);
+    const uint32_t wn = __reduce_min_sync(0xffffffffu, wins ? ((uint32_t)lane << 16) | cu.ti : 0xFFFFFFFFu);
+    const int win = (int)(wn >> 16), tw = (int)(wn & 0xFFFFu);
     if (lane == win) {
       usage[cu.ti] = cu.ui + 1u;
       place(cc, tw);
@@ -853,7 +854,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
       }
       if (!done && !row_start && chosen != 0xFFFFFFFFu && (chosen & 0x10000u) &&
           rec[c & (R - 1)].epoch == epoch) {
-        const int tw = window_cell(c, cur, last, y > 0);
+        const int tw = window_cell(c, cur, last, y > 0, (int)(chosen >> 17));
         if (tw >= 0) {
           t = tw;
           done = true;
