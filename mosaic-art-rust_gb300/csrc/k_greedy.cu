@@ -32,7 +32,7 @@
 //    exactly as greedy_walk does -- except that with the palette Lab in global
 //    memory a window that closes inside the filtered list is settled from the
 //    record (window_cell).  A scout builds a record once the walker has placed
-//    the cell kScoutLead cells (or a row) back, polling the walker's ring of
+//    the cell kLead cells (or a row) back, polling the walker's ring of
 //    placed cells, and a reset bumps an epoch that invalidates older snapshots.
 //    The walker's shared memory holds rings (records, placed cells), not the
 //    grid, so a mosaic of any cell count walks in this form.  After the walk
@@ -71,7 +71,13 @@ constexpr uint32_t kInvalidEpoch = 0xFFFFFFFFu;
 constexpr uint32_t kWalkPolls = 1u << 24;      // the walker's bounded wait for a record
 constexpr uint32_t kInjectedWalkPolls = 1u << 12;  // ... when a timeout is injected (well under a millisecond)
 constexpr uint32_t kScoutPolls = 1u << 22;  // polls of about 1 us each
-constexpr int kScoutLead = 124;            // records built at most this many cells ahead (a ring of 128)
+// Records are built at most kLead cells ahead of the walker: 124 in the
+// five-CTA shape (a ring of 128 holds them; fewer late records), 80 in the
+// three-CTA shape of batches (fresher snapshots: fewer cells whose whole list
+// was capped since, which matters with their dense palettes).  The rings are
+// sized for the larger.
+constexpr int kScoutLead = 124;
+constexpr int kScoutLeadBatch = 80;
 constexpr int kCostChunk = 2048;  // cells per pass of the final cost sum
 enum Ctrl { kProgress = 0, kEpoch = 1, kAbort = 2 };
 
@@ -393,7 +399,7 @@ __device__ inline WalkerLayout walker_layout(uint8_t* smem, int gw, int n, int p
 // generic ones.)
 // withhold: build the records but never publish them (an injected fault: the
 // walker's wait for the first record then runs out).
-template <bool kRing>
+template <bool kRing, int kLead>
 __device__ bool scout_cells(int s, const GreedyJob& J, const float4* __restrict__ pal, int p, uint8_t* smem,
                             ScoutStage& S, int R, uint32_t* err, bool withhold) {
   const int lane = threadIdx.x & 31;
@@ -426,16 +432,16 @@ __device__ bool scout_cells(int s, const GreedyJob& J, const float4* __restrict_
         d[r] = __ldg(cd + j);
       }
     }
-    // Wait until the walker has placed cell c - min(gw, kScoutLead): the
+    // Wait until the walker has placed cell c - min(gw, kLead): the
     // cell above is then placed, and the counters this record is filtered by
-    // are at most kScoutLead placements old (in a region of one colour a
+    // are at most kLead placements old (in a region of one colour a
     // row's placements cap dozens of the nearest materials; a record built a
     // whole row ahead would list none left).  Each cell is written once, by a
     // single 16-bit store, so a scout that sees a value sees the final one; and
     // the walker read that cell's record before placing it (the placement
     // depends on it), so the walker is done with the ring slot this record
     // reuses (the ring holds more than gw records).
-    const int lead = c - min(gw, kScoutLead);
+    const int lead = c - min(gw, kLead);
     uint32_t v_lead = kNoCell;  // the lead cell's material in the low 16 bits
     if (lead >= 0) {
       const uint32_t a_lead = kRing ? r_cells + 4u * (uint32_t)(lead & cmask) : r_cells + 2u * (uint32_t)lead;
@@ -570,7 +576,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
     ScoutStage* stage = reinterpret_cast<ScoutStage*>(smem);
     float* terms = reinterpret_cast<float*>(smem + (size_t)kWarps * sizeof(ScoutStage));
     static_assert(kScoutCtas * kWarps == kScouts, "64 scouts");
-    bool ok = scout_cells<kRing>((int)(rank - 1) * kWarps + warp, J, pal, p, smem, stage[warp], R, err,
+    bool ok = scout_cells<kRing, kScoutCtas == 4 ? kScoutLead : kScoutLeadBatch>((int)(rank - 1) * kWarps + warp, J, pal, p, smem, stage[warp], R, err,
                                        withhold != 0u);
     if (rank > 1) {
       cluster_sync_all();
