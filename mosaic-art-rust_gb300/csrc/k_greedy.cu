@@ -79,6 +79,7 @@ constexpr uint32_t kScoutPolls = 1u << 22;  // polls of about 1 us each
 constexpr int kScoutLead = 124;
 constexpr int kScoutLeadBatch = 80;
 constexpr int kCostChunk = 2048;  // cells per pass of the final cost sum
+constexpr uint32_t kFollowPolls = 1u << 26;  // the cost warp's bounded wait for a placement (seconds)
 enum Ctrl { kProgress = 0, kEpoch = 1, kAbort = 2 };
 
 // A cell's prepared decision: two candidate lists of up to 32 entries in list
@@ -582,6 +583,10 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
       cluster_sync_all();
       return;
     }
+    if (!kRing) {  // the walker CTA's cost warp follows the walk instead
+      cluster_sync_all();
+      return;
+    }
     // calculate_total_cost (adjacency.rs:91-130) of the placed grid once the
     // walk is complete: terms in parallel, one sequential FP32 sum in the
     // reference's order (right then down, row-major).
@@ -630,6 +635,60 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
         __syncthreads();
       }
       if (threadIdx.x == 0 && J.total_cost) *J.total_cost = total;
+    }
+    cluster_sync_all();
+    return;
+  }
+  if (!kRing && warp == 1) {
+    // ---- CTA 0, warp 1: calculate_total_cost (adjacency.rs:91-130) following
+    // the walk, and the placed grid into global memory.  Cell c's terms (right,
+    // then down) are final once cells c, c + 1 and c + gw are placed (each is
+    // written once, so a value seen is the final one); one FP32 sum in the
+    // reference's order, 32 cells behind a row of the walker at most, so the
+    // total is ready when the walk ends.  On another SMSP than the walker.
+    auto lab_of = [&](int i) -> float4 { return kLabSmem ? L.lab[i] : __ldg(pal + i); };
+    const volatile uint16_t* g16 = L.grid16;
+    float total = 0.0f;
+    bool ok = true;
+    for (int c0 = 0; c0 < n && ok; c0 += 32) {
+      const int c = c0 + lane, x = c % gw, y = c / gw;
+      int cur = 0, rt = 0, dn = 0;
+      bool lane_ok = true;
+      if (c < n) {
+        uint32_t polls = 0;
+        for (;;) {
+          cur = g16[c];
+          rt = x < gw - 1 ? g16[c + 1] : 0;
+          dn = y < gh - 1 ? g16[c + gw] : 0;
+          if (cur != kUnplaced && rt != kUnplaced && dn != kUnplaced) break;
+          if (ld_volatile_u32(&L.ctrl[kAbort]) || ++polls > kFollowPolls) {
+            lane_ok = false;
+            break;
+          }
+          __nanosleep(128);
+        }
+      }
+      ok = __all_sync(0xffffffffu, lane_ok);
+      if (!ok) break;
+      float tr = 0.0f, td = 0.0f;
+      if (c < n) {
+        const float4 lc = lab_of(cur);
+        if (x < gw - 1) tr = wgt(lc, lab_of(rt));
+        if (y < gh - 1) td = wgt(lc, lab_of(dn));
+        J.grid[c] = cur;
+      }
+      const int m = min(32, n - c0);
+      for (int i = 0; i < m; ++i) {
+        const float a = __shfl_sync(0xffffffffu, tr, i), b = __shfl_sync(0xffffffffu, td, i);
+        total = __fadd_rn(__fadd_rn(total, a), b);
+      }
+    }
+    if (ok) {
+      if (lane == 0 && J.total_cost) *J.total_cost = total;
+    } else {
+      // the walk gave up: every cell empty (this warp is the grid's only writer)
+      for (int i = lane; i < n; i += 32) J.grid[i] = -1;
+      if (lane == 0) atomicOr(err, kErrTimeout);
     }
     cluster_sync_all();
     return;
@@ -909,16 +968,16 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
       atomicOr(err, kErrTimeout);
       *reinterpret_cast<volatile uint32_t*>(&ctrl[kAbort]) = 1u;
     }
-    // every cell empty, so the stages after the walk read no stale index
-    for (int i = lane; i < n; i += 32) J.grid[i] = -1;
+    // every cell empty, so the stages after the walk read no stale index (in
+    // the 16-bit grid form the cost warp writes the global grid)
+    if (kRing)
+      for (int i = lane; i < n; i += 32) J.grid[i] = -1;
     if (lane == 0 && J.n_resets) *J.n_resets = 0;
   } else {
     // the placed grid in global memory (every lane's stores visible) before the
-    // completion the scout CTA waits for
-    if (kRing)
-      __threadfence();
-    else
-      for (int i = lane; i < n; i += 32) J.grid[i] = (int32_t)grid16[i];
+    // completion the scout CTA waits for; in the 16-bit grid form the cost warp
+    // writes it
+    if (kRing) __threadfence();
     if (lane == 0 && J.n_resets) *J.n_resets = resets;
     __syncwarp();
     if (lane == 0) st_release_cluster(smem_u32(&ctrl[kProgress]), (uint32_t)n);
