@@ -38,9 +38,11 @@ using anneal_detail::wgt;
 
 constexpr int kChainWarps = 4;
 constexpr int kThreads = kChainWarps * 32;
-constexpr int kRound = kChainWarps * 4;  // proposals per round (8 lanes each)
+// Proposals per round: 16 (eight lanes each, one neighbour term a lane) or,
+// on large grids, where two proposals of a round rarely touch, 32 (four lanes
+// each, two terms a lane): about as long a round, nearly twice the swaps.
+constexpr int kRoundMax = 32;
 constexpr int kCtaRing = 4 * kThreads;   // decoded proposals in shared memory
-constexpr int kConfPerWarp = (kRound - 1 + kChainWarps - 1) / kChainWarps;  // conflict tests per warp
 
 struct RoundSlot {  // one proposal's outcome of step 1
   float delta;
@@ -51,19 +53,23 @@ struct RoundSlot {  // one proposal's outcome of step 1
 };
 
 __host__ __device__ inline size_t anneal_cta_smem_bytes(int max_cells, int p, bool lab_smem) {
-  return (size_t)kCtaRing * 16 + (size_t)kRound * sizeof(RoundSlot) + (lab_smem ? (size_t)p * 16 : 0) +
+  return (size_t)kCtaRing * 16 + (size_t)kRoundMax * sizeof(RoundSlot) + (lab_smem ? (size_t)p * 16 : 0) +
          (((size_t)max_cells * 2 + 15) & ~(size_t)15);
 }
 
-template <bool kLabSmem>
+template <bool kLabSmem, int kRound>
 __device__ __forceinline__ void anneal_chain_cta(const float4* __restrict__ pal, int p, const AnnealJob& J, int chain,
                                                  uint8_t* smem) {
+  static_assert(kRound == 16 || kRound == 32, "16 or 32 proposals a round");
+  constexpr int kL = kThreads / kRound;  // lanes per proposal: 8 or 4
+  constexpr int kT = 8 / kL;             // neighbour terms per lane: 1 or 2
+  constexpr int kConfPerWarp = (kRound - 1 + kChainWarps - 1) / kChainWarps;  // conflict tests per warp
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int gw = J.gw, gh = J.gh, n = gw * gh;
   __shared__ unsigned s_conf[kChainWarps];  // written after the round's first barrier, read after the second
   int4* s_ring = reinterpret_cast<int4*>(smem);
   RoundSlot* s_round = reinterpret_cast<RoundSlot*>(smem + (size_t)kCtaRing * 16);
-  float4* s_lab = reinterpret_cast<float4*>(smem + (size_t)kCtaRing * 16 + (size_t)kRound * sizeof(RoundSlot));
+  float4* s_lab = reinterpret_cast<float4*>(smem + (size_t)kCtaRing * 16 + (size_t)kRoundMax * sizeof(RoundSlot));
   uint16_t* s_grid = reinterpret_cast<uint16_t*>(reinterpret_cast<uint8_t*>(s_lab) +
                                                  (kLabSmem ? (size_t)p * sizeof(float4) : 0));
   if (kLabSmem)
@@ -108,8 +114,8 @@ __device__ __forceinline__ void anneal_chain_cta(const float4* __restrict__ pal,
   const bool greedy_only = J.greedy_only != 0;
   const uint32_t k0 = J.key0, k1 = J.key1, strm = J.stream;
   const long long iters = J.iters;
-  const int grp = lane >> 3, slot = lane & 7, leader = grp << 3;
-  const int q_mine = warp * 4 + grp;  // this group's proposal within the round
+  const int grp = lane / kL, slot = lane % kL, leader = grp * kL;
+  const int q_mine = warp * (32 / kL) + grp;  // this group's proposal within the round
 
   long long it = 0, filled = 0;
   while (it < iters) {
@@ -140,33 +146,67 @@ __device__ __forceinline__ void anneal_chain_cta(const float4* __restrict__ pal,
     const uint16_t g1 = s_grid[p1], g2 = s_grid[p2];
     const bool skip = !live || p1 == p2 || g1 == kNone16 || g2 == kNone16;
     const bool same = g1 == g2;
-    const bool first = slot < 4;
-    const int dir = slot & 3;
-    const int bx = first ? x1 : x2, by = first ? y1 : y2;
-    const int nx = bx + (dir == 2 ? -1 : (dir == 3 ? 1 : 0)), ny = by + (dir == 0 ? -1 : (dir == 1 ? 1 : 0));
-    const bool inb = nx >= 0 && nx < gw && ny >= 0 && ny < gh;
-    const int nb = inb ? ny * gw + nx : p1;
-    const bool mutual = inb && nb == (first ? p2 : p1);
-    const uint16_t an = s_grid[nb];
-    const bool work = !skip && !same && inb;
-    const bool nbr = work && !mutual && an != kNone16;  // a placed neighbour
-    const uint16_t gs1 = skip ? (uint16_t)0 : g1, gs2 = skip ? (uint16_t)0 : g2;
-    const uint16_t c_idx = mutual ? gs2 : (an != kNone16 ? an : gs1);
-    const float4 la1 = lab(gs1), la2 = lab(gs2), lc = lab(c_idx);
-    const float w1 = wgt(la1, lc), w2 = wgt(la2, lc);
-    const float o = nbr ? (first ? w1 : w2) : 0.0f;
-    const float nw = nbr ? (first ? w2 : w1) : 0.0f;
-    const float m = (work && mutual && first) ? w1 : 0.0f;
-    float old_cost = 0.0f, new_cost = 0.0f;
+    float old_cost = 0.0f, new_cost = 0.0f, m0 = 0.0f;
+    if constexpr (kT == 1) {
+      const bool first = slot < 4;
+      const int dir = slot & 3;
+      const int bx = first ? x1 : x2, by = first ? y1 : y2;
+      const int nx = bx + (dir == 2 ? -1 : (dir == 3 ? 1 : 0)), ny = by + (dir == 0 ? -1 : (dir == 1 ? 1 : 0));
+      const bool inb = nx >= 0 && nx < gw && ny >= 0 && ny < gh;
+      const int nb = inb ? ny * gw + nx : p1;
+      const bool mutual = inb && nb == (first ? p2 : p1);
+      const uint16_t an = s_grid[nb];
+      const bool work = !skip && !same && inb;
+      const bool nbr = work && !mutual && an != kNone16;  // a placed neighbour
+      const uint16_t gs1 = skip ? (uint16_t)0 : g1, gs2 = skip ? (uint16_t)0 : g2;
+      const uint16_t c_idx = mutual ? gs2 : (an != kNone16 ? an : gs1);
+      const float4 la1 = lab(gs1), la2 = lab(gs2), lc = lab(c_idx);
+      const float w1 = wgt(la1, lc), w2 = wgt(la2, lc);
+      const float o = nbr ? (first ? w1 : w2) : 0.0f;
+      const float nw = nbr ? (first ? w2 : w1) : 0.0f;
+      m0 = (work && mutual && first) ? w1 : 0.0f;
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      old_cost = __fadd_rn(old_cost, __shfl_sync(0xffffffffu, o, leader + t));
-      new_cost = __fadd_rn(new_cost, __shfl_sync(0xffffffffu, nw, leader + t));
+      for (int t = 0; t < 8; ++t) {
+        old_cost = __fadd_rn(old_cost, __shfl_sync(0xffffffffu, o, leader + t));
+        new_cost = __fadd_rn(new_cost, __shfl_sync(0xffffffffu, nw, leader + t));
+      }
+    } else {
+      const uint16_t gs1 = skip ? (uint16_t)0 : g1, gs2 = skip ? (uint16_t)0 : g2;
+      const float4 la1 = lab(gs1), la2 = lab(gs2);
+      // this lane's terms t = slot + kL * tt (0-3: neighbours of pos1 in up, down,
+      // left, right order; 4-7: those of pos2)
+      float o[kT], nw[kT], m[kT];
+#pragma unroll
+      for (int tt = 0; tt < kT; ++tt) {
+        const int t = slot + kL * tt;
+        const bool first = t < 4;
+        const int dir = t & 3;
+        const int bx = first ? x1 : x2, by = first ? y1 : y2;
+        const int nx = bx + (dir == 2 ? -1 : (dir == 3 ? 1 : 0)), ny = by + (dir == 0 ? -1 : (dir == 1 ? 1 : 0));
+        const bool inb = nx >= 0 && nx < gw && ny >= 0 && ny < gh;
+        const int nb = inb ? ny * gw + nx : p1;
+        const bool mutual = inb && nb == (first ? p2 : p1);
+        const uint16_t an = s_grid[nb];
+        const bool work = !skip && !same && inb;
+        const bool nbr = work && !mutual && an != kNone16;  // a placed neighbour
+        const uint16_t c_idx = mutual ? gs2 : (an != kNone16 ? an : gs1);
+        const float4 lc = lab(c_idx);
+        const float w1 = wgt(la1, lc), w2 = wgt(la2, lc);
+        o[tt] = nbr ? (first ? w1 : w2) : 0.0f;
+        nw[tt] = nbr ? (first ? w2 : w1) : 0.0f;
+        m[tt] = (work && mutual && first) ? w1 : 0.0f;
+      }
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        old_cost = __fadd_rn(old_cost, __shfl_sync(0xffffffffu, o[t / kL], leader + t % kL));
+        new_cost = __fadd_rn(new_cost, __shfl_sync(0xffffffffu, nw[t / kL], leader + t % kL));
+      }
+      m0 = m[0];
     }
     const int dx = x2 - x1, dy = y2 - y1;
     const bool adjacent = (dx == 0 && (dy == 1 || dy == -1)) || (dy == 0 && (dx == 1 || dx == -1));
     const int dir12 = dy == -1 ? 0 : (dy == 1 ? 1 : (dx == -1 ? 2 : 3));
-    const float mm = __shfl_sync(0xffffffffu, m, leader + dir12);
+    const float mm = __shfl_sync(0xffffffffu, m0, leader + dir12);  // term dir12 < 4 sits in lane dir12's first term
     if (adjacent) {
       old_cost = __fadd_rn(old_cost, mm);
       new_cost = __fadd_rn(new_cost, mm);
@@ -190,7 +230,9 @@ __device__ __forceinline__ void anneal_chain_cta(const float4* __restrict__ pal,
     const unsigned live_mask = __ballot_sync(0xffffffffu, lane < kRound && !skip_q);  // bit q: not skipped
     // The temperatures T_k (the chain's T after k more coolings, multiplied step
     // by step); lane k keeps T_k.
-    float t_lane = temp;
+    // (T_kRound, wanted when every proposal of a 32-proposal round cools, is
+    // held by every lane as t_last: there is no lane 32)
+    float t_lane = temp, t_last = temp;
     if (!greedy_only) {
       float tk = temp;
 #pragma unroll
@@ -198,6 +240,7 @@ __device__ __forceinline__ void anneal_chain_cta(const float4* __restrict__ pal,
         tk = __fmul_rn(tk, decay);
         if (kk == lane) t_lane = tk;
       }
+      t_last = tk;
     }
     bool acc_q = false;
     {
@@ -235,7 +278,7 @@ __device__ __forceinline__ void anneal_chain_cta(const float4* __restrict__ pal,
     const unsigned cmask = conf_mask & live_mask;
     const int gc = cmask ? __ffs(cmask) - 1 : kRound;  // >= 1: proposal 0 never conflicts
     const int ncommit = (int)min((long long)gc, iters - it);
-    const unsigned commit = (1u << ncommit) - 1u;  // ncommit <= kRound < 32
+    const unsigned commit = ncommit >= 32 ? 0xFFFFFFFFu : (1u << ncommit) - 1u;
     // in-order bookkeeping (every thread, identical values)
 #pragma unroll
     for (int h = 0; h < kRound; ++h) {
@@ -250,7 +293,10 @@ __device__ __forceinline__ void anneal_chain_cta(const float4* __restrict__ pal,
     accepted += __popc(acc_mask & commit);
     const int ncool = __popc(live_mask & commit);  // skipped proposals do not cool
     cooled += ncool;
-    if (!greedy_only) temp = __shfl_sync(0xffffffffu, t_lane, ncool);
+    if (!greedy_only) {
+      const float t_n = __shfl_sync(0xffffffffu, t_lane, ncool & 31);
+      temp = ncool == 32 ? t_last : t_n;
+    }
     // ---- 3. committed accepted swaps -------------------------------------------------------
     if (slot == 0 && q_mine < ncommit && ((acc_mask >> q_mine) & 1u)) {
       s_grid[p1] = g2;

@@ -39,7 +39,7 @@ struct mg_batch {
   mg_ctx* ctx = nullptr;
   int device = 0;  // destroy must not touch ctx, which may already be gone
   mg_palette* pal = nullptr;
-  int n = 0, total_cells = 0, max_gw = 0, max_cells = 0, max_sa_cells = 0, max_out_px = 0;
+  int n = 0, total_cells = 0, max_gw = 0, max_cells = 0, max_sa_cells = 0, min_sa_cells = 0, max_out_px = 0;
   int total_chains = 0;
   std::vector<BatchMosaic> h_mos;
   std::vector<int> cells, out_w, out_h, chains;
@@ -176,7 +176,7 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
   size_t out_bytes = 0, chain_cells = 0, n_results = 0;
   int cell_base = 0, grid_base = 0;
   b->total_chains = 0;
-  b->max_gw = b->max_cells = b->max_sa_cells = b->max_out_px = 0;
+  b->max_gw = b->max_cells = b->max_sa_cells = b->min_sa_cells = b->max_out_px = 0;
   for (int i = 0; i < n; ++i) {
     const mg_mosaic& r = ms[i];
     const int64_t st = r.target_stride ? r.target_stride : 3ll * r.target_w;
@@ -228,7 +228,10 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
     b->total_chains += M.chains;
     b->max_gw = std::max(b->max_gw, r.grid_w);
     b->max_cells = std::max(b->max_cells, N);
-    if (run_sa) b->max_sa_cells = std::max(b->max_sa_cells, N);
+    if (run_sa) {
+      b->min_sa_cells = b->max_sa_cells == 0 ? N : std::min(b->min_sa_cells, N);
+      b->max_sa_cells = std::max(b->max_sa_cells, N);
+    }
     b->max_out_px = std::max(b->max_out_px, b->out_w[i] * b->out_h[i]);
     if (run_sa && (size_t)N * 2 > 180 * 1024) return fail(MG_ERR_ARG, "mosaic too large for the annealer");
   }
@@ -390,7 +393,7 @@ int batch_enqueue(mg_batch* b, bool with_events) {
     // every annealing chain of every mosaic (k_anneal.cu), then per mosaic the
     // best chain -- or the greedy grid when it is not optimised -- as its final grid
     MG_CHECK(launch_anneal(pal->pal_lab.as<float4>(), P, b->ajobs.as<AnnealJob>(), b->chain_job.as<int>(),
-                           b->chain_id.as<int>(), b->total_chains, b->max_sa_cells, s));
+                           b->chain_id.as<int>(), b->total_chains, b->max_sa_cells, s, b->min_sa_cells));
     MG_CHECK(launch_select_best(b->ajobs.as<AnnealJob>(), n, b->finals_ptr.as<int32_t*>(), b->best.as<int>(), s));
   } else {
     MG_CUDA(cudaMemsetAsync(b->finals.p, 0xFF, b->finals.cap, s));

@@ -9,7 +9,7 @@ namespace mg {
 namespace {
 using namespace anneal_detail;
 
-template <bool kLabSmem>
+template <bool kLabSmem, int kRound>
 __global__ void __launch_bounds__(anneal_cta_detail::kThreads)
     anneal_cta_kernel(const float4* __restrict__ pal, int p, const AnnealJob* __restrict__ jobs,
                       const int* __restrict__ chain_job, const int* __restrict__ chain_id) {
@@ -17,8 +17,11 @@ __global__ void __launch_bounds__(anneal_cta_detail::kThreads)
   const int jid = chain_job ? chain_job[blockIdx.x] : 0;
   const int chain = chain_id ? chain_id[blockIdx.x] : (int)blockIdx.x;
   const AnnealJob J = jobs[jid];
-  anneal_cta_detail::anneal_chain_cta<kLabSmem>(pal, p, J, chain, smem);
+  anneal_cta_detail::anneal_chain_cta<kLabSmem, kRound>(pal, p, J, chain, smem);
 }
+
+// Grids of at least this many cells take 32 proposals a round.
+constexpr int kWideRoundCells = 12000;
 
 template <bool kLabSmem>
 __global__ void __launch_bounds__(32) anneal_kernel(const float4* __restrict__ pal, int p,
@@ -143,7 +146,7 @@ __global__ void total_cost_kernel(const float4* __restrict__ pal, const int32_t*
 }  // namespace
 
 int launch_anneal(const float4* pal, int p, const AnnealJob* jobs_dev, const int* chain_job_dev,
-                  const int* chain_id_dev, int total_chains, int max_cells, cudaStream_t stream) {
+                  const int* chain_id_dev, int total_chains, int max_cells, cudaStream_t stream, int min_cells) {
   if (total_chains <= 0) return MG_OK;
   if (p >= 65535) return fail(MG_ERR_ARG, "annealing supports palettes below 65535 materials");
   const size_t grid_bytes = kRing * sizeof(int4) + (((size_t)max_cells * 2 + 15) & ~(size_t)15);
@@ -156,8 +159,10 @@ int launch_anneal(const float4* pal, int p, const AnnealJob* jobs_dev, const int
   if (configured_device != dev) {
     MG_CUDA(cudaFuncSetAttribute(anneal_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
     MG_CUDA(cudaFuncSetAttribute(anneal_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
-    MG_CUDA(cudaFuncSetAttribute(anneal_cta_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
-    MG_CUDA(cudaFuncSetAttribute(anneal_cta_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    MG_CUDA(cudaFuncSetAttribute(anneal_cta_kernel<true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    MG_CUDA(cudaFuncSetAttribute(anneal_cta_kernel<false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    MG_CUDA(cudaFuncSetAttribute(anneal_cta_kernel<true, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+    MG_CUDA(cudaFuncSetAttribute(anneal_cta_kernel<false, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
     configured_device = dev;
   }
   // A CTA of several warps per chain (more proposals per round) when it fits.
@@ -165,12 +170,19 @@ int launch_anneal(const float4* pal, int p, const AnnealJob* jobs_dev, const int
     using anneal_cta_detail::anneal_cta_smem_bytes;
     const size_t with_lab = anneal_cta_smem_bytes(max_cells, p, true), no_lab = anneal_cta_smem_bytes(max_cells, p, false);
     if (with_lab <= kMaxSmem || no_lab <= kMaxSmem) {
-      if (with_lab <= kMaxSmem)
-        anneal_cta_kernel<true><<<total_chains, anneal_cta_detail::kThreads, with_lab, stream>>>(
-            pal, p, jobs_dev, chain_job_dev, chain_id_dev);
-      else
-        anneal_cta_kernel<false><<<total_chains, anneal_cta_detail::kThreads, no_lab, stream>>>(
-            pal, p, jobs_dev, chain_job_dev, chain_id_dev);
+      const bool wide = (min_cells < 0 ? max_cells : min_cells) >= kWideRoundCells;
+      const unsigned nt = anneal_cta_detail::kThreads;
+      if (with_lab <= kMaxSmem) {
+        if (wide)
+          anneal_cta_kernel<true, 32><<<total_chains, nt, with_lab, stream>>>(pal, p, jobs_dev, chain_job_dev, chain_id_dev);
+        else
+          anneal_cta_kernel<true, 16><<<total_chains, nt, with_lab, stream>>>(pal, p, jobs_dev, chain_job_dev, chain_id_dev);
+      } else {
+        if (wide)
+          anneal_cta_kernel<false, 32><<<total_chains, nt, no_lab, stream>>>(pal, p, jobs_dev, chain_job_dev, chain_id_dev);
+        else
+          anneal_cta_kernel<false, 16><<<total_chains, nt, no_lab, stream>>>(pal, p, jobs_dev, chain_job_dev, chain_id_dev);
+      }
       g_launches += 1;
       MG_CUDA(cudaGetLastError());
       return MG_OK;

@@ -166,8 +166,10 @@ struct AnnealJob {
   uint32_t key0, key1, stream;
   int greedy_only;
 };
+// min_cells: the smallest grid among the chains (< 0: max_cells), which picks
+// the round size.
 int launch_anneal(const float4* pal, int p, const AnnealJob* jobs_dev, const int* chain_job_dev,
-                  const int* chain_id_dev, int total_chains, int max_cells, cudaStream_t stream);
+                  const int* chain_id_dev, int total_chains, int max_cells, cudaStream_t stream, int min_cells = -1);
 // Per job: the chain with the lowest final cost (ties: the lowest chain) into
 // its final grid; a job with no chains copies grid_in and records -1.
 int launch_select_best(const AnnealJob* jobs_dev, int n_jobs, int32_t* const* final_grids_dev,

@@ -211,7 +211,10 @@ def test_greedy_ring_form_bit_exact(ctx, orc, p, max_usage, region):
     (10, 4, 4, 200, 2, 100.0, 0.0, False), (10, 4, 4, 200, 2, 0.0, 0.99995, False),
     (10, 4, 4, 200, 2, -3.0, 0.99995, False), (40, 10, 8, 1000, 2, 100.0, 0.99995, True),
     (1, 1, 1, 100, 1, 100.0, 0.99995, False), (20, 6, 5, 0, 2, 100.0, 0.99995, False),
-    (80, 33, 20, 20000, 5, 100.0, 0.99995, False)])
+    (80, 33, 20, 20000, 5, 100.0, 0.99995, False),
+    # grids of at least 12 000 cells: 32 proposals a round (four lanes each)
+    (300, 150, 100, 20000, 3, 100.0, 0.99995, False), (200, 120, 100, 5000, 2, 1.0, 0.95, False),
+    (150, 130, 100, 3000, 2, 100.0, 0.99995, True), (90, 150, 80, 2000, 2, 0.0, 0.99995, False)])
 def test_anneal_chains_bit_exact(ctx, orc, p, gw, gh, iters, chains, t0, decay, greedy):
     rng = np.random.default_rng(p * 7 + iters)
     pal = rand_lab(rng, p)
