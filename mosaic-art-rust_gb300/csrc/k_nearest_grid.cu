@@ -197,6 +197,124 @@ __device__ __forceinline__ void scan_box(const int* start, int g, const Box& o, 
   }
 }
 
+// ---- the select-then-sort query ------------------------------------------------------------
+// Most queries take this form: their candidate keys are gathered into the
+// warp's flat buffer (the WarpLists memory, kGatherCap keys), the k-th
+// distance among them is found by bisection on the distance bits (a warp
+// count per step), the buffer is cut to the keys at or below it, and one
+// bitonic sort of what is left gives the k smallest keys -- instead of the
+// top-k list's repeated sorts and merges.  A query whose candidates do not fit
+// takes the list form (scan_box + warp_merge), which gives the same keys.
+constexpr int kGatherCap = 3 * kListCap;  // list, tmp and buf of WarpLists, contiguous
+
+// Appends the keys of box o (minus box in, when has_in) whose distance bits
+// are at most dthr to buf[n..); returns the new count (beyond cap: nothing
+// past cap was stored, the caller falls back).
+__device__ __forceinline__ int gather_box(const int* start, int g, const Box& o, const Box& in, bool has_in,
+                                          const float4* __restrict__ sorted, const float4& q,
+                                          unsigned long long* buf, int n, int cap, uint32_t dthr, int lane) {
+  const int ny = o.y1 - o.y0 + 1, nz = o.z1 - o.z0 + 1;
+  const int nseg = ny * nz * 2;
+  for (int sb = 0; sb < nseg; sb += 32) {
+    const int si = sb + lane;
+    int beg = 0, cnt = 0;
+    if (si < nseg) {
+      const int row = si >> 1, partno = si & 1;
+      const int z = o.z0 + row / ny, y = o.y0 + row % ny;
+      int xa = o.x0, xb = o.x1;
+      const bool inner = has_in && y >= in.y0 && y <= in.y1 && z >= in.z0 && z <= in.z1;
+      if (!inner) {
+        if (partno) xb = xa - 1;
+      } else if (partno == 0) {
+        xb = min(o.x1, in.x0 - 1);
+      } else {
+        xa = max(o.x0, in.x1 + 1);
+      }
+      if (xa <= xb) {
+        const int rb = (z * g + y) * g;
+        beg = start[rb + xa];
+        cnt = start[rb + xb + 1] - beg;
+      }
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int t = __shfl_up_sync(kFull, incl, d);
+      if (lane >= d) incl += t;
+    }
+    const int total = __shfl_sync(kFull, incl, 31);
+    const int excl = incl - cnt;
+    const int delta = beg - excl;
+    for (int t0 = 0; t0 < total; t0 += 32) {
+      const int t = t0 + lane;
+      int j = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int e = __shfl_sync(kFull, excl, j + step);
+        if (e <= t) j += step;
+      }
+      const int dj = __shfl_sync(kFull, delta, j);
+      unsigned long long key = kMaxKey;
+      if (t < total) {
+        const float4 e = __ldg(&sorted[t + dj]);
+        key = ((unsigned long long)__float_as_uint(sq_dist(q.x, q.y, q.z, e.x, e.y, e.z)) << 32) |
+              (unsigned)__float_as_int(e.w);
+      }
+      const bool pass = t < total && (uint32_t)(key >> 32) <= dthr;
+      const unsigned mask = __ballot_sync(kFull, pass);
+      const int pos = n + __popc(mask & ((1u << lane) - 1u));
+      if (pass && pos < cap) buf[pos] = key;
+      n += __popc(mask);
+    }
+  }
+  __syncwarp();
+  return n;
+}
+
+// The smallest distance D (as bits) with at least k of buf[0..n) at or below
+// it (k <= n <= kGatherCap): bisection between the smallest and the largest.
+__device__ uint32_t kth_dist_bits(const unsigned long long* buf, int n, int k, int lane) {
+  constexpr int kPer = kGatherCap / 32;
+  uint32_t d[kPer];
+  uint32_t mn = 0xFFFFFFFFu, mx = 0u;
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    const int i = lane + 32 * j;
+    d[j] = i < n ? (uint32_t)(buf[i] >> 32) : 0xFFFFFFFFu;
+    if (i < n) {
+      mn = min(mn, d[j]);
+      mx = max(mx, d[j]);
+    }
+  }
+  uint32_t lo = __reduce_min_sync(kFull, mn), hi = __reduce_max_sync(kFull, mx);
+  while (lo < hi) {  // warp-uniform
+    const uint32_t mid = lo + ((hi - lo) >> 1);
+    unsigned c = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) c += d[j] <= mid ? 1u : 0u;
+    if ((int)__reduce_add_sync(kFull, c) >= k) hi = mid;
+    else lo = mid + 1u;
+  }
+  return lo;
+}
+
+// Keeps the keys of buf[0..n) whose distance bits are at most dthr (in order);
+// returns their count.
+__device__ __forceinline__ int cut_keys(unsigned long long* buf, int n, uint32_t dthr, int lane) {
+  int m = 0;
+  for (int b = 0; b < n; b += 32) {
+    const int i = b + lane;
+    const unsigned long long key = i < n ? buf[i] : kMaxKey;
+    const bool keep = i < n && (uint32_t)(key >> 32) <= dthr;
+    const unsigned mask = __ballot_sync(kFull, keep);
+    __syncwarp();
+    if (keep) buf[m + __popc(mask & ((1u << lane) - 1u))] = key;
+    m += __popc(mask);
+    __syncwarp();
+  }
+  return m;
+}
+
 // Entries in the rows of box b, summed over the warp.
 __device__ __forceinline__ int count_box(const int* start, int g, const Box& b, int lane) {
   const int ny = b.y1 - b.y0 + 1, rows = ny * (b.z1 - b.z0 + 1);
@@ -230,27 +348,79 @@ __global__ void __launch_bounds__(kGridThreads, 2) nearest_grid_kernel(
     const int cx = grid_coord(q.x, H.lo[0], H.inv[0], g), cy = grid_coord(q.y, H.lo[1], H.inv[1], g),
               cz = grid_coord(q.z, H.lo[2], H.inv[2], g);
     Box c{0, g - 1, 0, g - 1, 0, g - 1};
+    int cube_n = H.p;
     if (finite) {
       for (int s = 0;; ++s) {
         c = Box{max(cx - s, 0), min(cx + s, g - 1), max(cy - s, 0), min(cy + s, g - 1), max(cz - s, 0),
                 min(cz + s, g - 1)};
-        if (box_is_all(c, g) || count_box(start, g, c, lane) >= target) break;
+        if (box_is_all(c, g)) break;
+        cube_n = count_box(start, g, c, lane);
+        if (cube_n >= target) break;
+      }
+      if (box_is_all(c, g)) cube_n = H.p;
+    }
+    // ---- select, then sort (the common form)
+    unsigned long long* fb = W.list;  // kGatherCap keys
+    bool done = false;
+    if (cube_n <= kGatherCap) {
+      int m = gather_box(start, g, c, c, false, sorted, q, fb, 0, kGatherCap, 0xFFFFFFFFu, lane);
+      bool fits = m <= kGatherCap;
+      if (fits && m > 0 && !box_is_all(c, g)) {
+        // the cube holds >= min(P, k) entries: its k-th distance bounds the search
+        const uint32_t dk = kth_dist_bits(fb, m, min(k, m), lane);
+        m = cut_keys(fb, m, dk, lane);
+        if (m >= k) {
+          const float r = __fsqrt_rn(__uint_as_float(dk));
+          const float R = __fadd_rn(__fmul_rn(r, 1.001f), 1e-3f);
+          const Box o{grid_coord(__fsub_rn(q.x, R), H.lo[0], H.inv[0], g), grid_coord(__fadd_rn(q.x, R), H.lo[0], H.inv[0], g),
+                      grid_coord(__fsub_rn(q.y, R), H.lo[1], H.inv[1], g), grid_coord(__fadd_rn(q.y, R), H.lo[1], H.inv[1], g),
+                      grid_coord(__fsub_rn(q.z, R), H.lo[2], H.inv[2], g), grid_coord(__fadd_rn(q.z, R), H.lo[2], H.inv[2], g)};
+          m = gather_box(start, g, o, c, true, sorted, q, fb, m, kGatherCap, dk, lane);
+        } else {
+          // fewer than k in the cube (palette below k): every entry counts
+          const Box all{0, g - 1, 0, g - 1, 0, g - 1};
+          m = gather_box(start, g, all, c, true, sorted, q, fb, m, kGatherCap, 0xFFFFFFFFu, lane);
+        }
+        fits = m <= kGatherCap;
+      }
+      if (fits && m > 0) {
+        const int kk = min(k, m);
+        const uint32_t d2 = kth_dist_bits(fb, m, kk, lane);
+        m = cut_keys(fb, m, d2, lane);  // the k smallest keys and their ties at the k-th distance
+        int mp = 1;
+        while (mp < m) mp <<= 1;
+        if (mp <= kGatherCap) {
+          for (int i = m + lane; i < mp; i += 32) fb[i] = kMaxKey;
+          __syncwarp();
+          warp_bitonic_sort(fb, mp, lane);
+          len = kk;
+          done = true;
+        }
+      } else if (fits) {
+        len = 0;
+        done = true;
       }
     }
-    scan_box(start, g, c, c, false, sorted, q, W, len, nbuf, thr, k, lane);
-    if (!box_is_all(c, g)) {
+    if (!done) {
+      // ---- the top-k list form (candidates beyond the buffer)
+      len = 0;
+      nbuf = 0;
+      thr = kMaxKey;
+      scan_box(start, g, c, c, false, sorted, q, W, len, nbuf, thr, k, lane);
+      if (!box_is_all(c, g)) {
+        __syncwarp();
+        warp_merge(W, len, nbuf, thr, k, lane);
+        // the cube holds >= min(P, k) entries: len == k unless P < k
+        const float r = __fsqrt_rn(__uint_as_float((uint32_t)(thr >> 32)));
+        const float R = __fadd_rn(__fmul_rn(r, 1.001f), 1e-3f);
+        const Box o = len < k ? Box{0, g - 1, 0, g - 1, 0, g - 1} : Box{grid_coord(__fsub_rn(q.x, R), H.lo[0], H.inv[0], g), grid_coord(__fadd_rn(q.x, R), H.lo[0], H.inv[0], g),
+                    grid_coord(__fsub_rn(q.y, R), H.lo[1], H.inv[1], g), grid_coord(__fadd_rn(q.y, R), H.lo[1], H.inv[1], g),
+                    grid_coord(__fsub_rn(q.z, R), H.lo[2], H.inv[2], g), grid_coord(__fadd_rn(q.z, R), H.lo[2], H.inv[2], g)};
+        scan_box(start, g, o, c, true, sorted, q, W, len, nbuf, thr, k, lane);
+      }
       __syncwarp();
       warp_merge(W, len, nbuf, thr, k, lane);
-      // the cube holds >= min(P, k) entries: len == k unless P < k
-      const float r = __fsqrt_rn(__uint_as_float((uint32_t)(thr >> 32)));
-      const float R = __fadd_rn(__fmul_rn(r, 1.001f), 1e-3f);
-      const Box o = len < k ? Box{0, g - 1, 0, g - 1, 0, g - 1} : Box{grid_coord(__fsub_rn(q.x, R), H.lo[0], H.inv[0], g), grid_coord(__fadd_rn(q.x, R), H.lo[0], H.inv[0], g),
-                  grid_coord(__fsub_rn(q.y, R), H.lo[1], H.inv[1], g), grid_coord(__fadd_rn(q.y, R), H.lo[1], H.inv[1], g),
-                  grid_coord(__fsub_rn(q.z, R), H.lo[2], H.inv[2], g), grid_coord(__fadd_rn(q.z, R), H.lo[2], H.inv[2], g)};
-      scan_box(start, g, o, c, true, sorted, q, W, len, nbuf, thr, k, lane);
     }
-    __syncwarp();
-    warp_merge(W, len, nbuf, thr, k, lane);
     for (int i = lane; i < out_stride; i += 32) {
       const unsigned long long key = i < len ? W.list[i] : kMaxKey;
       out_idx[(size_t)qi * out_stride + i] = i < len ? (uint32_t)key : 0xFFFFFFFFu;
