@@ -699,6 +699,11 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
   }
 
   // ---- CTA 0, warp 0: the walker
+  // Windows that are not clear are settled inside the common loop in the
+  // batch shape (dense palettes: a fifth of a batch's cells had one, each
+  // leaving the loop), and on the uncommon path in the five-CTA shape, whose
+  // loop the larger body slowed.
+  constexpr bool kInlineWindows = kScoutCtas == 2;
   uint32_t* ctrl = L.ctrl;
   CellRecord* rec = L.rec;
   uint32_t* seq = L.seq;
@@ -767,6 +772,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
   };
   struct Cur {
     uint32_t key, ti, ui;
+    bool f;  // the key is the record's f entry (its epoch is the walk's)
   };
   auto load_head = [&](int c) {
     const CellRecord& Rc = rec[c & (R - 1)];
@@ -774,7 +780,8 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
   };
   auto finish = [&](const Head& h) {
     Cur r;
-    r.key = h.ep == epoch ? h.kf : h.kr;
+    r.f = h.ep == epoch;
+    r.key = r.f ? h.kf : h.kr;
     r.ti = r.key & 0xFFFFu;
     r.ui = (r.key != 0xFFFFFFFFu && r.ti < (uint32_t)p) ? usage[r.ti] : 0xFFFFFFFFu;
     return r;
@@ -816,7 +823,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
     }
     return tw;
   };
-  Cur cur{0xFFFFFFFFu, 0u, 0xFFFFFFFFu};
+  Cur cur{0xFFFFFFFFu, 0u, 0xFFFFFFFFu, false};
   bool cur_fresh = true;  // cur's counters include the previous commit
   Head h1{0u, 0xFFFFFFFFu, 0xFFFFFFFFu};
   bool h1_ok = false;
@@ -850,8 +857,12 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
                                          : 0xFFFFFFFFu;
     return o;
   };
+  const float two_w = __fmul_rn(2.0f, weight);
+  int last_pos = -1;  // position of the previous cell's choice in its record's f list, -1 unknown
+  bool win_tried = false;
   int c = 0;
   while (c < n && !aborted) {
+    win_tried = false;
     Head h2{};
     bool h2_ok = false;
     Cur nxt = cur;
@@ -870,7 +881,27 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
       // neighbour's material (at a row start, that material's counter + 1)
       const bool same = wc.ti == (uint32_t)last;
       const uint32_t w = !same ? wc.wb : (x != 0 ? 0xFFFFFFFFu : (cur_fresh ? wc.wb : wc.wp));
-      const uint32_t b = __reduce_min_sync(0xffffffffu, w);
+      uint32_t b = __reduce_min_sync(0xffffffffu, w);
+      if (kInlineWindows && (b != 0xFFFFFFFFu) & ((b & (1u << 26)) != 0u) & (x != 0) & cur.f) {
+        // (c) a window that is not clear, settled here (window_cell's
+        // decision) when the record closes it; the left neighbour's Lab comes
+        // from the previous record's entry it was chosen as, else the palette
+        win_tried = true;
+        const CellRecord& Rc = rec[c & (R - 1)];
+        const int e0 = (int)(b >> 27);
+        const float b0 = __fadd_rn(Rc.wd[e0], two_w);
+        if (Rc.f_next >= b0) {
+          const float dl = Rc.wd[lane];
+          const bool in = (w != 0xFFFFFFFFu) & (lane >= e0) & (dl < b0);
+          const float4 lab_left = last_pos >= 0 ? rec[(c - 1) & (R - 1)].wl[last_pos] : lab(last);
+          const float pen = __fadd_rn(Rc.wu[lane], wgt(Rc.wl[lane], lab_left));  // 0 + w_up, then + w_left
+          const uint32_t sb = in ? __float_as_uint(__fadd_rn(dl, __fmul_rn(pen, weight))) : 0xFFFFFFFFu;
+          const uint32_t mn = __reduce_min_sync(0xffffffffu, sb);
+          const uint32_t wn = __reduce_min_sync(0xffffffffu, (in & (sb == mn)) ? w : 0xFFFFFFFFu);
+          const uint32_t pk = (mn == 0xFFFFFFFFu ? b : wn) & ~(1u << 26);
+          if (((pk >> 16) & 1023u) != 1023u) b = pk;  // a counter that fits its field
+        }
+      }
       fast = (b != 0xFFFFFFFFu) & !(b & (1u << 26));
       if (!fast || !h1_ok) {
         // the record's key form for the uncommon path; a row start is redone there
@@ -881,6 +912,10 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
       const int t = (int)(b & 0xFFFFu);
       usage[t] = ((b >> 16) & 1023u) + 1u;
       place(c, t);
+      if (kInlineWindows) {
+        last_pos = cur.f ? (int)(b >> 27) : -1;
+        win_tried = false;
+      }
       last = t;
       cur = nxt;
       wc = words(nxt);
@@ -917,7 +952,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
           done = true;
         }
       }
-      if (!done && !row_start && chosen != 0xFFFFFFFFu && (chosen & 0x10000u) &&
+      if (!done && !win_tried && !row_start && chosen != 0xFFFFFFFFu && (chosen & 0x10000u) &&
           rec[c & (R - 1)].epoch == epoch) {
         const int tw = window_cell(c, cur, last, y > 0, (int)(chosen >> 17));
         if (tw >= 0) {
@@ -954,6 +989,7 @@ __global__ void __cluster_dims__(1 + kScoutCtas, 1, 1) __maxnreg__(65536 / (kWar
       }
     }
     last = t;
+    last_pos = -1;
     cur = nxt;
     cur_fresh = nxt_fresh;
     h1 = h2;

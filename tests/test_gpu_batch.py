@@ -117,3 +117,31 @@ def test_palette_lab_and_similarity_match_oracle(ctx, orc):
     assert ctx.lib.mg_palette_read_similarity(pal.h, sim.ctypes.data_as(C.POINTER(C.c_float))) == 0
     assert np.array_equal(sim.view(np.uint32), orc.similarity_full(lab).view(np.uint32))
     pal.close()
+
+
+def test_many_mosaics_take_the_batch_walk_shape(ctx):
+    """A batch of 40 mosaics walks in the three-CTA cluster shape (five SMs a
+    mosaic would not fit them all at once), which settles windows that are not
+    clear inside its common loop; over the dense 10 000-colour palette a fifth of
+    the cells have such a window.  Every mosaic must equal the same request as a
+    one-mosaic batch (the five-CTA shape, which settles them on its uncommon
+    path), bit for bit, with and without annealing."""
+    from mosaic_gpu import job
+
+    specs, mats, thumbs = job.batched_workload(n=40, seed=424242, scale=0.5)
+    pal = job.Palette(ctx, mats, thumbs, 32, 32, target_aspect=4 / 3)
+    for iters in (0, 600):
+        reqs = job.batched_requests(specs, iterations=iters, chains=2)
+        batch = job.Batch(ctx, pal, reqs)
+        batch.run()
+        for i, r in enumerate(reqs):
+            single = job.Batch(ctx, pal, [r])
+            single.run()
+            r1, g1, im1 = single.read(0)
+            r2, g2, im2 = batch.read(i)
+            assert np.array_equal(g1, g2), (iters, i)
+            assert np.array_equal(im1, im2), (iters, i)
+            assert r1.n_resets == r2.n_resets and np.float32(r1.final_cost) == np.float32(r2.final_cost)
+            single.close()
+        batch.close()
+    pal.close()
