@@ -19,8 +19,9 @@ greedy placement, the annealing chains and the colour-adjusted composite.
          wall time per call, including the uploads and the download of the
          output image and grid.
 
-With one GPU the same line also carries the benchmark spec's two systems patterns
-and the large single mosaic, each measured in this run on the current build:
+With one GPU the same line also carries the two serving patterns (batches of
+uneven mosaics, a request stream) and the large single mosaic, each measured
+in this run on the current build:
   batched  256 uneven mosaics over one resident 10 000-material palette
            (mosaics/s, against the same mosaics one single-mosaic batch after
            another, the plain path)
@@ -442,7 +443,7 @@ def run_ours(args, rank, world, local):
     plan.close()
     del flush
     if rank == 0 and world == 1 and not args.no_patterns and args.workload == WORKLOAD:
-        # the benchmark spec's systems patterns and the large mosaic, on this GPU, in this run
+        # the batched and served patterns and the large mosaic, on this GPU, in this run
         for key, fn in (("batched", lambda: measure_batched(args, 0, 1, local, ctx)),
                         ("served", lambda: measure_served(args, 0, 1, local, ctx)),
                         ("large", lambda: measure_large(args, local, ctx))):
