@@ -112,6 +112,8 @@ __global__ void __launch_bounds__(256) batch_composite_kernel(const BatchMosaic*
                                                               int total_cells, const uint8_t* __restrict__ thumbs,
                                                               int tw, int th, const float4* __restrict__ adj) {
   __shared__ float s_bc[2][256];
+  __shared__ uint32_t s_perm[8];
+  sector_perm_table(s_perm);
   const int per = (total_cells + gridDim.x - 1) / gridDim.x;
   const int c0 = blockIdx.x * per, c1 = min(total_cells, c0 + per);
   int mi = c0 < c1 ? find_mosaic(mos, nm, c0) : 0;
@@ -136,7 +138,7 @@ __global__ void __launch_bounds__(256) batch_composite_kernel(const BatchMosaic*
     const int cy = local / M.gw, cx = local - cy * M.gw;
     uint8_t* dst = M.out + (size_t)cy * th * pitch + (size_t)cx * tw * 3;
     const uint8_t* src = g >= 0 ? thumbs + (size_t)g * tw * th * 3 : nullptr;
-    composite_tile(src, dst, tw, th, pitch, adjust, a, bc);
+    composite_tile(src, dst, tw, th, pitch, adjust, a, bc, s_perm);
   }
 }
 

@@ -42,6 +42,8 @@ __global__ void __launch_bounds__(256) composite_kernel(const int32_t* __restric
                                                         const uint8_t* __restrict__ thumbs, int tw, int th,
                                                         const float4* __restrict__ adj, uint8_t* __restrict__ out) {
   __shared__ float s_bc[2][256];
+  __shared__ uint32_t s_perm[8];
+  sector_perm_table(s_perm);
   const int n = gw * gh;
   const size_t pitch = (size_t)gw * tw * 3;
   int it = 0;
@@ -58,23 +60,38 @@ __global__ void __launch_bounds__(256) composite_kernel(const int32_t* __restric
     const int cy = c / gw, cx = c - cy * gw;
     uint8_t* dst = out + (size_t)cy * th * pitch + (size_t)cx * tw * 3;
     const uint8_t* src = m >= 0 ? thumbs + (size_t)m * tw * th * 3 : nullptr;
-    composite_tile(src, dst, tw, th, pitch, kAdjust, a, bc);
+    composite_tile(src, dst, tw, th, pitch, kAdjust, a, bc, s_perm);
   }
 }
 
+// apply_to_image: adjust_pixel on every pixel; for adjustments in
+// adjustment_new's ranges (and a brightness and contrast that are not NaN,
+// so the brightness/contrast table holds channels in [0, 1]) through the
+// composite's arithmetic, the table and adjust_word.
 __global__ void __launch_bounds__(256) adjust_image_kernel(float4 a4, const uint8_t* __restrict__ in, int w, int h,
                                                            int64_t stride, uint8_t* __restrict__ out) {
   __shared__ float s_unit[256];
-  s_unit[threadIdx.x] = u8_unit(threadIdx.x);
-  __syncthreads();
+  __shared__ uint32_t s_perm[8];
   const Adjust a{a4.x, a4.y, a4.z, a4.w};
+  const bool word = adjust_word_applies(a) && a.brightness == a.brightness && a.contrast == a.contrast;
+  if (word) s_unit[threadIdx.x] = brightness_contrast(u8_unit(threadIdx.x), a.brightness, a.contrast);
+  else s_unit[threadIdx.x] = u8_unit(threadIdx.x);
+  sector_perm_table(s_perm);
+  __syncthreads();
   const int64_t total = (int64_t)w * h;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int y = (int)(t / w), x = (int)(t - (int64_t)y * w);
     const uint8_t* s = in + (int64_t)y * stride + 3 * x;
+    uint8_t* d = out + t * 3;
+    if (word) {
+      const uint32_t p = adjust_word(a, s_unit[s[0]], s_unit[s[1]], s_unit[s[2]], s_perm);
+      d[0] = (uint8_t)p;
+      d[1] = (uint8_t)(p >> 8);
+      d[2] = (uint8_t)(p >> 16);
+      continue;
+    }
     uint8_t o0, o1, o2;
     adjust_pixel(a, s_unit[s[0]], s_unit[s[1]], s_unit[s[2]], o0, o1, o2);
-    uint8_t* d = out + t * 3;
     d[0] = o0;
     d[1] = o1;
     d[2] = o2;

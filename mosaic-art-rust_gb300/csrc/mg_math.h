@@ -471,6 +471,100 @@ MG_HD void adjust_unit(const Adjust& a, float c0, float c1, float c2, uint8_t& o
   o2 = (uint8_t)unit_to_u8(c2);
 }
 
+// y in [-0, 2^23): the bits of the float 2^23 + trunc(y) (the sum rounded
+// toward zero: floats in [2^23, 2^24) are the integers), whose low byte is
+// trunc(y) mod 256.
+MG_HD uint32_t trunc_word(float y) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(__fadd_rz(y, 8388608.0f));
+#else
+  return 0x4B000000u + (uint32_t)y;
+#endif
+}
+// h in [-0, 2^21): the bits of the float 2^21 + floor(4h) / 4 (the sum rounded
+// toward zero: floats in [2^21, 2^22) step by 1/4), 0x4A000000 + floor(4h).
+MG_HD uint32_t quarter_word(float h) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(__fadd_rz(h, 2097152.0f));
+#else
+  return 0x4A000000u + (uint32_t)(h * 4.0f);
+#endif
+}
+// Bytes of the 8-byte value hi:lo picked by the nibbles of sel (each 0..7).
+MG_HD uint32_t perm_bytes(uint32_t lo, uint32_t hi, uint32_t sel) {
+#if defined(__CUDA_ARCH__)
+  return __byte_perm(lo, hi, sel);
+#else
+  const uint64_t v = (uint64_t)hi << 32 | lo;
+  uint32_t r = 0;
+  for (int k = 0; k < 4; ++k) r |= (uint32_t)((v >> (8 * ((sel >> (4 * k)) & 7u))) & 0xFFu) << (8 * k);
+  return r;
+#endif
+}
+// The byte selector of hue sector i for adjust_word: channel r, g, b (result
+// bytes 0, 1, 2) takes c (selector 0), x (1) or 0 (4), as hsv_to_rgb's sectors
+// (c, x, 0), (x, c, 0), (0, c, x), (0, x, c), (x, 0, c), (c, 0, x), and h = 6
+// the last sector's.
+MG_HD uint32_t sector_perm(uint32_t i) {
+  return i == 0 ? 0x410u : i == 1 ? 0x401u : i == 2 ? 0x104u : i == 3 ? 0x014u : i == 4 ? 0x041u : 0x140u;
+}
+// The hue shift and saturation for which adjust_word equals adjust_unit
+// (adjustment_new's ranges, the HSV step active).
+MG_HD bool adjust_word_applies(const Adjust& a) {
+  return (a.hue_shift != 0.0f || a.saturation != 1.0f) && a.hue_shift >= -180.0f && a.hue_shift <= 180.0f &&
+         a.saturation >= 0.0f && a.saturation <= 2.0f;
+}
+
+// adjust_unit for adjustments with adjust_word_applies, the output bytes as
+// one word (r | g << 8 | b << 16; byte 3 is not part of the result).  `perm`
+// holds sector_perm(i) at index i (0..7; device code: shared memory).
+// Rearranged further without changing a result:
+//  - the shifted hue x = hh + shift lies in [-240, 480] (hh in [-60, 300]), so
+//    fmod_360 and the wrap below zero are x - 360 from 360 up (exact), x + 360
+//    below zero, x itself between;
+//  - pos / 60 by div60's multiply and FMA correction at every pos: below
+//    2^-120 both quotients are below 2^-126, and a quotient that small
+//    reaches the output only through sector 0 and t = |h - 1| = 1;
+//  - floor(h) and 2 floor(h / 2) read from quarter_word(h);
+//  - each output channel is one of c + m, x + m and m (min1(0 + m) = m, as
+//    0 <= m = v - c <= v <= 1), each converted once by trunc_word, and the
+//    sector's byte permutation picks them.
+MG_HD uint32_t adjust_word(const Adjust& a, float c0, float c1, float c2, const uint32_t* perm) {
+  float mx, mn, sep, coeff;
+  if (c0 > c1) { mx = c0; mn = c1; sep = MG_SUB(c1, c2); coeff = 0.0f; }
+  else { mx = c1; mn = c0; sep = MG_SUB(c2, c0); coeff = 2.0f; }
+  if (c2 > mx) { mx = c2; sep = MG_SUB(c0, c1); coeff = 4.0f; }
+  else if (c2 < mn) { mn = c2; }
+  float hh = 0.0f, s = 0.0f;
+  if (mx != mn) {
+    const float d = MG_SUB(mx, mn);
+    hh = MG_MUL(MG_ADD(MG_DIV(sep, d), coeff), 60.0f);
+    s = MG_DIV(d, mx);
+  }
+  const float xs = MG_ADD(hh, a.hue_shift);
+  float pos = MG_ADD(xs, xs < 0.0f ? 360.0f : (xs >= 360.0f ? -360.0f : 0.0f));
+  pos = (pos > 0.0f && pos < 360.0f) ? pos : 0.0f;
+  const float v = mx;
+  const float c = MG_MUL(v, min1(MG_MUL(s, a.saturation)));
+  const float q = MG_MUL(pos, 1.0f / 60.0f);
+  const float h = MG_FMA(MG_FMA(-q, 60.0f, pos), 1.0f / 60.0f, q);
+  const uint32_t hq = quarter_word(h);
+  const float hm2 = MG_SUB(h, MG_SUB(u2f(hq & ~7u), 2097152.0f));
+  float t = MG_SUB(hm2, 1.0f);
+  t = t < 0.0f ? -t : t;
+  const float x = MG_MUL(c, MG_SUB(1.0f, t));
+  const float m = MG_SUB(v, c);
+  const uint32_t wc = trunc_word(MG_MUL(min1(MG_ADD(c, m)), 255.0f));
+  const uint32_t wx = trunc_word(MG_MUL(min1(MG_ADD(x, m)), 255.0f));
+  const uint32_t wz = trunc_word(MG_MUL(m, 255.0f));
+#if defined(__CUDA_ARCH__)
+  const uint32_t sel = *reinterpret_cast<const uint32_t*>(reinterpret_cast<const char*>(perm) + (hq & 0x1Cu));
+#else
+  const uint32_t sel = perm[(hq >> 2) & 7u];
+#endif
+  return perm_bytes(perm_bytes(wc, wx, 0x40u), wz, sel);
+}
+
 // color_adjustment.rs:53-87 adjust_pixel.  r, g, b are the channels as v/255.
 MG_HD void adjust_pixel(const Adjust& a, float r, float g, float b, uint8_t& o0, uint8_t& o1, uint8_t& o2) {
   adjust_from_bc(a, brightness_contrast(r, a.brightness, a.contrast), brightness_contrast(g, a.brightness, a.contrast),

@@ -242,6 +242,15 @@ def adjust_pixel(adj, px):
     return o
 
 
+def adjust_pixels(adj, img):
+    """adjust_pixel on every pixel of an RGB8 array (any shape ending in 3)."""
+    a = np.ascontiguousarray(adj, np.float32)
+    i = np.ascontiguousarray(img, np.uint8)
+    o = np.zeros_like(i)
+    lib().orc_adjust_pixels(p(a, C.c_float), p(i, C.c_uint8), i.size // 3, p(o, C.c_uint8))
+    return o
+
+
 def adjustment_new(b, c, h, s):
     out = np.zeros(4, np.float32)
     lib().orc_adjustment_new(b, c, h, s, p(out, C.c_float))

@@ -271,6 +271,26 @@ def test_apply_adjustment_bit_exact(ctx, orc, adj):
             assert np.array_equal(out[y, x], orc.adjust_pixel(a, img[y, x])), (y, x)
 
 
+def test_apply_adjustment_every_colour(ctx, orc):
+    """Every byte triple (a 4096 x 4096 image) through apply_to_image on the
+    device -- for adjustments in adjustment_new's ranges the composite's own
+    per-pixel arithmetic (the brightness/contrast table and the packed HSV
+    round trip) -- against the oracle's adjust_pixel, byte for byte: hue
+    shifts of both signs up to the clamp's ends and one below 2^-120,
+    saturation 0..2, brightness and contrast changes, one adjustment outside
+    the ranges."""
+    v = np.arange(1 << 24, dtype=np.uint32)
+    img = np.stack([v >> 16, (v >> 8) & 255, v & 255], axis=-1).astype(np.uint8).reshape(4096, 4096, 3)
+    for adj in [(0.0, 1.0, 37.5, 1.0), (0.1, 1.0, -64.0, 0.8), (0.05, 1.3, -90.0, 1.6), (-1.0, 1.0, 5.0, 2.0),
+                (0.0, 1.0, 1e-38, 1.0), (0.1, 0.9, 180.0, 2.0), (-0.1, 1.1, -180.0, 0.0), (0.0, 1.0, 0.0, 0.5),
+                (0.0, 1.0, 400.0, 2.5)]:
+        out = ctx.apply_adjustment(adj, img)
+        ref = orc.adjust_pixels(np.array(adj, np.float32), img)
+        bad = np.flatnonzero(np.any(out != ref, axis=-1).ravel())
+        assert bad.size == 0, (adj, bad[:5], img.reshape(-1, 3)[bad[:5]], out.reshape(-1, 3)[bad[:5]],
+                               ref.reshape(-1, 3)[bad[:5]])
+
+
 @pytest.mark.parametrize("strength", [0.0, 0.4, 1.0])
 @pytest.mark.parametrize("tw,th", [(12, 10), (7, 5), (48, 48)])
 def test_composite_bit_exact(ctx, orc, strength, tw, th):
