@@ -422,7 +422,8 @@ int mg_batch_tuning(mg_batch* batch, int* cells_per_cta, int* nearest_chunk);
 int mg_batch_launches(mg_batch* batch);
 int mg_batch_destroy(mg_batch* batch);
 /* One batch from host buffers to host buffers (targets in pinned host memory
- * are read in place). */
+ * are read in place).  The context keeps the batch's device buffers for its
+ * next call (they only grow; mg_ctx_destroy releases them). */
 int mg_generate_batch(mg_ctx* ctx, mg_palette* pal, const mg_mosaic* mosaics, int n, mg_result* results);
 
 /* ---- serving: a request loop over one resident palette ------------------------------

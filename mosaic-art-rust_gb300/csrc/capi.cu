@@ -260,6 +260,7 @@ int mg_ctx_destroy(mg_ctx* ctx) {
   if (!ctx) return MG_OK;
   cudaSetDevice(ctx->device);
   if (ctx->gen_plan) mg_plan_destroy(ctx->gen_plan);
+  if (ctx->gen_batch) mg::batch_free(ctx->gen_batch);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->in0, &ctx->in1, &ctx->in2, &ctx->out0, &ctx->out1, &ctx->out2, &ctx->sums, &ctx->regions,
                     &ctx->err, &ctx->lab_consts})

@@ -44,6 +44,7 @@ struct mg_batch {
   std::vector<BatchMosaic> h_mos;
   std::vector<int> cells, out_w, out_h, chains;
   std::vector<size_t> out_off;
+  int grid_total = 0;
   DevBuf targets, mos, cell_lab, cell_rgb, cand_idx, cand_dist, grids, finals, chain_grids, results, resets,
       init_cost, best, adj, out, err, gjobs, usage, ajobs, chain_job, chain_id, finals_ptr;
   // walk jobs (gjobs): the n_wide mosaics that walk in the three-CTA form first, then the rest
@@ -236,6 +237,7 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
     if (run_sa && (size_t)N * 2 > 180 * 1024) return fail(MG_ERR_ARG, "mosaic too large for the annealer");
   }
   b->total_cells = cell_base;
+  b->grid_total = grid_base;
   // device buffers
   if (tgt_bytes > 0) MG_CHECK(b->targets.ensure((size_t)tgt_bytes));
   MG_CHECK(b->cell_lab.ensure(sizeof(float4) * std::max(cell_base, 1)));
@@ -484,27 +486,13 @@ int batch_run(mg_batch* b) {
   return MG_OK;
 }
 
-int batch_read(mg_batch* b, int i, mg_result* res) {
-  if (!b->ran) return fail(MG_ERR_STATE, "batch has not run");
-  if (i < 0 || i >= b->n) return fail(MG_ERR_ARG, "mosaic index out of range");
-  mg_ctx* ctx = b->ctx;
-  cudaStream_t s = ctx->stream;
+// Mosaic i's result from its final grid (palette indices), reset count, best
+// chain and chain summaries, read back.
+void fill_result(const mg_batch* b, int i, const int32_t* grid, int resets, int best, const ChainResult* chains,
+                 int n_chains, mg_result* res) {
   const BatchMosaic& M = b->h_mos[i];
-  std::vector<int32_t> grid(M.n);
-  int best = -1, resets = 0;
   ChainResult cr{};
-  // every chain's summary comes back with the grid, so one synchronisation serves the read
-  std::vector<ChainResult> chains(M.run_sa && M.chains > 0 ? M.chains : 0);
-  if (res->image)
-    MG_CUDA(cudaMemcpyAsync(res->image, M.out, (size_t)b->out_w[i] * b->out_h[i] * 3, cudaMemcpyDeviceToHost, s));
-  MG_CUDA(cudaMemcpyAsync(grid.data(), M.final_grid, sizeof(int32_t) * M.n, cudaMemcpyDeviceToHost, s));
-  MG_CUDA(cudaMemcpyAsync(&resets, M.n_resets, sizeof(int), cudaMemcpyDeviceToHost, s));
-  MG_CUDA(cudaMemcpyAsync(&best, M.best_chain, sizeof(int), cudaMemcpyDeviceToHost, s));
-  if (!chains.empty())
-    MG_CUDA(cudaMemcpyAsync(chains.data(), M.results, sizeof(ChainResult) * chains.size(), cudaMemcpyDeviceToHost, s));
-  MG_CUDA(cudaStreamSynchronize(s));
-  MG_CHECK(batch_check(b));
-  if (M.run_sa && best >= 0 && best < (int)chains.size()) cr = chains[best];
+  if (M.run_sa && best >= 0 && best < n_chains) cr = chains[best];
   if (res->grid)
     for (int c = 0; c < M.n; ++c) res->grid[c] = grid[c] < 0 ? -1 : b->pal->selected[grid[c]];
   res->out_w = b->out_w[i];
@@ -517,6 +505,63 @@ int batch_read(mg_batch* b, int i, mg_result* res) {
   res->best_cost = cr.best_cost;
   res->accepted_count = cr.accepted;
   res->improved_count = cr.improved;
+}
+
+int batch_read(mg_batch* b, int i, mg_result* res) {
+  if (!b->ran) return fail(MG_ERR_STATE, "batch has not run");
+  if (i < 0 || i >= b->n) return fail(MG_ERR_ARG, "mosaic index out of range");
+  mg_ctx* ctx = b->ctx;
+  cudaStream_t s = ctx->stream;
+  const BatchMosaic& M = b->h_mos[i];
+  std::vector<int32_t> grid(M.n);
+  int best = -1, resets = 0;
+  // every chain's summary comes back with the grid, so one synchronisation serves the read
+  std::vector<ChainResult> chains(M.run_sa && M.chains > 0 ? M.chains : 0);
+  if (res->image)
+    MG_CUDA(cudaMemcpyAsync(res->image, M.out, (size_t)b->out_w[i] * b->out_h[i] * 3, cudaMemcpyDeviceToHost, s));
+  MG_CUDA(cudaMemcpyAsync(grid.data(), M.final_grid, sizeof(int32_t) * M.n, cudaMemcpyDeviceToHost, s));
+  MG_CUDA(cudaMemcpyAsync(&resets, M.n_resets, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MG_CUDA(cudaMemcpyAsync(&best, M.best_chain, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (!chains.empty())
+    MG_CUDA(cudaMemcpyAsync(chains.data(), M.results, sizeof(ChainResult) * chains.size(), cudaMemcpyDeviceToHost, s));
+  MG_CUDA(cudaStreamSynchronize(s));
+  MG_CHECK(batch_check(b));
+  fill_result(b, i, grid.data(), resets, best, chains.data(), (int)chains.size(), res);
+  return MG_OK;
+}
+
+// Every mosaic's result: the images, then all final grids, reset counts, best
+// chains and chain summaries in one copy each (they are contiguous on the
+// device), and one synchronisation.  (Compositing straight into pinned caller
+// buffers over the CPU-GPU link measured slower than compositing in device
+// memory and copying.)
+int batch_read_all(mg_batch* b, mg_result* res) {
+  if (!b->ran) return fail(MG_ERR_STATE, "batch has not run");
+  const int n = b->n;
+  if (n == 0) return MG_OK;
+  cudaStream_t s = b->ctx->stream;
+  for (int i = 0; i < n; ++i)
+    if (res[i].image)
+      MG_CUDA(cudaMemcpyAsync(res[i].image, b->h_mos[i].out, (size_t)b->out_w[i] * b->out_h[i] * 3,
+                              cudaMemcpyDeviceToHost, s));
+  std::vector<int32_t> grids(std::max(b->grid_total, 1));
+  std::vector<int> resets(n), best(n);
+  std::vector<ChainResult> chains(std::max(b->total_chains, 1));
+  MG_CUDA(cudaMemcpyAsync(grids.data(), b->finals.p, sizeof(int32_t) * b->grid_total, cudaMemcpyDeviceToHost, s));
+  MG_CUDA(cudaMemcpyAsync(resets.data(), b->resets.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  MG_CUDA(cudaMemcpyAsync(best.data(), b->best.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  if (b->total_chains > 0)
+    MG_CUDA(cudaMemcpyAsync(chains.data(), b->results.p, sizeof(ChainResult) * b->total_chains,
+                            cudaMemcpyDeviceToHost, s));
+  MG_CUDA(cudaStreamSynchronize(s));
+  MG_CHECK(batch_check(b));
+  size_t gpos = 0, rpos = 0;
+  for (int i = 0; i < n; ++i) {
+    const BatchMosaic& M = b->h_mos[i];
+    fill_result(b, i, grids.data() + gpos, resets[i], best[i], chains.data() + rpos, M.chains, res + i);
+    gpos += M.n;
+    rpos += M.chains;
+  }
   return MG_OK;
 }
 
@@ -660,16 +705,18 @@ int mg_batch_destroy(mg_batch* b) {
 int mg_generate_batch(mg_ctx* ctx, mg_palette* pal, const mg_mosaic* mosaics, int n, mg_result* results) {
   MG_CHECK(check_ctx(ctx));
   if (n > 0 && !results) return fail(MG_ERR_ARG, "null results");
-  mg_batch b;
-  int st = batch_setup(&b, ctx, pal, mosaics, n, true);
+  // the context keeps the batch (its device buffers only grow) for the next call
+  if (!ctx->gen_batch) ctx->gen_batch = new mg_batch();
+  mg_batch* b = ctx->gen_batch;
+  b->ran = false;
+  int st = batch_setup(b, ctx, pal, mosaics, n, true);
   if (st == MG_OK) {
-    b.tuned = true;  // one-shot: default shapes, no tuning runs
-    st = batch_enqueue(&b, true);
-    b.ran = true;
+    b->tuned = true;  // one-shot: default shapes, no tuning runs
+    st = batch_enqueue(b, true);
+    b->ran = st == MG_OK;
   }
-  for (int i = 0; st == MG_OK && i < n; ++i) st = batch_read(&b, i, results + i);
+  if (st == MG_OK) st = batch_read_all(b, results);
   cudaStreamSynchronize(ctx->stream);
-  batch_release(&b);
   return st;
 }
 
@@ -680,7 +727,7 @@ namespace mg {
 
 mg_batch* server_batch_new() { return new mg_batch(); }
 
-void server_batch_free(mg_batch* b) {
+void batch_free(mg_batch* b) {
   if (!b) return;
   cudaSetDevice(b->device);
   cudaDeviceSynchronize();

@@ -17,10 +17,12 @@ struct mg_ctx {
   int thumb_filter = 0;                   // MG_THUMB_*: how missing thumbnails are made
   mg::ResizePlan resize;                  // mg_resize's tables
   mg::LabIndex nn_index;                  // grid of the last single-call palette
+  mg_batch* gen_batch = nullptr;          // mg_generate_batch's buffers, kept for the next call
 };
 
 namespace mg {
 int check_ctx(mg_ctx* ctx);
+void batch_free(mg_batch* b);  // synchronises the device, releases the batch's buffers, deletes it
 std::vector<float4> to_f4(const float* lab3, int n);
 int upload(mg_ctx* ctx, DevBuf& b, const void* src, size_t bytes);
 int finish(mg_ctx* ctx);

@@ -35,7 +35,7 @@ int server_batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosai
 int server_batch_enqueue(mg_batch* b);
 int server_batch_read(mg_batch* b, int i, mg_result* res);
 mg_batch* server_batch_new();
-void server_batch_free(mg_batch* b);
+void batch_free(mg_batch* b);
 int64_t server_request_bytes(const mg_palette* pal, const mg_mosaic* m);
 }  // namespace mg
 
@@ -310,7 +310,7 @@ int mg_server_destroy(mg_server* S) {
   if (S->dispatcher.joinable()) S->dispatcher.join();
   if (S->completer.joinable()) S->completer.join();
   for (auto& sl : S->slots) {
-    if (sl.batch) server_batch_free(sl.batch);
+    if (sl.batch) batch_free(sl.batch);
     if (sl.done) cudaEventDestroy(sl.done);
     if (sl.ctx) mg_ctx_destroy(sl.ctx);
   }

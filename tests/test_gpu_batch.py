@@ -79,6 +79,27 @@ def test_batch_equals_single_mosaic_path(ctx):
     results, grids, images = job.generate_batch(ctx, pal, reqs)
     for i, (res, grid, image) in enumerate(singles):
         assert np.array_equal(grids[i], grid) and np.array_equal(images[i], image)
+    # again, twice, into pinned buffers (one of them starting one byte past a
+    # 16-byte boundary), the context's batch buffers reused
+    import ctypes as C
+
+    lib = ctx.lib
+    outs, blocks = [], []
+    for i, r in enumerate(reqs):
+        nb = 3 * r.grid_w * r.grid_h * TILE * TILE
+        blk = lib.mg_host_alloc(nb + 16)
+        blocks.append(blk)
+        off = 1 if i == 1 else 0
+        im = np.ctypeslib.as_array(C.cast(blk + off, C.POINTER(C.c_uint8)), shape=(r.grid_h * TILE, r.grid_w * TILE, 3))
+        im[:] = 7
+        outs.append((np.zeros(r.grid_w * r.grid_h, np.int32), im))
+    for rep in range(2):
+        results2, grids2, images2 = job.generate_batch(ctx, pal, reqs, outputs=outs)
+        for i, (res, grid, image) in enumerate(singles):
+            assert np.array_equal(grids2[i], grid) and np.array_equal(images2[i], image), (rep, i)
+            assert results2[i].best_chain == results[i].best_chain and results2[i].n_resets == results[i].n_resets
+    for blk in blocks:
+        lib.mg_host_free(blk)
     batch.close()
     pal.close()
 
