@@ -261,6 +261,10 @@ int mg_ctx_destroy(mg_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->gen_plan) mg_plan_destroy(ctx->gen_plan);
   if (ctx->gen_batch) mg::batch_free(ctx->gen_batch);
+  for (int g = 0; g < mg::kGenGroups; ++g) {
+    if (ctx->gen_sub_batch[g]) mg::batch_free(ctx->gen_sub_batch[g]);
+    if (ctx->gen_sub[g]) mg_ctx_destroy(ctx->gen_sub[g]);
+  }
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->in0, &ctx->in1, &ctx->in2, &ctx->out0, &ctx->out1, &ctx->out2, &ctx->sums, &ctx->regions,
                     &ctx->err, &ctx->lab_consts})

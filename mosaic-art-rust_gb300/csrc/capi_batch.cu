@@ -530,20 +530,25 @@ int batch_read(mg_batch* b, int i, mg_result* res) {
   return MG_OK;
 }
 
-// Every mosaic's result: the images, then all final grids, reset counts, best
-// chains and chain summaries in one copy each (they are contiguous on the
-// device), and one synchronisation.  (Compositing straight into pinned caller
-// buffers over the CPU-GPU link measured slower than compositing in device
-// memory and copying.)
-int batch_read_all(mg_batch* b, mg_result* res) {
+// Every mosaic's image into its result buffer (asynchronous when the buffer
+// is pinned host memory).
+int batch_copy_images(mg_batch* b, mg_result* res) {
+  cudaStream_t s = b->ctx->stream;
+  for (int i = 0; i < b->n; ++i)
+    if (res[i].image)
+      MG_CUDA(cudaMemcpyAsync(res[i].image, b->h_mos[i].out, (size_t)b->out_w[i] * b->out_h[i] * 3,
+                              cudaMemcpyDeviceToHost, s));
+  return MG_OK;
+}
+
+// Every mosaic's other results: all final grids, reset counts, best chains and
+// chain summaries in one copy each (they are contiguous on the device), and
+// one synchronisation.
+int batch_read_rest(mg_batch* b, mg_result* res) {
   if (!b->ran) return fail(MG_ERR_STATE, "batch has not run");
   const int n = b->n;
   if (n == 0) return MG_OK;
   cudaStream_t s = b->ctx->stream;
-  for (int i = 0; i < n; ++i)
-    if (res[i].image)
-      MG_CUDA(cudaMemcpyAsync(res[i].image, b->h_mos[i].out, (size_t)b->out_w[i] * b->out_h[i] * 3,
-                              cudaMemcpyDeviceToHost, s));
   std::vector<int32_t> grids(std::max(b->grid_total, 1));
   std::vector<int> resets(n), best(n);
   std::vector<ChainResult> chains(std::max(b->total_chains, 1));
@@ -563,6 +568,52 @@ int batch_read_all(mg_batch* b, mg_result* res) {
     rpos += M.chains;
   }
   return MG_OK;
+}
+
+// mg_generate_batch of at least kGroupCells cells runs its mosaics as up to
+// kGroups groups (contiguous runs of about equal cells), each a batch on a
+// stream of its own with its targets copied in by the copy engine: one group's
+// uploads and downloads overlap the others' kernels, and the groups' kernels
+// overlap one another.  (Compositing straight into pinned caller buffers over
+// the CPU-GPU link measured slower than compositing in device memory and
+// copying.)
+constexpr int64_t kGroupCells = 16384;
+
+int generate_grouped(mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, int n, mg_result* res, int groups) {
+  std::vector<int> lo(groups + 1, n);
+  int64_t total = 0;
+  for (int i = 0; i < n; ++i) total += (int64_t)ms[i].grid_w * ms[i].grid_h;
+  lo[0] = 0;
+  int64_t acc = 0;
+  for (int i = 0, g = 1; i < n && g < groups; ++i) {
+    acc += (int64_t)ms[i].grid_w * ms[i].grid_h;
+    if (acc * groups >= total * g) lo[g++] = i + 1;
+  }
+  for (int g = 1; g <= groups; ++g) lo[g] = std::max(lo[g], lo[g - 1]);
+  int st = MG_OK;
+  for (int g = 0; g < groups && st == MG_OK; ++g) {
+    if (!ctx->gen_sub[g]) st = mg_ctx_create(ctx->device, &ctx->gen_sub[g]);
+    if (st == MG_OK && !ctx->gen_sub_batch[g]) ctx->gen_sub_batch[g] = new mg_batch();
+  }
+  for (int g = 0; g < groups && st == MG_OK; ++g) {
+    mg_ctx* sc = ctx->gen_sub[g];
+    sc->scoring = ctx->scoring;
+    mg_batch* b = ctx->gen_sub_batch[g];
+    b->ran = false;
+    st = batch_setup(b, sc, pal, ms + lo[g], lo[g + 1] - lo[g], false);
+    if (st == MG_OK) {
+      b->tuned = true;
+      st = batch_enqueue(b, false);
+      b->ran = st == MG_OK;
+    }
+    if (st == MG_OK) st = batch_copy_images(b, res + lo[g]);
+  }
+  for (int g = 0; g < groups; ++g) {
+    if (!ctx->gen_sub[g]) continue;
+    if (st == MG_OK) st = batch_read_rest(ctx->gen_sub_batch[g], res + lo[g]);
+    cudaStreamSynchronize(ctx->gen_sub[g]->stream);
+  }
+  return st;
 }
 
 }  // namespace
@@ -705,6 +756,10 @@ int mg_batch_destroy(mg_batch* b) {
 int mg_generate_batch(mg_ctx* ctx, mg_palette* pal, const mg_mosaic* mosaics, int n, mg_result* results) {
   MG_CHECK(check_ctx(ctx));
   if (n > 0 && !results) return fail(MG_ERR_ARG, "null results");
+  if (!pal || (n > 0 && !mosaics) || n < 0) return fail(MG_ERR_ARG, "invalid batch");
+  int64_t cells = 0;
+  for (int i = 0; i < n; ++i) cells += (int64_t)std::max(mosaics[i].grid_w, 0) * std::max(mosaics[i].grid_h, 0);
+  if (cells >= kGroupCells && n >= 2) return generate_grouped(ctx, pal, mosaics, n, results, std::min(n, kGenGroups));
   // the context keeps the batch (its device buffers only grow) for the next call
   if (!ctx->gen_batch) ctx->gen_batch = new mg_batch();
   mg_batch* b = ctx->gen_batch;
@@ -715,7 +770,8 @@ int mg_generate_batch(mg_ctx* ctx, mg_palette* pal, const mg_mosaic* mosaics, in
     st = batch_enqueue(b, true);
     b->ran = st == MG_OK;
   }
-  if (st == MG_OK) st = batch_read_all(b, results);
+  if (st == MG_OK) st = batch_copy_images(b, results);
+  if (st == MG_OK) st = batch_read_rest(b, results);
   cudaStreamSynchronize(ctx->stream);
   return st;
 }

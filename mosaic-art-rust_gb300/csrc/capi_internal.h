@@ -5,6 +5,10 @@
 
 #include "mg_internal.h"
 
+namespace mg {
+constexpr int kGenGroups = 3;  // streams of a large mg_generate_batch
+}  // namespace mg
+
 struct mg_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -18,6 +22,9 @@ struct mg_ctx {
   mg::ResizePlan resize;                  // mg_resize's tables
   mg::LabIndex nn_index;                  // grid of the last single-call palette
   mg_batch* gen_batch = nullptr;          // mg_generate_batch's buffers, kept for the next call
+  // mg_generate_batch's groups of a large batch: a context (stream) and buffers each
+  mg_ctx* gen_sub[mg::kGenGroups] = {};
+  mg_batch* gen_sub_batch[mg::kGenGroups] = {};
 };
 
 namespace mg {

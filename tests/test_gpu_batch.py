@@ -146,7 +146,9 @@ def test_many_mosaics_take_the_batch_walk_shape(ctx):
     clear inside its common loop; over the dense 10 000-colour palette a fifth of
     the cells have such a window.  Every mosaic must equal the same request as a
     one-mosaic batch (the five-CTA shape, which settles them on its uncommon
-    path), bit for bit, with and without annealing."""
+    path), bit for bit, with and without annealing.  The one-shot
+    mg_generate_batch of these 31 529 cells runs them as three groups on
+    streams of their own, and must equal the batch too."""
     from mosaic_gpu import job
 
     specs, mats, thumbs = job.batched_workload(n=40, seed=424242, scale=0.5)
@@ -155,7 +157,12 @@ def test_many_mosaics_take_the_batch_walk_shape(ctx):
         reqs = job.batched_requests(specs, iterations=iters, chains=2)
         batch = job.Batch(ctx, pal, reqs)
         batch.run()
+        results, grids, images = job.generate_batch(ctx, pal, reqs)
         for i, r in enumerate(reqs):
+            rb, gb, imb = batch.read(i)
+            assert np.array_equal(grids[i], gb) and np.array_equal(images[i], imb), (iters, i)
+            assert results[i].n_resets == rb.n_resets and results[i].best_chain == rb.best_chain
+            assert np.float32(results[i].final_cost) == np.float32(rb.final_cost)
             single = job.Batch(ctx, pal, [r])
             single.run()
             r1, g1, im1 = single.read(0)
