@@ -265,6 +265,11 @@ int mg_ctx_destroy(mg_ctx* ctx) {
     if (ctx->gen_sub_batch[g]) mg::batch_free(ctx->gen_sub_batch[g]);
     if (ctx->gen_sub[g]) mg_ctx_destroy(ctx->gen_sub[g]);
   }
+  for (cudaStream_t cs : {ctx->gen_up, ctx->gen_down})
+    if (cs) {
+      cudaStreamSynchronize(cs);
+      cudaStreamDestroy(cs);
+    }
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf* b : {&ctx->in0, &ctx->in1, &ctx->in2, &ctx->out0, &ctx->out1, &ctx->out2, &ctx->sums, &ctx->regions,
                     &ctx->err, &ctx->lab_consts})

@@ -56,6 +56,9 @@ struct mg_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t ev[5] = {};
+  // mg_generate_batch groups: targets uploaded on another stream (up_done), images
+  // downloaded on another stream after the run (run_done)
+  cudaEvent_t up_done = nullptr, run_done = nullptr;
   bool ran = false;
   bool capturing = false;
   int launches = 0;
@@ -152,12 +155,21 @@ void batch_release(mg_batch* b) {
   b->graph = nullptr;
   for (auto& e : b->ev)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t* e : {&b->up_done, &b->run_done}) {
+    if (*e) cudaEventDestroy(*e);
+    *e = nullptr;
+  }
   release({&b->targets, &b->mos, &b->cell_lab, &b->cell_rgb, &b->cand_idx, &b->cand_dist, &b->grids, &b->finals,
            &b->chain_grids, &b->results, &b->resets, &b->init_cost, &b->best, &b->adj, &b->out, &b->err,
            &b->gjobs, &b->usage, &b->ajobs, &b->chain_job, &b->chain_id, &b->finals_ptr});
 }
 
-int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, int n, bool zero_copy) {
+// wait: return after the uploads have completed (else they may still be in
+// flight, ahead of anything enqueued on the context's stream next).
+// copy_stream: the stream that copies the targets (nullptr: the context's);
+// the context's stream waits for them.
+int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, int n, bool zero_copy,
+                bool wait = true, cudaStream_t copy_stream = nullptr) {
   if (!pal || (n > 0 && !ms) || n < 0) return fail(MG_ERR_ARG, "invalid batch");
   b->ctx = ctx;
   b->device = ctx->device;
@@ -255,16 +267,8 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
   MG_CHECK(b->out.ensure(std::max<size_t>(out_bytes, 16)));
   MG_CHECK(b->err.ensure(16));
   MG_CUDA(cudaMemsetAsync(b->err.p, 0, 16, s));
-  // targets that are not read in place
-  for (int i = 0; i < n; ++i) {
-    if (tgt_off[i] < 0) continue;
-    const mg_mosaic& r = ms[i];
-    const int64_t st = r.target_stride ? r.target_stride : 3ll * r.target_w;
-    uint8_t* dst = b->targets.as<uint8_t>() + tgt_off[i];
-    MG_CUDA(cudaMemcpy2DAsync(dst, 3ull * r.target_w, r.target, st, 3ull * r.target_w, r.target_h,
-                              cudaMemcpyDefault, s));
-    b->h_mos[i].target = dst;
-  }
+  for (int i = 0; i < n; ++i)
+    if (tgt_off[i] >= 0) b->h_mos[i].target = b->targets.as<uint8_t>() + tgt_off[i];
   // per-mosaic device pointers
   size_t gpos = 0, cpos = 0, rpos = 0;
   for (int i = 0; i < n; ++i) {
@@ -351,7 +355,22 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
   MG_CHECK(upload(ctx, b->chain_id, cid.data(), sizeof(int) * cid.size()));
   for (auto& e : b->ev)
     if (!e) MG_CUDA(cudaEventCreate(&e));
-  MG_CUDA(cudaStreamSynchronize(s));
+  // targets that are not read in place, copied last: a copy from pageable host
+  // memory (the uploads above) may wait for the stream's earlier work
+  const cudaStream_t cs = copy_stream ? copy_stream : s;
+  for (int i = 0; i < n; ++i) {
+    if (tgt_off[i] < 0) continue;
+    const mg_mosaic& r = ms[i];
+    const int64_t st = r.target_stride ? r.target_stride : 3ll * r.target_w;
+    MG_CUDA(cudaMemcpy2DAsync(b->targets.as<uint8_t>() + tgt_off[i], 3ull * r.target_w, r.target, st,
+                              3ull * r.target_w, r.target_h, cudaMemcpyDefault, cs));
+  }
+  if (cs != s) {
+    if (!b->up_done) MG_CUDA(cudaEventCreateWithFlags(&b->up_done, cudaEventDisableTiming));
+    MG_CUDA(cudaEventRecord(b->up_done, cs));
+    MG_CUDA(cudaStreamWaitEvent(s, b->up_done, 0));
+  }
+  if (wait) MG_CUDA(cudaStreamSynchronize(s));
   b->ran = false;
   return MG_OK;
 }
@@ -531,9 +550,15 @@ int batch_read(mg_batch* b, int i, mg_result* res) {
 }
 
 // Every mosaic's image into its result buffer (asynchronous when the buffer
-// is pinned host memory).
-int batch_copy_images(mg_batch* b, mg_result* res) {
+// is pinned host memory), on `stream` after the run (nullptr: the context's).
+int batch_copy_images(mg_batch* b, mg_result* res, cudaStream_t stream = nullptr) {
   cudaStream_t s = b->ctx->stream;
+  if (stream && stream != s) {
+    if (!b->run_done) MG_CUDA(cudaEventCreateWithFlags(&b->run_done, cudaEventDisableTiming));
+    MG_CUDA(cudaEventRecord(b->run_done, s));
+    MG_CUDA(cudaStreamWaitEvent(stream, b->run_done, 0));
+    s = stream;
+  }
   for (int i = 0; i < b->n; ++i)
     if (res[i].image)
       MG_CUDA(cudaMemcpyAsync(res[i].image, b->h_mos[i].out, (size_t)b->out_w[i] * b->out_h[i] * 3,
@@ -571,10 +596,11 @@ int batch_read_rest(mg_batch* b, mg_result* res) {
 }
 
 // mg_generate_batch of at least kGroupCells cells runs its mosaics as up to
-// kGroups groups (contiguous runs of about equal cells), each a batch on a
-// stream of its own with its targets copied in by the copy engine: one group's
-// uploads and downloads overlap the others' kernels, and the groups' kernels
-// overlap one another.  (Compositing straight into pinned caller buffers over
+// kGenGroups groups (contiguous runs of about equal cells), each a batch on a
+// stream of its own: the groups' targets are copied in one after another on
+// one stream and their images out one after another on another, so a group's
+// kernels start once its own targets are in, its images leave as soon as it
+// is done, and the groups' kernels overlap one another.  (Compositing straight into pinned caller buffers over
 // the CPU-GPU link measured slower than compositing in device memory and
 // copying.)
 constexpr int64_t kGroupCells = 16384;
@@ -595,24 +621,30 @@ int generate_grouped(mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, int n, m
     if (!ctx->gen_sub[g]) st = mg_ctx_create(ctx->device, &ctx->gen_sub[g]);
     if (st == MG_OK && !ctx->gen_sub_batch[g]) ctx->gen_sub_batch[g] = new mg_batch();
   }
+  for (cudaStream_t* cs : {&ctx->gen_up, &ctx->gen_down})
+    if (st == MG_OK && !*cs && cudaStreamCreateWithFlags(cs, cudaStreamNonBlocking) != cudaSuccess)
+      st = cuda_fail(cudaGetLastError(), "cudaStreamCreateWithFlags");
   for (int g = 0; g < groups && st == MG_OK; ++g) {
     mg_ctx* sc = ctx->gen_sub[g];
     sc->scoring = ctx->scoring;
     mg_batch* b = ctx->gen_sub_batch[g];
     b->ran = false;
-    st = batch_setup(b, sc, pal, ms + lo[g], lo[g + 1] - lo[g], false);
+    st = batch_setup(b, sc, pal, ms + lo[g], lo[g + 1] - lo[g], false, false, ctx->gen_up);
     if (st == MG_OK) {
       b->tuned = true;
       st = batch_enqueue(b, false);
       b->ran = st == MG_OK;
     }
-    if (st == MG_OK) st = batch_copy_images(b, res + lo[g]);
+    if (st == MG_OK) st = batch_copy_images(b, res + lo[g], ctx->gen_down);
   }
   for (int g = 0; g < groups; ++g) {
     if (!ctx->gen_sub[g]) continue;
     if (st == MG_OK) st = batch_read_rest(ctx->gen_sub_batch[g], res + lo[g]);
     cudaStreamSynchronize(ctx->gen_sub[g]->stream);
   }
+  for (cudaStream_t cs : {ctx->gen_up, ctx->gen_down})
+    if (cs && cudaStreamSynchronize(cs) != cudaSuccess && st == MG_OK)
+      st = cuda_fail(cudaGetLastError(), "cudaStreamSynchronize");
   return st;
 }
 

@@ -6,7 +6,7 @@
 #include "mg_internal.h"
 
 namespace mg {
-constexpr int kGenGroups = 3;  // streams of a large mg_generate_batch
+constexpr int kGenGroups = 4;  // streams of a large mg_generate_batch
 }  // namespace mg
 
 struct mg_ctx {
@@ -25,6 +25,7 @@ struct mg_ctx {
   // mg_generate_batch's groups of a large batch: a context (stream) and buffers each
   mg_ctx* gen_sub[mg::kGenGroups] = {};
   mg_batch* gen_sub_batch[mg::kGenGroups] = {};
+  cudaStream_t gen_up = nullptr, gen_down = nullptr;  // their target uploads, their image downloads
 };
 
 namespace mg {

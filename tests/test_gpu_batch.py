@@ -147,7 +147,7 @@ def test_many_mosaics_take_the_batch_walk_shape(ctx):
     the cells have such a window.  Every mosaic must equal the same request as a
     one-mosaic batch (the five-CTA shape, which settles them on its uncommon
     path), bit for bit, with and without annealing.  The one-shot
-    mg_generate_batch of these 31 529 cells runs them as three groups on
+    mg_generate_batch of these 31 529 cells runs them as four groups on
     streams of their own, and must equal the batch too."""
     from mosaic_gpu import job
 
