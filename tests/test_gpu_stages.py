@@ -289,6 +289,8 @@ def test_apply_adjustment_every_colour(ctx, orc):
         bad = np.flatnonzero(np.any(out != ref, axis=-1).ravel())
         assert bad.size == 0, (adj, bad[:5], img.reshape(-1, 3)[bad[:5]], out.reshape(-1, 3)[bad[:5]],
                                ref.reshape(-1, 3)[bad[:5]])
+        odd = np.ascontiguousarray(img[1000:1003, 77:82])  # 15 pixels: an odd count
+        assert np.array_equal(ctx.apply_adjustment(adj, odd), orc.adjust_pixels(np.array(adj, np.float32), odd)), adj
 
 
 @pytest.mark.parametrize("strength", [0.0, 0.4, 1.0])
