@@ -838,12 +838,8 @@ int server_batch_enqueue(mg_batch* b) {
   return MG_OK;
 }
 
-// Every request's results: the images, then the rest in one copy per kind and
-// one synchronisation.
-int server_batch_read_all(mg_batch* b, mg_result* res) {
-  MG_CHECK(batch_copy_images(b, res));
-  return batch_read_rest(b, res);
-}
+// Request i's results, read as soon as they are on the host (its latency ends there).
+int server_batch_read(mg_batch* b, int i, mg_result* res) { return batch_read(b, i, res); }
 
 // Device bytes a request adds to a batch (upper bound; a target in host memory
 // that cannot be read in place counts as copied).

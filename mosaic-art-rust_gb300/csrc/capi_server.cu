@@ -33,7 +33,7 @@ namespace mg {
 // capi_batch.cu
 int server_batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, int n);
 int server_batch_enqueue(mg_batch* b);
-int server_batch_read_all(mg_batch* b, mg_result* res);
+int server_batch_read(mg_batch* b, int i, mg_result* res);
 mg_batch* server_batch_new();
 void batch_free(mg_batch* b);
 int64_t server_request_bytes(const mg_palette* pal, const mg_mosaic* m);
@@ -162,21 +162,14 @@ void complete_loop(mg_server* S) {
     }
     Slot& sl = S->slots[slot];
     if (sl.status == MG_OK && cudaEventSynchronize(sl.done) != cudaSuccess) sl.status = MG_ERR_CUDA;
-    // every request's grid and image, one synchronisation for the batch
-    std::vector<mg_result> res(sl.reqs.size());
-    for (size_t i = 0; i < sl.reqs.size(); ++i) {
-      res[i].grid = sl.reqs[i].grid_out;
-      res[i].image = sl.reqs[i].image_out;
-    }
-    int st = sl.status;
-    if (st == MG_OK && !res.empty()) st = server_batch_read_all(sl.batch, res.data());
-    const Clock::time_point now = Clock::now();
     std::vector<Done> results(sl.reqs.size());
     for (size_t i = 0; i < sl.reqs.size(); ++i) {
       Done& d = results[i];
-      d.status = st;
-      d.res = res[i];
-      d.latency_ms = std::chrono::duration<double, std::milli>(now - sl.reqs[i].submitted).count();
+      d.status = sl.status;
+      d.res.grid = sl.reqs[i].grid_out;
+      d.res.image = sl.reqs[i].image_out;
+      if (d.status == MG_OK) d.status = server_batch_read(sl.batch, (int)i, &d.res);
+      d.latency_ms = std::chrono::duration<double, std::milli>(Clock::now() - sl.reqs[i].submitted).count();
     }
     {
       std::lock_guard<std::mutex> lk(S->mu);
