@@ -5,9 +5,12 @@
 // materials and main.rs:492 / 548 open them with image::open (+ to_rgb8);
 // for JPEG that is zune-jpeg 0.4.18 behind image 0.25.6.  This decoder is the
 // library's own, from ITU-T T.81 (the JPEG standard) and JFIF 1.02:
-//   * sequential DCT with Huffman coding, 8-bit samples (SOF0 baseline, SOF1
-//     extended); progressive (SOF2), lossless and arithmetic-coded files are
-//     refused with MG_ERR_ARG;
+//   * DCT with Huffman coding, 8-bit samples: sequential (SOF0 baseline, SOF1
+//     extended) and progressive (SOF2: spectral selection and successive
+//     approximation, T.81 G.1.2 -- DC first and refinement scans, AC first
+//     scans with end-of-band runs, AC refinement scans with correction bits);
+//     lossless, hierarchical and arithmetic-coded files are refused with
+//     MG_ERR_ARG;
 //   * one component (grey, replicated to RGB) or three (YCbCr per JFIF);
 //     sampling factors 1 or 2 in each direction; interleaved and
 //     one-component scans; 8- and 16-bit quantisation tables; restart
@@ -188,6 +191,10 @@ struct Decoder {
   Err& err;
   int width = 0, height = 0, ncomp = 0, hmax = 1, vmax = 1, mcux = 0, mcuy = 0;
   bool have_frame = false;
+  bool progressive = false;
+  // the current progressive scan: spectral band ss..se, successive approximation ah / al
+  int ss = 0, se = 63, ah = 0, al = 0;
+  int eobrun = 0;  // blocks left in the current end-of-band run
   int restart = 0;
   uint16_t qt[4][64];
   bool qt_set[4] = {false, false, false, false};
@@ -221,9 +228,10 @@ struct Decoder {
   }
 
   bool frame(const uint8_t* s, size_t len, int m) {
-    if (m == 0xC2 || m == 0xC6 || m == 0xCA || m == 0xCE) return err.bad("progressive JPEG is not supported");
-    if (m != 0xC0 && m != 0xC1) return err.bad("lossless, hierarchical or arithmetic-coded JPEG is not supported");
+    if (m != 0xC0 && m != 0xC1 && m != 0xC2)
+      return err.bad("lossless, hierarchical or arithmetic-coded JPEG is not supported");
     if (have_frame) return err.bad("second frame header");
+    progressive = m == 0xC2;
     if (len < 6) return err.bad("short frame header");
     if (s[0] != 8) return err.bad("only 8-bit samples are supported");
     height = s[1] << 8 | s[2];
@@ -316,6 +324,122 @@ struct Decoder {
     return true;
   }
 
+  // Progressive scans (T.81 G.1.2), one block each; coefficients kept in
+  // natural order, scaled by 2^al as they arrive.
+  bool put_coef(int16_t* out, int z, int v) {
+    if (v < -32768 || v > 32767) return err.bad("coefficient out of range");
+    out[z] = (int16_t)v;
+    return true;
+  }
+  // DC first scan: the DC difference, the prediction, the value << al.
+  bool dc_first(Bits& b, Component& c, int16_t* out) {
+    const int t = b.decode(dc[c.td]);
+    if (t < 0 || t > 11) return err.bad("bad DC code");
+    c.pred += extend(b.get(t), t);
+    if (c.pred < -32768 || c.pred > 32767) return err.bad("DC value out of range");
+    return put_coef(out, 0, c.pred * (1 << al));
+  }
+  // DC refinement: one bit, bit al of the DC value.
+  void dc_refine(Bits& b, int16_t* out) {
+    if (b.get(1)) out[0] = (int16_t)(out[0] | (1 << al));
+  }
+  // AC first scan of band ss..se: run/size codes, ZRL, and end-of-band runs
+  // (symbol r << 4 with r < 15: 2^r blocks plus r more bits, this one included).
+  bool ac_first(Bits& b, Component& c, int16_t* out) {
+    if (eobrun > 0) {
+      --eobrun;
+      return true;
+    }
+    const Huff& ha = ac[c.ta];
+    for (int k = ss; k <= se;) {
+      const int rs = b.decode(ha);
+      if (rs < 0) return err.bad("bad AC code");
+      const int r = rs >> 4, sz = rs & 15;
+      if (sz == 0) {
+        if (r == 15) {
+          k += 16;
+          continue;
+        }
+        eobrun = (1 << r) - 1;
+        if (r) eobrun += (int)b.get(r);
+        break;
+      }
+      k += r;
+      if (k > se) return err.bad("AC coefficients run past the band");
+      if (!put_coef(out, kZigzag[k], extend(b.get(sz), sz) * (1 << al))) return false;
+      ++k;
+    }
+    return true;
+  }
+  // A correction bit for a coefficient already nonzero: when set, bit al is
+  // added to its magnitude (if not there yet).
+  bool correct(Bits& b, int16_t* out, int z) {
+    if (!b.get(1)) return true;
+    const int p1 = 1 << al, v = out[z];
+    if ((v & p1) != 0) return true;
+    return put_coef(out, z, v >= 0 ? v + p1 : v - p1);
+  }
+  // AC refinement of band ss..se at bit al: each code places one new
+  // coefficient of magnitude 2^al (its sign the next bit) after r zero-history
+  // positions, or skips 16 of them (ZRL), or starts an end-of-band run; every
+  // already-nonzero coefficient passed on the way takes a correction bit, as do
+  // those of the rest of the block in an end-of-band run.
+  bool ac_refine(Bits& b, Component& c, int16_t* out) {
+    const int p1 = 1 << al;
+    int k = ss;
+    if (eobrun == 0) {
+      const Huff& ha = ac[c.ta];
+      while (k <= se) {
+        const int rs = b.decode(ha);
+        if (rs < 0) return err.bad("bad AC code");
+        int r = rs >> 4;
+        const int sz = rs & 15;
+        int val = 0;
+        if (sz != 0) {
+          if (sz != 1) return err.bad("bad refinement code");
+          val = b.get(1) ? p1 : -p1;
+        } else if (r != 15) {
+          eobrun = 1 << r;
+          if (r) eobrun += (int)b.get(r);
+          break;
+        }
+        bool placed = false;
+        while (k <= se) {
+          const int z = kZigzag[k];
+          if (out[z] != 0) {
+            if (!correct(b, out, z)) return false;
+          } else {
+            if (r == 0) {
+              if (val) out[z] = (int16_t)val;
+              ++k;
+              placed = true;
+              break;
+            }
+            --r;
+          }
+          ++k;
+        }
+        if (!placed && (val != 0 || r > 0)) return err.bad("refinement runs past the band");
+      }
+    }
+    if (eobrun > 0) {
+      for (; k <= se; ++k) {
+        const int z = kZigzag[k];
+        if (out[z] != 0 && !correct(b, out, z)) return false;
+      }
+      --eobrun;
+    }
+    return true;
+  }
+  bool prog_block(Bits& b, Component& c, int16_t* out) {
+    if (ss == 0) {
+      if (ah == 0) return dc_first(b, c, out);
+      dc_refine(b, out);
+      return true;
+    }
+    return ah == 0 ? ac_first(b, c, out) : ac_refine(b, c, out);
+  }
+
   bool scan(const uint8_t* s, size_t len, size_t& pos) {
     if (!have_frame) return err.bad("scan before the frame header");
     if (len < 1) return err.bad("short scan header");
@@ -330,12 +454,29 @@ struct Decoder {
       sc[i] = &comp[j];
       sc[i]->td = s[2 + 2 * i] >> 4;
       sc[i]->ta = s[2 + 2 * i] & 15;
-      if (sc[i]->td > 3 || sc[i]->ta > 3 || !dc[sc[i]->td].present || !ac[sc[i]->ta].present)
-        return err.bad("scan uses a missing Huffman table");
+      if (sc[i]->td > 3 || sc[i]->ta > 3) return err.bad("bad Huffman table index");
       sc[i]->pred = 0;
     }
-    if (s[1 + 2 * ns] != 0 || s[2 + 2 * ns] != 63 || s[3 + 2 * ns] != 0)
-      return err.bad("spectral selection or successive approximation in a sequential scan");
+    ss = s[1 + 2 * ns];
+    se = s[2 + 2 * ns];
+    ah = s[3 + 2 * ns] >> 4;
+    al = s[3 + 2 * ns] & 15;
+    eobrun = 0;
+    if (!progressive) {
+      if (ss != 0 || se != 63 || ah != 0 || al != 0)
+        return err.bad("spectral selection or successive approximation in a sequential scan");
+    } else {
+      if (ss == 0 ? se != 0 : (se < ss || se > 63 || ns != 1))
+        return err.bad("bad spectral selection in a progressive scan");
+      if (al > 13 || (ah != 0 && ah != al + 1)) return err.bad("bad successive approximation");
+    }
+    // the tables a scan decodes with: DC codes in sequential and first DC
+    // scans, AC codes in sequential and AC scans (a DC refinement uses none)
+    for (int i = 0; i < ns; ++i) {
+      const bool need_dc = !progressive || (ss == 0 && ah == 0), need_ac = !progressive || ss > 0;
+      if ((need_dc && !dc[sc[i]->td].present) || (need_ac && !ac[sc[i]->ta].present))
+        return err.bad("scan uses a missing Huffman table");
+    }
     // entropy-coded data
     Bits b{d + pos, d + n};
     int mx, my;
@@ -354,12 +495,14 @@ struct Decoder {
         if (!b.restart(next_rst)) return err.bad("restart marker missing or out of order");
         next_rst = (next_rst + 1) & 7;
         for (int i = 0; i < ns; ++i) sc[i]->pred = 0;
+        eobrun = 0;
         left = restart;
       }
       if (ns == 1) {
         Component& c = *sc[0];
         const int bx = (int)(u % mx), by = (int)(u / mx);
-        if (!block(b, c, c.coef.data() + ((size_t)by * c.bw + bx) * 64)) return false;
+        int16_t* blk = c.coef.data() + ((size_t)by * c.bw + bx) * 64;
+        if (!(progressive ? prog_block(b, c, blk) : block(b, c, blk))) return false;
       } else {
         const int ux = (int)(u % mx), uy = (int)(u / mx);
         for (int i = 0; i < ns; ++i) {
@@ -367,7 +510,8 @@ struct Decoder {
           for (int y = 0; y < c.v; ++y)
             for (int x = 0; x < c.h; ++x) {
               const int bx = ux * c.h + x, by = uy * c.v + y;
-              if (!block(b, c, c.coef.data() + ((size_t)by * c.bw + bx) * 64)) return false;
+              int16_t* blk = c.coef.data() + ((size_t)by * c.bw + bx) * 64;
+              if (!(progressive ? prog_block(b, c, blk) : block(b, c, blk))) return false;
             }
         }
       }

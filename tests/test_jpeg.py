@@ -1,10 +1,12 @@
 """JPEG materials (main.rs:172-185 accepts jpg/jpeg; main.rs:492/548 image::open),
 decoded by csrc/io_jpeg.cpp, on the CPU.
 
-The files are written here by a small baseline encoder of this test's own
-(ITU-T T.81: JFIF YCbCr, FDCT in float64, quantisation, DC/AC Huffman codes
-built from the symbol counts of the image, optional restart intervals, one
-interleaved scan or one scan per component, 4:4:4 / 4:2:2 / 4:2:0 / grey).
+The files are written here by a small encoder of this test's own (ITU-T T.81:
+JFIF YCbCr, FDCT in float64, quantisation, DC/AC Huffman codes built from the
+symbol counts of the image, optional restart intervals, one interleaved scan
+or one scan per component, 4:4:4 / 4:2:2 / 4:2:0 / grey; and the same
+coefficients as progressive files by a scan script of spectral bands and
+successive-approximation bit planes).
 Because the encoder keeps the quantised coefficients, the decoder can be held
 to a float32 restatement of its own output steps (T.81 A.3.3 inverse DCT in
 the same order, replication upsampling, the JFIF colour equations) bit for
@@ -117,10 +119,9 @@ def _segment(marker, payload):
     return bytes([0xFF, marker]) + struct.pack(">H", len(payload) + 2) + payload
 
 
-def encode_jpeg(img, sampling=(1, 1), quant=1, restart=0, interleaved=True, grey=False):
-    """img: (h, w, 3) uint8 (or (h, w) for grey).  sampling: the luma factors (h, v)
-    with chroma at 1x1.  quant: one quantiser for every coefficient.  Returns
-    (file bytes, {component: quantised coefficients (bh, bw, 64) natural order}, planes)."""
+def _coefficients(img, sampling, quant, grey):
+    """The quantised DCT coefficients of each component: ({cid: (bh, bw, 64) natural
+    order}, [(cid, h, v)], {cid: the component's own block grid (bx, by)}, mcux, mcuy)."""
     if grey:
         planes = [img.astype(np.float64)]
         comps = [(1, 1, 1)]
@@ -149,6 +150,40 @@ def encode_jpeg(img, sampling=(1, 1), quant=1, restart=0, interleaved=True, grey
         q = np.floor(F / quant + 0.5).astype(np.int32)
         coefs[cid] = q.reshape(bh, bw, 64)
         scan_blocks[cid] = (-(-cw // 8), -(-ch // 8))  # the component's own grid (one-component scans)
+    return coefs, comps, scan_blocks, mcux, mcuy
+
+
+def _unit_order(cid_list, comps, scan_blocks, mcux, mcuy):
+    """The scan's units, each a list of (cid, block row, block column): a
+    one-component scan walks the component's own grid, an interleaved one the MCUs."""
+    if len(cid_list) == 1:
+        cid = cid_list[0]
+        bx, by = scan_blocks[cid]
+        return [[(cid, y, x)] for y in range(by) for x in range(bx)]
+    units = []
+    for uy in range(mcuy):
+        for ux in range(mcux):
+            units.append([(cid, uy * vs + y, ux * hs + x) for (cid, hs, vs) in comps if cid in cid_list
+                          for y in range(vs) for x in range(hs)])
+    return units
+
+
+def _headers(comps, quant, grey, H, W, sof_marker):
+    out = b"\xff\xd8" + _segment(0xE0, b"JFIF\x00\x01\x02\x00\x00\x01\x00\x01\x00\x00")
+    out += _segment(0xDB, bytes([0]) + bytes([quant] * 64) + (bytes([1]) + bytes([quant] * 64) if not grey else b""))
+    sof = struct.pack(">BHHB", 8, H, W, len(comps))
+    for cid, hs, vs in comps:
+        sof += bytes([cid, (hs << 4) | vs, 0 if cid == 1 else 1])
+    return out + _segment(sof_marker, sof)
+
+
+def encode_jpeg(img, sampling=(1, 1), quant=1, restart=0, interleaved=True, grey=False):
+    """img: (h, w, 3) uint8 (or (h, w) for grey).  sampling: the luma factors (h, v)
+    with chroma at 1x1.  quant: one quantiser for every coefficient.  Returns
+    (file bytes, {component: quantised coefficients (bh, bw, 64) natural order}, planes)."""
+    H, W = img.shape[:2]
+    coefs, comps, scan_blocks, mcux, mcuy = _coefficients(img, sampling, quant, grey)
+
     # entropy-code the scans, collecting symbols first for the Huffman codes
     def mcu_order(cid_list):
         if len(cid_list) == 1:
@@ -214,12 +249,7 @@ def encode_jpeg(img, sampling=(1, 1), quant=1, restart=0, interleaved=True, grey
         counts, order, code = _canonical(_huffman_lengths(freq))
         codes[(kind, t)] = code
         dht += bytes([(0 if kind == "dc" else 16) | t]) + bytes(counts) + bytes(order)
-    out = b"\xff\xd8" + _segment(0xE0, b"JFIF\x00\x01\x02\x00\x00\x01\x00\x01\x00\x00")
-    out += _segment(0xDB, bytes([0]) + bytes([quant] * 64) + (bytes([1]) + bytes([quant] * 64) if not grey else b""))
-    sof = struct.pack(">BHHB", 8, H, W, len(comps))
-    for cid, hs, vs in comps:
-        sof += bytes([cid, (hs << 4) | vs, 0 if cid == 1 else 1])
-    out += _segment(0xC0, sof) + _segment(0xC4, dht)
+    out = _headers(comps, quant, grey, H, W, 0xC0) + _segment(0xC4, dht)
     if restart:
         out += _segment(0xDD, struct.pack(">H", restart))
     for sc, events in streams:
@@ -238,6 +268,137 @@ def encode_jpeg(img, sampling=(1, 1), quant=1, restart=0, interleaved=True, grey
             bw.put(c, n)
             if e[4]:
                 bw.put(e[3], e[4])
+        bw.pad()
+        out += bytes(bw.out)
+    return out + b"\xff\xd9", coefs, comps
+
+
+PROGRESSIVE_COLOUR = [((1, 2, 3), 0, 0, 0, 1), ((1,), 1, 5, 0, 2), ((3,), 1, 63, 0, 1), ((2,), 1, 63, 0, 1),
+                      ((1,), 6, 63, 0, 2), ((1,), 1, 63, 2, 1), ((1, 2, 3), 0, 0, 1, 0), ((3,), 1, 63, 1, 0),
+                      ((2,), 1, 63, 1, 0), ((1,), 1, 63, 1, 0)]
+PROGRESSIVE_SEPARATE_DC = [((1,), 0, 0, 0, 2), ((2,), 0, 0, 0, 0), ((3,), 0, 0, 0, 0), ((1,), 1, 63, 0, 3),
+                           ((1,), 0, 0, 2, 1), ((1,), 1, 63, 3, 2), ((1,), 1, 63, 2, 1), ((1,), 0, 0, 1, 0),
+                           ((1,), 1, 9, 1, 0), ((1,), 10, 63, 1, 0), ((2,), 1, 63, 0, 0), ((3,), 1, 63, 0, 0)]
+PROGRESSIVE_GREY = [((1,), 0, 0, 0, 1), ((1,), 1, 5, 0, 2), ((1,), 6, 63, 0, 2), ((1,), 1, 63, 2, 1),
+                    ((1,), 0, 0, 1, 0), ((1,), 1, 63, 1, 0)]
+
+
+def encode_jpeg_progressive(img, sampling=(1, 1), quant=1, restart=0, grey=False, script=None):
+    """The same quantised coefficients as encode_jpeg, written as a progressive
+    file (SOF2) by the scan script [(components, Ss, Se, Ah, Al)]: DC first and
+    refinement scans, AC first scans with end-of-band runs, AC refinement scans
+    with correction bits (T.81 G.1.2), a Huffman table per scan from its own
+    symbol counts.  Returns (file bytes, coefficients, components)."""
+    H, W = img.shape[:2]
+    coefs, comps, scan_blocks, mcux, mcuy = _coefficients(img, sampling, quant, grey)
+    script = script or (PROGRESSIVE_GREY if grey else PROGRESSIVE_COLOUR)
+    out = _headers(comps, quant, grey, H, W, 0xC2)
+    if restart:
+        out += _segment(0xDD, struct.pack(">H", restart))
+    for cids, ss, se, ah, al in script:
+        units = _unit_order(list(cids), comps, scan_blocks, mcux, mcuy)
+        ev = []  # ("sym", symbol, value, bits) | ("bits", value, bits) | ("rst", n)
+        st = {"eobrun": 0, "be": []}
+
+        def flush_eobrun():
+            n = st["eobrun"]
+            if n:
+                nb = n.bit_length() - 1
+                ev.append(("sym", nb << 4, n - (1 << nb), nb))
+                for bit in st["be"]:
+                    ev.append(("bits", bit, 1))
+            st["eobrun"], st["be"] = 0, []
+
+        pred = {c: 0 for c in cids}
+        for ui, unit in enumerate(units):
+            if restart and ui and ui % restart == 0:
+                flush_eobrun()
+                ev.append(("rst", (ui // restart - 1) % 8))
+                pred = {c: 0 for c in cids}
+            for cid, by, bx in unit:
+                zz = [int(v) for v in coefs[cid][by, bx][ZIGZAG]]
+                if ss == 0 and ah == 0:  # DC first: arithmetic shift by al, then the difference
+                    v = zz[0] >> al
+                    diff, pred[cid] = v - pred[cid], v
+                    t = _category(diff)
+                    ev.append(("sym", t, diff if diff >= 0 else diff + (1 << t) - 1, t))
+                elif ss == 0:  # DC refinement: bit al
+                    ev.append(("bits", (zz[0] >> al) & 1, 1))
+                elif ah == 0:  # AC first: magnitudes shifted by al, signs kept
+                    vals = [(1 if c > 0 else -1) * (abs(c) >> al) for c in zz[ss:se + 1]]
+                    nz = [i for i, v in enumerate(vals) if v]
+                    if not nz:
+                        st["eobrun"] += 1
+                        if st["eobrun"] == 0x7FFF:
+                            flush_eobrun()
+                        continue
+                    flush_eobrun()
+                    run = 0
+                    for v in vals[:nz[-1] + 1]:
+                        if v == 0:
+                            run += 1
+                            continue
+                        while run > 15:
+                            ev.append(("sym", 0xF0, 0, 0))
+                            run -= 16
+                        t = _category(v)
+                        ev.append(("sym", (run << 4) | t, v if v >= 0 else v + (1 << t) - 1, t))
+                        run = 0
+                    if nz[-1] < len(vals) - 1:
+                        st["eobrun"] += 1
+                        if st["eobrun"] == 0x7FFF:
+                            flush_eobrun()
+                else:  # AC refinement at bit al
+                    absv = [abs(c) >> al for c in zz[ss:se + 1]]
+                    eob = max([i for i, t in enumerate(absv) if t == 1], default=-1)
+                    r, br = 0, []
+                    for i, t in enumerate(absv):
+                        if t == 0:
+                            r += 1
+                            continue
+                        while r > 15 and i <= eob:
+                            flush_eobrun()
+                            ev.append(("sym", 0xF0, 0, 0))
+                            r -= 16
+                            ev.extend(("bits", bit, 1) for bit in br)
+                            br = []
+                        if t > 1:
+                            br.append(t & 1)
+                            continue
+                        flush_eobrun()
+                        ev.append(("sym", (r << 4) | 1, 1 if zz[ss + i] > 0 else 0, 1))
+                        ev.extend(("bits", bit, 1) for bit in br)
+                        br, r = [], 0
+                    if r > 0 or br:
+                        st["eobrun"] += 1
+                        st["be"] += br
+                        if st["eobrun"] == 0x7FFF or len(st["be"]) > 937:
+                            flush_eobrun()
+        flush_eobrun()
+        freq = {}
+        for e in ev:
+            if e[0] == "sym":
+                freq[e[1]] = freq.get(e[1], 0) + 1
+        code = {}
+        if freq:
+            counts, order, code = _canonical(_huffman_lengths(freq))
+            out += _segment(0xC4, bytes([(0 if ss == 0 else 16)]) + bytes(counts) + bytes(order))
+        sos = bytes([len(cids)])
+        for cid in cids:
+            sos += bytes([cid, 0])
+        out += _segment(0xDA, sos + bytes([ss, se, (ah << 4) | al]))
+        bw = _BitWriter()
+        for e in ev:
+            if e[0] == "rst":
+                bw.pad()
+                bw.out += bytes([0xFF, 0xD0 + e[1]])
+            elif e[0] == "bits":
+                bw.put(e[1], e[2])
+            else:
+                c, n = code[e[1]]
+                bw.put(c, n)
+                if e[3]:
+                    bw.put(e[2], e[3])
         bw.pad()
         out += bytes(bw.out)
     return out + b"\xff\xd9", coefs, comps
@@ -316,6 +477,32 @@ def test_decode_equals_restated_steps(capi, sampling, quant, restart, interleave
             assert np.abs(got.astype(np.int16) - img.astype(np.int16)).max() <= 5
 
 
+PROG_CASES = [((1, 1), 1, 0, False, None), ((2, 2), 2, 0, False, None), ((2, 1), 1, 3, False, None),
+              ((2, 2), 4, 2, False, PROGRESSIVE_SEPARATE_DC), ((1, 2), 3, 0, False, PROGRESSIVE_SEPARATE_DC),
+              ((1, 1), 1, 0, True, None), ((1, 1), 2, 4, True, None)]
+
+
+@pytest.mark.parametrize("sampling,quant,restart,grey,script", PROG_CASES)
+@pytest.mark.parametrize("size", [(64, 48), (37, 29), (8, 8), (1, 1), (250, 3), (130, 70)])
+def test_progressive_decodes_like_the_sequential_file(capi, sampling, quant, restart, grey, script, size):
+    """A progressive file (SOF2: DC first and refinement scans, interleaved or
+    not; AC first scans over spectral bands with end-of-band runs; AC
+    refinement scans with correction bits; restart intervals) carries the same
+    quantised coefficients as the sequential file of the same image, so both
+    decode to the same pixels -- and to the restated output steps."""
+    rng = np.random.default_rng(size[0] * 13 + quant + 7 * restart)
+    for kind in ("smooth", "noise"):
+        img = _image(rng, *size, kind)
+        if grey:
+            img = img[..., 0]
+        data, coefs, comps = encode_jpeg_progressive(img, sampling, quant, restart, grey, script)
+        seq = encode_jpeg(img, sampling, quant, 0, True, grey)[0]
+        assert capi.image_info(data) == size
+        got = capi.image_decode(data)
+        assert np.array_equal(got, capi.image_decode(seq)), (kind, sampling, restart, script is None)
+        assert np.array_equal(got, decode_restated(coefs, comps, quant, *size)), kind
+
+
 def test_grey_blocks_decode_exactly(capi):
     """A grey image of 8x8 blocks of one level each, at quantiser 1: every block is
     its DC term alone, so the decoded pixels are the source's."""
@@ -350,8 +537,9 @@ def test_defects_fail_cleanly(capi):
         return lib.mg_image_decode(d, len(d), _capi.ptr(out, np.ctypeslib.ctypes.c_uint8), 64 * 3)
 
     assert code(data) == _capi.MG_OK
-    prog = data.replace(b"\xff\xc0", b"\xff\xc2", 1)
+    prog = data.replace(b"\xff\xc0", b"\xff\xc2", 1)  # a sequential scan in a progressive frame
     assert code(prog) == _capi.MG_ERR_ARG and b"progressive" in lib.mg_last_error()
+    assert code(data.replace(b"\xff\xc0", b"\xff\xc3", 1)) == _capi.MG_ERR_ARG  # lossless
     assert code(data[:2] + b"\xff\xcc\x00\x04\x00\x00" + data[2:]) == _capi.MG_ERR_ARG  # arithmetic coding
     for cut in range(0, len(data), 3):  # truncation anywhere: an error or a decode, never a crash
         assert code(data[:cut]) in (_capi.MG_OK, _capi.MG_ERR_ARG)
@@ -403,6 +591,11 @@ def test_fuzz_under_sanitizers(tmp_path, capi):
     p = tmp_path / "grey.jpg"
     p.write_bytes(encode_jpeg(_image(rng, 30, 20, "smooth")[..., 0], quant=2, restart=2, grey=True)[0])
     seeds.append(str(p))
+    for i, (sampling, quant, restart, grey, script) in enumerate(PROG_CASES):
+        img = _image(rng, 21 + 4 * i, 13 + 5 * i, "noise" if i % 2 else "smooth")
+        p = tmp_path / f"p{i}.jpg"
+        p.write_bytes(encode_jpeg_progressive(img[..., 0] if grey else img, sampling, quant, restart, grey, script)[0])
+        seeds.append(str(p))
     env = dict(__import__("os").environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=0")
     r = subprocess.run([str(exe), "1500", *seeds], capture_output=True, text=True, timeout=600, env=env)
     assert r.returncode == 0, r.stdout + r.stderr[-3000:]
