@@ -175,6 +175,15 @@ struct Bits {
   }
 };
 
+// v rounded to the nearest integer (ties to even, as lrintf) and clamped to
+// 0..255: v is clamped to [-1, 256] first (which rounds to the same clamped
+// byte), then 1.5 * 2^23 + v, whose unit in the last place is 1, rounds it.
+inline uint8_t round_clamp_u8(float v) {
+  v = v < -1.0f ? -1.0f : (v > 256.0f ? 256.0f : v);
+  const int iv = (int)((v + 12582912.0f) - 12582912.0f);
+  return (uint8_t)(iv < 0 ? 0 : (iv > 255 ? 255 : iv));
+}
+
 inline int extend(uint32_t v, int s) { return s == 0 ? 0 : (v < (1u << (s - 1)) ? (int)v - (1 << s) + 1 : (int)v); }
 
 struct Component {
@@ -574,32 +583,37 @@ struct Decoder {
   }
 
   // T.81 A.3.3 inverse DCT of one dequantised block, rows then columns, FP32,
-  // + 128, rounded to nearest, clamped.
-  static void idct(const int16_t* in, const uint16_t* q, uint8_t* out, int stride, const float (&cs)[8][8]) {
+  // + 128, rounded to nearest, clamped.  Each output is a sum from 0 over the
+  // eight frequencies in order; the loops run the eight outputs of a row (or
+  // column pass) side by side (ct[u][x] = cs[x][u]) so that the compiler can
+  // keep them in vector lanes without reordering any sum.
+  static void idct(const int16_t* in, const uint16_t* q, uint8_t* out, int stride, const float (&ct)[8][8]) {
     float t[64];
     for (int u = 0; u < 64; ++u) t[u] = (float)in[u] * (float)q[u];
     float r[64];
-    for (int y = 0; y < 8; ++y)  // 1-D over the horizontal frequency of each row
-      for (int x = 0; x < 8; ++x) {
-        float s = 0.0f;
-        for (int u = 0; u < 8; ++u) s += cs[x][u] * t[y * 8 + u];
-        r[y * 8 + x] = s;
+    for (int y = 0; y < 8; ++y) {  // 1-D over the horizontal frequency of each row
+      float s[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+      for (int u = 0; u < 8; ++u) {
+        const float tu = t[y * 8 + u];
+        for (int x = 0; x < 8; ++x) s[x] += ct[u][x] * tu;
       }
-    for (int x = 0; x < 8; ++x)
-      for (int y = 0; y < 8; ++y) {
-        float s = 0.0f;
-        for (int v = 0; v < 8; ++v) s += cs[y][v] * r[v * 8 + x];
-        const float val = s + 128.0f;
-        const long iv = std::lrintf(val);
-        out[y * stride + x] = (uint8_t)(iv < 0 ? 0 : (iv > 255 ? 255 : iv));
+      for (int x = 0; x < 8; ++x) r[y * 8 + x] = s[x];
+    }
+    for (int y = 0; y < 8; ++y) {  // then over the vertical frequency of each column
+      float s[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+      for (int v = 0; v < 8; ++v) {
+        const float c = ct[v][y];
+        for (int x = 0; x < 8; ++x) s[x] += c * r[v * 8 + x];
       }
+      for (int x = 0; x < 8; ++x) out[y * stride + x] = round_clamp_u8(s[x] + 128.0f);
+    }
   }
 
   bool output(uint8_t* out, int64_t stride) {
-    float cs[8][8];  // C(u)/2 cos((2x+1) u pi / 16)
+    float ct[8][8];  // ct[u][x] = C(u)/2 cos((2x+1) u pi / 16)
     for (int x = 0; x < 8; ++x)
       for (int u = 0; u < 8; ++u)
-        cs[x][u] = (float)((u == 0 ? std::sqrt(0.5) : 1.0) * 0.5 * std::cos((2 * x + 1) * u * M_PI / 16.0));
+        ct[u][x] = (float)((u == 0 ? std::sqrt(0.5) : 1.0) * 0.5 * std::cos((2 * x + 1) * u * M_PI / 16.0));
     std::vector<std::vector<uint8_t>> plane(ncomp);
     for (int i = 0; i < ncomp; ++i) {
       Component& c = comp[i];
@@ -608,7 +622,7 @@ struct Decoder {
       for (int by = 0; by < c.bh; ++by)
         for (int bx = 0; bx < c.bw; ++bx)
           idct(c.coef.data() + ((size_t)by * c.bw + bx) * 64, qt[c.tq], plane[i].data() + (size_t)by * 8 * pw + bx * 8,
-               pw, cs);
+               pw, ct);
     }
     for (int y = 0; y < height; ++y) {
       uint8_t* o = out + (int64_t)y * stride;
@@ -618,20 +632,18 @@ struct Decoder {
         continue;
       }
       const uint8_t* row[3];
-      int sx[3];
+      int sh[3];  // horizontal replication: x >> sh (factors 1 or 2)
       for (int i = 0; i < 3; ++i) {
         const Component& c = comp[i];
         const int yy = y * c.v / vmax;  // replication
         row[i] = plane[i].data() + (size_t)yy * c.bw * 8;
-        sx[i] = hmax / c.h;
+        sh[i] = hmax / c.h == 2 ? 1 : 0;
       }
       for (int x = 0; x < width; ++x) {
-        const float Y = row[0][x / sx[0]], cb = row[1][x / sx[1]] - 128.0f, cr = row[2][x / sx[2]] - 128.0f;
-        const float rgb[3] = {Y + 1.402f * cr, Y - 0.344136f * cb - 0.714136f * cr, Y + 1.772f * cb};
-        for (int c = 0; c < 3; ++c) {
-          const long iv = std::lrintf(rgb[c]);
-          o[3 * x + c] = (uint8_t)(iv < 0 ? 0 : (iv > 255 ? 255 : iv));
-        }
+        const float Y = row[0][x >> sh[0]], cb = row[1][x >> sh[1]] - 128.0f, cr = row[2][x >> sh[2]] - 128.0f;
+        o[3 * x] = round_clamp_u8(Y + 1.402f * cr);
+        o[3 * x + 1] = round_clamp_u8(Y - 0.344136f * cb - 0.714136f * cr);
+        o[3 * x + 2] = round_clamp_u8(Y + 1.772f * cb);
       }
     }
     return true;
