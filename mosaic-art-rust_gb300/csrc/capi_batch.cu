@@ -39,7 +39,7 @@ struct mg_batch {
   mg_ctx* ctx = nullptr;
   int device = 0;  // destroy must not touch ctx, which may already be gone
   mg_palette* pal = nullptr;
-  int n = 0, total_cells = 0, max_gw = 0, max_cells = 0, max_sa_cells = 0, min_sa_cells = 0, max_out_px = 0;
+  int n = 0, total_cells = 0, max_gw = 0, max_cells = 0, max_sa_cells = 0, min_sa_cells = 0;
   int total_chains = 0;
   std::vector<BatchMosaic> h_mos;
   std::vector<int> cells, out_w, out_h, chains;
@@ -189,7 +189,7 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
   size_t out_bytes = 0, chain_cells = 0, n_results = 0;
   int cell_base = 0, grid_base = 0;
   b->total_chains = 0;
-  b->max_gw = b->max_cells = b->max_sa_cells = b->min_sa_cells = b->max_out_px = 0;
+  b->max_gw = b->max_cells = b->max_sa_cells = b->min_sa_cells = 0;
   for (int i = 0; i < n; ++i) {
     const mg_mosaic& r = ms[i];
     const int64_t st = r.target_stride ? r.target_stride : 3ll * r.target_w;
@@ -245,7 +245,6 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
       b->min_sa_cells = b->max_sa_cells == 0 ? N : std::min(b->min_sa_cells, N);
       b->max_sa_cells = std::max(b->max_sa_cells, N);
     }
-    b->max_out_px = std::max(b->max_out_px, b->out_w[i] * b->out_h[i]);
     if (run_sa && (size_t)N * 2 > 180 * 1024) return fail(MG_ERR_ARG, "mosaic too large for the annealer");
   }
   b->total_cells = cell_base;
@@ -422,7 +421,7 @@ int batch_enqueue(mg_batch* b, bool with_events) {
   if (with_events) MG_CUDA(record(b, b->ev[3], s));
   MG_CHECK(launch_batch_finish(b->mos.as<BatchMosaic>(), n, b->total_cells, pal->thumb_rgb.as<uchar4>(),
                                b->cell_rgb.as<uchar4>(), b->adj.as<float4>(), pal->thumbs.as<uint8_t>(), pal->tw,
-                               pal->th, b->max_out_px, s));
+                               pal->th, s));
   if (with_events) MG_CUDA(record(b, b->ev[4], s));
   b->launches = (int)(g_launches - l0);
   return MG_OK;

@@ -158,8 +158,7 @@ int launch_batch_cells(const BatchMosaic* mos, int nm, int total_cells, const La
 }
 
 int launch_batch_finish(const BatchMosaic* mos, int nm, int total_cells, const uchar4* thumb_rgb,
-                        const uchar4* cell_rgb, float4* adj, const uint8_t* thumbs, int tw, int th, int max_out_px,
-                        cudaStream_t stream) {
+                        const uchar4* cell_rgb, float4* adj, const uint8_t* thumbs, int tw, int th, cudaStream_t stream) {
   if (nm <= 0) return MG_OK;
   batch_adjust_kernel<<<(total_cells + 255) / 256, 256, 0, stream>>>(mos, nm, total_cells, thumb_rgb, cell_rgb, adj);
   int dev = 0, sms = 0;

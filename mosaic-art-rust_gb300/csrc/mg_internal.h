@@ -204,8 +204,7 @@ const LabConsts& host_lab_consts();
 int launch_batch_cells(const BatchMosaic* mos, int nm, int total_cells, const LabConsts* consts, float4* lab,
                        uchar4* rgb, int warps, cudaStream_t stream);
 int launch_batch_finish(const BatchMosaic* mos, int nm, int total_cells, const uchar4* thumb_rgb,
-                        const uchar4* cell_rgb, float4* adj, const uint8_t* thumbs, int tw, int th, int max_out_px,
-                        cudaStream_t stream);
+                        const uchar4* cell_rgb, float4* adj, const uint8_t* thumbs, int tw, int th, cudaStream_t stream);
 
 // (f) colour adjustment + composite.
 int launch_cell_adjust(const int32_t* grid, int n_cells, const uchar4* thumb_rgb, const uchar4* cell_rgb,

@@ -11,8 +11,10 @@
 
 #if defined(__CUDACC__)
 #define MG_HD __host__ __device__ __forceinline__
+#define MG_UNROLL _Pragma("unroll")
 #else
 #define MG_HD inline
+#define MG_UNROLL
 #endif
 
 #if defined(__CUDA_ARCH__)
@@ -88,7 +90,7 @@ MG_HD void mulhilo(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo) {
 }
 
 MG_HD u32x4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1) {
-#pragma unroll
+MG_UNROLL
   for (int r = 0; r < 10; ++r) {
     uint32_t hi0, lo0, hi1, lo1;
     mulhilo(0xD2511F53u, c0, hi0, lo0);
@@ -149,7 +151,7 @@ MG_HD float exp_spec(float x) {
 constexpr int kCbrtNewton = 2;
 MG_HD float cbrt_spec(float t) {
   float r = u2f(0x54A2FA8Cu - f2u(t) / 3u);
-#pragma unroll
+MG_UNROLL
   for (int k = 0; k < kCbrtNewton; ++k) {
     float r2 = MG_MUL(r, r);
     float r3 = MG_MUL(r2, r);
