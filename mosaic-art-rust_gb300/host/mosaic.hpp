@@ -298,6 +298,209 @@ class UsageTracker {
 };
 
 // ---- similarity.rs ---------------------------------------------------------------------
+namespace detail {
+// A small JSON reader and writer for the crate's similarity database files
+// (serde_json of similarity.rs:31-41).  Numbers keep their text, so that a
+// float is converted once (strtof: the exact f32 the crate wrote) and an index
+// as an integer.
+struct Json {
+  enum Kind { kNull, kBool, kNum, kStr, kArr, kObj } kind = kNull;
+  bool b = false;
+  std::string text;  // a number's token, or a string's decoded UTF-8
+  std::vector<Json> arr;
+  std::vector<std::pair<std::string, Json>> obj;
+  const Json* get(const std::string& key) const {
+    for (const auto& kv : obj)
+      if (kv.first == key) return &kv.second;
+    return nullptr;
+  }
+};
+
+class JsonReader {
+ public:
+  JsonReader(const std::string& s, const Path& file) : p_(s.data()), e_(s.data() + s.size()), file_(file) {}
+  Json document() {
+    Json v = value(0);
+    ws();
+    if (p_ != e_) fail("trailing characters");
+    return v;
+  }
+
+ private:
+  const char* p_;
+  const char* e_;
+  const Path& file_;
+  [[noreturn]] void fail(const char* what) { throw Error(MG_ERR_ARG, std::string("JSON: ") + what + ": " + file_.string()); }
+  void ws() {
+    while (p_ != e_ && (*p_ == ' ' || *p_ == '\t' || *p_ == '\n' || *p_ == '\r')) ++p_;
+  }
+  bool take(char c) {
+    ws();
+    if (p_ != e_ && *p_ == c) {
+      ++p_;
+      return true;
+    }
+    return false;
+  }
+  static void utf8(std::string& out, uint32_t cp) {
+    if (cp < 0x80) {
+      out += (char)cp;
+    } else if (cp < 0x800) {
+      out += (char)(0xC0 | cp >> 6);
+      out += (char)(0x80 | (cp & 0x3F));
+    } else if (cp < 0x10000) {
+      out += (char)(0xE0 | cp >> 12);
+      out += (char)(0x80 | ((cp >> 6) & 0x3F));
+      out += (char)(0x80 | (cp & 0x3F));
+    } else {
+      out += (char)(0xF0 | cp >> 18);
+      out += (char)(0x80 | ((cp >> 12) & 0x3F));
+      out += (char)(0x80 | ((cp >> 6) & 0x3F));
+      out += (char)(0x80 | (cp & 0x3F));
+    }
+  }
+  uint32_t hex4() {
+    if (e_ - p_ < 4) fail("short \\u escape");
+    uint32_t v = 0;
+    for (int i = 0; i < 4; ++i, ++p_) {
+      const char c = *p_;
+      v <<= 4;
+      if (c >= '0' && c <= '9') v |= (uint32_t)(c - '0');
+      else if (c >= 'a' && c <= 'f') v |= (uint32_t)(c - 'a' + 10);
+      else if (c >= 'A' && c <= 'F') v |= (uint32_t)(c - 'A' + 10);
+      else fail("bad \\u escape");
+    }
+    return v;
+  }
+  std::string string() {
+    if (!take('"')) fail("string expected");
+    std::string out;
+    for (;;) {
+      if (p_ == e_) fail("unterminated string");
+      const char c = *p_++;
+      if (c == '"') return out;
+      if ((unsigned char)c < 0x20) fail("control character in a string");
+      if (c != '\\') {
+        out += c;
+        continue;
+      }
+      if (p_ == e_) fail("unterminated string");
+      const char x = *p_++;
+      switch (x) {
+        case '"': out += '"'; break;
+        case '\\': out += '\\'; break;
+        case '/': out += '/'; break;
+        case 'b': out += '\b'; break;
+        case 'f': out += '\f'; break;
+        case 'n': out += '\n'; break;
+        case 'r': out += '\r'; break;
+        case 't': out += '\t'; break;
+        case 'u': {
+          uint32_t cp = hex4();
+          if (cp >= 0xD800 && cp < 0xDC00) {  // a surrogate pair
+            if (e_ - p_ < 2 || p_[0] != '\\' || p_[1] != 'u') fail("lone surrogate");
+            p_ += 2;
+            const uint32_t lo = hex4();
+            if (lo < 0xDC00 || lo > 0xDFFF) fail("bad surrogate pair");
+            cp = 0x10000 + ((cp - 0xD800) << 10) + (lo - 0xDC00);
+          } else if (cp >= 0xDC00 && cp < 0xE000) {
+            fail("lone surrogate");
+          }
+          utf8(out, cp);
+          break;
+        }
+        default: fail("bad escape");
+      }
+    }
+  }
+  Json value(int depth) {
+    if (depth > 64) fail("nested too deeply");
+    ws();
+    if (p_ == e_) fail("value expected");
+    Json v;
+    const char c = *p_;
+    if (c == '{') {
+      ++p_;
+      v.kind = Json::kObj;
+      if (take('}')) return v;
+      do {
+        std::string k = string();
+        if (!take(':')) fail("':' expected");
+        v.obj.emplace_back(std::move(k), value(depth + 1));
+      } while (take(','));
+      if (!take('}')) fail("'}' expected");
+    } else if (c == '[') {
+      ++p_;
+      v.kind = Json::kArr;
+      if (take(']')) return v;
+      do v.arr.push_back(value(depth + 1));
+      while (take(','));
+      if (!take(']')) fail("']' expected");
+    } else if (c == '"') {
+      v.kind = Json::kStr;
+      v.text = string();
+    } else if (c == '-' || (c >= '0' && c <= '9')) {
+      const char* b = p_;
+      while (p_ != e_ && (std::isdigit((unsigned char)*p_) || *p_ == '-' || *p_ == '+' || *p_ == '.' || *p_ == 'e' ||
+                          *p_ == 'E'))
+        ++p_;
+      v.kind = Json::kNum;
+      v.text.assign(b, p_);
+    } else if (e_ - p_ >= 4 && std::strncmp(p_, "true", 4) == 0) {
+      p_ += 4;
+      v.kind = Json::kBool;
+      v.b = true;
+    } else if (e_ - p_ >= 5 && std::strncmp(p_, "false", 5) == 0) {
+      p_ += 5;
+      v.kind = Json::kBool;
+    } else if (e_ - p_ >= 4 && std::strncmp(p_, "null", 4) == 0) {
+      p_ += 4;
+    } else {
+      fail("unexpected character");
+    }
+    return v;
+  }
+};
+
+inline float json_f32(const Json& v, const Path& file) {
+  if (v.kind != Json::kNum) throw Error(MG_ERR_ARG, "JSON: number expected: " + file.string());
+  char* end = nullptr;
+  const float f = std::strtof(v.text.c_str(), &end);
+  if (end != v.text.c_str() + v.text.size()) throw Error(MG_ERR_ARG, "JSON: bad number: " + file.string());
+  return f;
+}
+inline uint64_t json_index(const std::string& t, const Path& file) {
+  char* end = nullptr;
+  const unsigned long long v = t.empty() || t[0] == '-' ? 0 : std::strtoull(t.c_str(), &end, 10);
+  if (t.empty() || t[0] == '-' || end != t.c_str() + t.size()) throw Error(MG_ERR_ARG, "JSON: bad index: " + file.string());
+  return v;
+}
+inline void json_string(std::string& out, const std::string& s) {
+  out += '"';
+  for (const unsigned char c : s) {
+    if (c == '"') out += "\\\"";
+    else if (c == '\\') out += "\\\\";
+    else if (c == '\n') out += "\\n";
+    else if (c == '\r') out += "\\r";
+    else if (c == '\t') out += "\\t";
+    else if (c < 0x20) {
+      char b[8];
+      std::snprintf(b, sizeof(b), "\\u%04x", c);
+      out += b;
+    } else {
+      out += (char)c;
+    }
+  }
+  out += '"';
+}
+inline void json_f32_text(std::string& out, float f) {
+  char b[32];
+  std::snprintf(b, sizeof(b), "%.9g", (double)f);  // nine digits: strtof gives back the same f32
+  out += b;
+  if (!std::strpbrk(b, ".eEn")) out += ".0";
+}
+}  // namespace detail
+
 class SimilarityDatabase {
  public:
   SimilarityDatabase() = default;
@@ -364,13 +567,61 @@ class SimilarityDatabase {
     if (!f) throw Error(MG_ERR_ARG, "write failed: " + file.string());
   }
 
-  // similarity.rs:119-123.  Throws Error when the file is missing or malformed.
+  // similarity.rs:112-116 in the crate's own format: the serde JSON of its
+  // four fields (path_to_index, index_to_path, lab_colors, similarities), so a
+  // database written here can be read by the crate.  Throws Error on I/O failure.
+  void save_json(const Path& file) const {
+    std::string o = "{\n  \"path_to_index\": {";
+    const size_t n = labs_.size();
+    for (size_t i = 0; i < n; ++i) {
+      o += i ? ",\n    " : "\n    ";
+      detail::json_string(o, index_to_path_.at(i).generic_string());
+      o += ": " + std::to_string(i);
+    }
+    o += n ? "\n  },\n  \"index_to_path\": {" : "},\n  \"index_to_path\": {";
+    for (size_t i = 0; i < n; ++i) {
+      o += i ? ",\n    \"" : "\n    \"";
+      o += std::to_string(i) + "\": ";
+      detail::json_string(o, index_to_path_.at(i).generic_string());
+    }
+    o += n ? "\n  },\n  \"lab_colors\": [" : "},\n  \"lab_colors\": [";
+    for (size_t i = 0; i < n; ++i) {
+      o += i ? ",\n    {\n      \"l\": " : "\n    {\n      \"l\": ";
+      detail::json_f32_text(o, labs_[i].l);
+      o += ",\n      \"a\": ";
+      detail::json_f32_text(o, labs_[i].a);
+      o += ",\n      \"b\": ";
+      detail::json_f32_text(o, labs_[i].b);
+      o += "\n    }";
+    }
+    o += n ? "\n  ],\n  \"similarities\": [" : "],\n  \"similarities\": [";
+    for (size_t i = 0; i < sims_.size(); ++i) {
+      o += i ? ",\n    " : "\n    ";
+      detail::json_f32_text(o, sims_[i]);
+    }
+    o += sims_.empty() ? "]\n}" : "\n  ]\n}";
+    std::ofstream f(file, std::ios::binary | std::ios::trunc);
+    if (!f) throw Error(MG_ERR_ARG, "cannot create " + file.string());
+    f.write(o.data(), (std::streamsize)o.size());
+    if (!f) throw Error(MG_ERR_ARG, "write failed: " + file.string());
+  }
+
+  // similarity.rs:119-123.  Reads the binary format below or the crate's JSON
+  // (a file whose first non-blank character is '{'), so the crate's existing
+  // database files load unchanged.  Throws Error when the file is missing or
+  // malformed.
   static SimilarityDatabase load_from_file(const Path& file) {
     std::ifstream f(file, std::ios::binary);
     if (!f) throw Error(MG_ERR_ARG, "cannot open " + file.string());
     char magic[8];
     f.read(magic, 8);
-    if (!f || std::memcmp(magic, kMagic, 8) != 0) throw Error(MG_ERR_ARG, "not a similarity database: " + file.string());
+    if (!f || std::memcmp(magic, kMagic, 8) != 0) {
+      const std::vector<uint8_t> bytes = detail::read_file(file);
+      size_t k = 0;
+      while (k < bytes.size() && (bytes[k] == ' ' || bytes[k] == '\t' || bytes[k] == '\n' || bytes[k] == '\r')) ++k;
+      if (k < bytes.size() && bytes[k] == '{') return load_json(std::string(bytes.begin(), bytes.end()), file);
+      throw Error(MG_ERR_ARG, "not a similarity database: " + file.string());
+    }
     if (get<uint32_t>(f, file) != kVersion) throw Error(MG_ERR_ARG, "unsupported version: " + file.string());
     const uint64_t n = get<uint64_t>(f, file), ns = get<uint64_t>(f, file);
     if (ns != 0 && ns != n * (n - 1) / 2) throw Error(MG_ERR_ARG, "inconsistent sizes: " + file.string());
@@ -394,6 +645,49 @@ class SimilarityDatabase {
     if (ns) f.read(reinterpret_cast<char*>(db.sims_.data()), (std::streamsize)(ns * sizeof(float)));
     if (!f) throw Error(MG_ERR_ARG, "truncated file: " + file.string());
     db.built_n_ = ns ? n : 0;
+    return db;
+  }
+
+  // The crate's JSON layout: lab_colors gives the tiles in index order,
+  // index_to_path (or else path_to_index) their paths, similarities the strict
+  // upper triangle as the crate holds it (any length; lookups past it find
+  // nothing, as similarity.rs:98-102).
+  static SimilarityDatabase load_json(const std::string& text, const Path& file) {
+    using detail::Json;
+    const Json root = detail::JsonReader(text, file).document();
+    const Json* labs = root.get("lab_colors");
+    const Json* i2p = root.get("index_to_path");
+    const Json* p2i = root.get("path_to_index");
+    const Json* sims = root.get("similarities");
+    if (root.kind != Json::kObj || !labs || labs->kind != Json::kArr || !sims || sims->kind != Json::kArr ||
+        ((!i2p || i2p->kind != Json::kObj) && (!p2i || p2i->kind != Json::kObj)))
+      throw Error(MG_ERR_ARG, "not a similarity database: " + file.string());
+    const size_t n = labs->arr.size();
+    std::vector<std::optional<std::string>> paths(n);
+    if (i2p && i2p->kind == Json::kObj) {
+      for (const auto& kv : i2p->obj) {
+        const uint64_t i = detail::json_index(kv.first, file);
+        if (i >= n || kv.second.kind != Json::kStr || paths[i]) throw Error(MG_ERR_ARG, "bad index_to_path: " + file.string());
+        paths[i] = kv.second.text;
+      }
+    } else {
+      for (const auto& kv : p2i->obj) {
+        if (kv.second.kind != Json::kNum) throw Error(MG_ERR_ARG, "bad path_to_index: " + file.string());
+        const uint64_t i = detail::json_index(kv.second.text, file);
+        if (i >= n || paths[i]) throw Error(MG_ERR_ARG, "bad path_to_index: " + file.string());
+        paths[i] = kv.first;
+      }
+    }
+    SimilarityDatabase db;
+    for (size_t i = 0; i < n; ++i) {
+      const Json& c = labs->arr[i];
+      const Json *l = c.get("l"), *a = c.get("a"), *b = c.get("b");
+      if (!paths[i] || c.kind != Json::kObj || !l || !a || !b) throw Error(MG_ERR_ARG, "bad lab_colors: " + file.string());
+      db.add_tile(Path(*paths[i]), Lab{detail::json_f32(*l, file), detail::json_f32(*a, file), detail::json_f32(*b, file)});
+    }
+    db.sims_.reserve(sims->arr.size());
+    for (const Json& v : sims->arr) db.sims_.push_back(detail::json_f32(v, file));
+    db.built_n_ = n >= 2 && db.sims_.size() == n * (n - 1) / 2 ? n : 0;
     return db;
   }
 

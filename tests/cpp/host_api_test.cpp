@@ -149,6 +149,106 @@ static void similarity_host_tests() {
   }
 }
 
+// The crate's own database file (serde_json::to_string_pretty of
+// similarity.rs:31-41, save_to_file :112-116) loads unchanged, is written back
+// in the same layout, and defects in it are errors.
+static void similarity_json_tests() {
+  const Path f = tmp_file("_crate.json"), f2 = tmp_file("_back.json"), f3 = tmp_file("_back.bin");
+  const std::string q = "tiles/a \"q\" \xc3\xbc.png";  // a quote and a non-ASCII letter in the path
+  {
+    std::ofstream o(f);
+    o << R"({
+  "path_to_index": {
+    "tiles/b.png": 1,
+    "tiles/a \"q\" \u00fc.png": 0,
+    "tiles/c.png": 2
+  },
+  "index_to_path": {
+    "1": "tiles/b.png",
+    "0": "tiles/a \"q\" \u00fc.png",
+    "2": "tiles/c.png"
+  },
+  "lab_colors": [
+    {
+      "l": 50.0,
+      "a": 25.0,
+      "b": -15.0
+    },
+    {
+      "l": 53.23288,
+      "a": 80.10931,
+      "b": 67.22006
+    },
+    {
+      "l": 0.0,
+      "a": -0.0,
+      "b": 1e-7
+    }
+  ],
+  "similarities": [
+    1.5,
+    2.25,
+    0.3
+  ]
+})";
+  }
+  SimilarityDatabase db = SimilarityDatabase::load_or_new(f);
+  CHECK(db.len() == 3 && db.built());
+  CHECK(db.index_of(q) && *db.index_of(q) == 0 && db.path_of(2) == Path("tiles/c.png"));
+  CHECK(db.get_lab_color("tiles/b.png") && db.get_lab_color("tiles/b.png")->l == 53.23288f &&
+        db.get_lab_color("tiles/b.png")->b == 67.22006f && db.get_lab_color("tiles/c.png")->b == 1e-7f);
+  CHECK(db.get_similarity(q, "tiles/b.png") == 1.5f && db.get_similarity("tiles/c.png", q) == 2.25f &&
+        db.get_similarity("tiles/b.png", "tiles/c.png") == 0.3f);
+  db.save_json(f2);
+  SimilarityDatabase back = SimilarityDatabase::load_from_file(f2);
+  db.save_to_file(f3);
+  SimilarityDatabase bin = SimilarityDatabase::load_from_file(f3);
+  for (const SimilarityDatabase* d : {&back, &bin}) {
+    CHECK(d->len() == 3 && d->built() && d->similarities() == db.similarities() && d->flat_lab() == db.flat_lab());
+    for (size_t i = 0; i < 3; ++i) CHECK(d->path_of(i) == db.path_of(i));
+  }
+  {
+    std::ifstream in(f2);
+    const std::string text((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+    CHECK(text.find("\"path_to_index\": {") != std::string::npos && text.find("\"0\": \"tiles/a \\\"q\\\"") != std::string::npos);
+  }
+  {  // an empty database written by the crate
+    std::ofstream o(f);
+    o << "{\n  \"path_to_index\": {},\n  \"index_to_path\": {},\n  \"lab_colors\": [],\n  \"similarities\": []\n}";
+  }
+  SimilarityDatabase empty = SimilarityDatabase::load_from_file(f);
+  CHECK(empty.len() == 0 && !empty.built());
+  empty.save_json(f2);
+  CHECK(SimilarityDatabase::load_from_file(f2).len() == 0);
+  // defects: each throws mosaic::Error (load_or_new then starts a new database)
+  const char* bad[] = {
+      "{\"path_to_index\": {}, \"index_to_path\": {\"0\": \"a.png\"}, \"lab_colors\": [], \"similarities\": []}",
+      "{\"index_to_path\": {\"0\": \"a.png\"}, \"lab_colors\": [{\"l\": 1, \"a\": 2}], \"similarities\": []}",
+      "{\"index_to_path\": {\"0\": \"a.png\"}, \"lab_colors\": [{\"l\": 1, \"a\": 2, \"b\": \"x\"}], \"similarities\": []}",
+      "{\"index_to_path\": {\"0\": \"a\\q.png\"}, \"lab_colors\": [{\"l\": 1, \"a\": 2, \"b\": 3}], \"similarities\": []}",
+      "{\"index_to_path\": {\"-1\": \"a.png\"}, \"lab_colors\": [{\"l\": 1, \"a\": 2, \"b\": 3}], \"similarities\": []}",
+      "{\"index_to_path\": {\"0\": \"a.png\"}, \"lab_colors\": [{\"l\": 1, \"a\": 2, \"b\": 3}], \"similarities\": [1,]}",
+      "{\"index_to_path\": {\"0\": \"a.png\"}, \"lab_colors\": [{\"l\": 1, \"a\": 2, \"b\": 3}], \"similarities\": []",
+      "{\"index_to_path\": {\"0\": \"\\ud800.png\"}, \"lab_colors\": [{\"l\": 1, \"a\": 2, \"b\": 3}], \"similarities\": []}",
+      "{\"lab_colors\": [], \"similarities\": []}",
+      "  {"};
+  for (const char* t : bad) {
+    {
+      std::ofstream o(f);
+      o << t;
+    }
+    bool threw = false;
+    try {
+      SimilarityDatabase::load_from_file(f);
+    } catch (const Error&) {
+      threw = true;
+    }
+    CHECK(threw);
+    CHECK(SimilarityDatabase::load_or_new(f).len() == 0);
+  }
+  for (const Path& p : {f, f2, f3}) std::filesystem::remove(p);
+}
+
 static void color_host_tests() {  // color_adjustment.rs:160-178
   ColorAdjustment d;
   CHECK(d.brightness == 0.0f && d.contrast == 1.0f && d.hue_shift == 0.0f && d.saturation == 1.0f);
@@ -614,6 +714,7 @@ int main(int argc, char** argv) {
   grid_position_tests();
   lab_distance_tests();
   similarity_host_tests();
+  similarity_json_tests();
   color_host_tests();
   result_tests();
   png_tests();
