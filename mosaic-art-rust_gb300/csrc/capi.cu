@@ -878,6 +878,10 @@ int plan_setup(mg_plan* pl, mg_ctx* ctx, const mg_request* r, bool zero_copy) {
   pl->ch = pl->H / pl->gh;
   pl->tw = r->tile_w ? r->tile_w : pl->cw;
   pl->th = r->tile_h ? r->tile_h : pl->ch;
+  // cell indices and output rows are 32-bit on the device
+  if ((int64_t)pl->gw * pl->gh > kMaxGridCells || (int64_t)pl->gw * pl->tw > INT32_MAX / 3 ||
+      (int64_t)pl->gh * pl->th > INT32_MAX)
+    return fail(MG_ERR_ARG, "grid or output image too large");
   pl->N = pl->gw * pl->gh;
   pl->weight = r->adjacency_penalty_weight;
   pl->strength = rclamp(r->color_adjustment_strength, 0.0f, 1.0f);

@@ -197,6 +197,10 @@ int batch_setup(mg_batch* b, mg_ctx* ctx, mg_palette* pal, const mg_mosaic* ms, 
     if (r.grid_w <= 0 || r.grid_h <= 0 || r.target_w / r.grid_w <= 0 || r.target_h / r.grid_h <= 0)
       return fail(MG_ERR_ARG, "invalid grid of mosaic " + std::to_string(i));
     if (r.max_usage_per_image < 0) return fail(MG_ERR_ARG, "negative max usage");
+    // cell indices (over the whole batch) and output rows are 32-bit on the device
+    if ((int64_t)r.grid_w * r.grid_h > kMaxGridCells || (int64_t)r.grid_w * tw > INT32_MAX / 3 ||
+        (int64_t)r.grid_h * th > INT32_MAX || (int64_t)cell_base + (int64_t)r.grid_w * r.grid_h + 16 > kMaxGridCells)
+      return fail(MG_ERR_ARG, "grid or output image too large in mosaic " + std::to_string(i));
     const int N = r.grid_w * r.grid_h;
     const bool run_sa = r.enable_optimization && r.adjacency_penalty_weight > 0.0f && pal->P > 0;  // main.rs:608
     if (run_sa && (r.chains < 1 || r.chains > 65535 || r.optimization_iterations < 0))

@@ -146,6 +146,8 @@ int launch_greedy(const float4* pal, int p, const GreedyJob* jobs_dev, int n_job
                   int max_cells, uint32_t* usage_scratch, uint32_t* err, cudaStream_t stream, bool one_warp = false,
                   bool inject_timeout = false);
 inline size_t padded_cells(int n) { return ((size_t)n + 15) / 16 * 16; }
+// Most cells of one mosaic, or of all the mosaics of one batch (indices stay 32-bit).
+constexpr int64_t kMaxGridCells = int64_t(1) << 28;
 // Whether a mosaic of gw x (n / gw) cells over a palette of p walks in the
 // three-CTA form (else one warp).
 bool greedy_scouted_fits(int gw, int n, int p);
