@@ -391,6 +391,7 @@ int mg_cells_lab(mg_ctx* ctx, const uint8_t* img, int w, int h, int64_t stride, 
   MG_CHECK(check_ctx(ctx));
   if (!valid_image(img, w, h, stride) || !lab_out) return fail(MG_ERR_ARG, "invalid image");
   if (gw <= 0 || gh <= 0 || w / gw <= 0 || h / gh <= 0) return fail(MG_ERR_ARG, "grid larger than the image");
+  if ((int64_t)gw * gh > kMaxGridCells) return fail(MG_ERR_ARG, "grid too large");
   const int n = gw * gh;
   const size_t row = 3ull * w;
   MG_CHECK(ctx->in0.ensure(row * h));
@@ -531,6 +532,7 @@ int mg_nearest_n(mg_ctx* ctx, const float* palette_lab, int p, const float* quer
 // ---- adjacency ----------------------------------------------------------------------------
 static int check_grid(const float* pal, int p, const int32_t* grid, int gw, int gh) {
   if (gw <= 0 || gh <= 0 || !grid || p < 0 || (p > 0 && !pal)) return fail(MG_ERR_ARG, "invalid grid or palette");
+  if ((int64_t)gw * gh > kMaxGridCells) return fail(MG_ERR_ARG, "grid too large");
   for (int i = 0; i < gw * gh; ++i)
     if (grid[i] < -1 || grid[i] >= p) return fail(MG_ERR_ARG, "grid entry out of palette range");
   return MG_OK;
@@ -602,7 +604,8 @@ int mg_swap_delta_batch(mg_ctx* ctx, const float* palette_lab, int p, const int3
 int mg_place_greedy(mg_ctx* ctx, const float* palette_lab, int p, const float* cell_lab, int gw, int gh,
                     const mg_place_config* cfg, int32_t* grid_out, int* n_resets) {
   MG_CHECK(check_ctx(ctx));
-  if (!cfg || !cell_lab || !grid_out || gw <= 0 || gh <= 0 || p < 0 || (p > 0 && !palette_lab))
+  if (!cfg || !cell_lab || !grid_out || gw <= 0 || gh <= 0 || p < 0 || (p > 0 && !palette_lab) ||
+      (int64_t)gw * gh > kMaxGridCells)
     return fail(MG_ERR_ARG, "invalid arguments");
   if (cfg->max_usage_per_image < 0) return fail(MG_ERR_ARG, "negative max usage");
   const int n = gw * gh;
@@ -766,7 +769,8 @@ int mg_apply_adjustment(mg_ctx* ctx, const mg_color_adjustment* adj, const uint8
 int mg_composite(mg_ctx* ctx, const int32_t* grid, int gw, int gh, const uint8_t* thumbs, int p, int tw, int th,
                  const uint8_t* cell_avg_rgb, float strength, uint8_t* out) {
   MG_CHECK(check_ctx(ctx));
-  if (!grid || !out || gw <= 0 || gh <= 0 || tw <= 0 || th <= 0 || p < 0 || (p > 0 && !thumbs))
+  if (!grid || !out || gw <= 0 || gh <= 0 || tw <= 0 || th <= 0 || p < 0 || (p > 0 && !thumbs) ||
+      (int64_t)gw * gh > kMaxGridCells || (int64_t)gw * tw > INT32_MAX / 3 || (int64_t)gh * th > INT32_MAX)
     return fail(MG_ERR_ARG, "invalid arguments");
   const bool adjust = strength > 0.0f;
   if (adjust && !cell_avg_rgb) return fail(MG_ERR_ARG, "cell_avg_rgb required when strength > 0");
