@@ -58,14 +58,21 @@ struct Status {
 };
 
 // ---- checksums ----------------------------------------------------------------------
+// CRC-32 (ISO 3309, reflected polynomial 0xEDB88320), eight bytes a step
+// ("slicing-by-8", Kounavis and Berry 2005): t[k][b] is the CRC of byte b
+// followed by k zero bytes, so the eight table entries of one 8-byte word
+// combine by XOR; bytes are read one by one (no alignment or byte-order
+// assumption).
 struct CrcTable {
-  uint32_t t[256];
+  uint32_t t[8][256];
   CrcTable() {
     for (uint32_t n = 0; n < 256; ++n) {
       uint32_t c = n;
       for (int k = 0; k < 8; ++k) c = (c & 1u) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-      t[n] = c;
+      t[0][n] = c;
     }
+    for (int k = 1; k < 8; ++k)
+      for (uint32_t n = 0; n < 256; ++n) t[k][n] = (t[k - 1][n] >> 8) ^ t[0][t[k - 1][n] & 0xFFu];
   }
 };
 const CrcTable& crc_table() {
@@ -73,9 +80,15 @@ const CrcTable& crc_table() {
   return tab;
 }
 uint32_t crc32_update(uint32_t crc, const uint8_t* p, size_t n) {
-  const uint32_t* t = crc_table().t;
+  const auto& t = crc_table().t;
   uint32_t c = crc ^ 0xFFFFFFFFu;
-  for (size_t i = 0; i < n; ++i) c = t[(c ^ p[i]) & 0xFFu] ^ (c >> 8);
+  for (; n >= 8; p += 8, n -= 8) {
+    const uint32_t lo = c ^ ((uint32_t)p[0] | (uint32_t)p[1] << 8 | (uint32_t)p[2] << 16 | (uint32_t)p[3] << 24);
+    const uint32_t hi = (uint32_t)p[4] | (uint32_t)p[5] << 8 | (uint32_t)p[6] << 16 | (uint32_t)p[7] << 24;
+    c = t[7][lo & 0xFFu] ^ t[6][(lo >> 8) & 0xFFu] ^ t[5][(lo >> 16) & 0xFFu] ^ t[4][lo >> 24] ^ t[3][hi & 0xFFu] ^
+        t[2][(hi >> 8) & 0xFFu] ^ t[1][(hi >> 16) & 0xFFu] ^ t[0][hi >> 24];
+  }
+  for (; n; ++p, --n) c = t[0][(c ^ *p) & 0xFFu] ^ (c >> 8);
   return c ^ 0xFFFFFFFFu;
 }
 
