@@ -332,7 +332,9 @@ typedef struct mg_result {
 
 void mg_request_default(mg_request* req);
 /* One complete job from host buffers to host buffers.  Inputs in pinned host
- * memory (mg_host_alloc) are read in place over the CPU-GPU link. */
+ * memory (mg_host_alloc) are read in place over the CPU-GPU link.  A grid holds
+ * at most 2^28 cells and an output row at most 2^31 / 3 pixels (MG_ERR_ARG
+ * beyond; a batch's cells together obey the same cell limit). */
 int mg_generate(mg_ctx* ctx, const mg_request* req, mg_result* res);
 
 /* Device-resident form of the same job: mg_plan_create uploads the inputs
