@@ -157,6 +157,17 @@ int mg_png_encode(const uint8_t* rgb, int w, int h, int64_t stride, int level, i
  * Same conventions as the PNG calls: no context, any thread, RGB8 out. */
 int mg_jpeg_info(const uint8_t* data, size_t n, int* w, int* h);
 int mg_jpeg_decode(const uint8_t* data, size_t n, uint8_t* out, int64_t stride);
+/* main.rs:672 output_img.save(path) of a .jpg / .jpeg path (image's JPEG
+ * encoder, quality 75).  This library's own baseline JFIF encoder: 4:2:0
+ * YCbCr, the T.81 Annex K quantisation tables scaled by quality (1..100, the
+ * IJG rule), Huffman codes from the image's own symbol counts, one restart
+ * interval per row of 16-pixel MCUs (the rows are coded on up to `threads`
+ * host threads; <= 0: all).  Bytes differ from the crate's encoder's (not
+ * pinned).  w, h in 1..65535; out must hold mg_jpeg_encode_bound(w, h) bytes
+ * (else MG_ERR_ARG with *len = that bound); *len receives the file size. */
+size_t mg_jpeg_encode_bound(int w, int h);
+int mg_jpeg_encode(const uint8_t* rgb, int w, int h, int64_t stride, int quality, int threads, uint8_t* out,
+                   size_t cap, size_t* len);
 /* PNG or JPEG, told apart by the file's signature (image::open's format
  * detection for the two formats read here). */
 int mg_image_info(const uint8_t* data, size_t n, int* w, int* h);

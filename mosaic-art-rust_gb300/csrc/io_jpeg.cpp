@@ -25,6 +25,7 @@
 // decoder to +-1 of a float64 restatement of the same steps and to the exact
 // pixels of files whose content survives the codec unchanged.
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -665,6 +666,363 @@ bool is_png(const uint8_t* d, size_t n) {
   return d && n >= 8 && std::memcmp(d, sig, 8) == 0;
 }
 
+// ---- encoder (the output end: image::save of a .jpg / .jpeg path) ----------------
+//
+// Baseline JFIF (T.81 sequential DCT, Huffman): YCbCr with 4:2:0 chroma (the
+// mean of each 2x2 box), the forward DCT in FP32 with the decoder's cosine
+// table, the T.81 Annex K.1 quantisation tables scaled by quality with the
+// IJG rule (q < 50: 5000 / q percent, else 200 - 2q), rounding half away from
+// zero; Huffman codes built from this image's own symbol counts (T.81 Annex
+// K.2: code sizes, then lengths limited to 16 bits); one restart interval per
+// row of MCUs, so the rows are entropy-coded on all threads and joined with
+// RSTn markers.  The output bytes are not those of the crate's encoder (not
+// pinned); any JPEG reader decodes them.
+
+const uint8_t kQLuma[64] = {16, 11, 10, 16, 24,  40,  51,  61,  12, 12, 14, 19, 26,  58,  60,  55,
+                            14, 13, 16, 24, 40,  57,  69,  56,  14, 17, 22, 29, 51,  87,  80,  62,
+                            18, 22, 37, 56, 68,  109, 103, 77,  24, 35, 55, 64, 81,  104, 113, 92,
+                            49, 64, 78, 87, 103, 121, 120, 101, 72, 92, 95, 98, 112, 100, 103, 99};
+const uint8_t kQChroma[64] = {17, 18, 24, 47, 99, 99, 99, 99, 18, 21, 26, 66, 99, 99, 99, 99,
+                              24, 26, 56, 99, 99, 99, 99, 99, 47, 66, 99, 99, 99, 99, 99, 99,
+                              99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99,
+                              99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99, 99};
+
+void scaled_quant(const uint8_t* base, int quality, uint8_t* q) {
+  const int scale = quality < 50 ? 5000 / quality : 200 - 2 * quality;
+  for (int i = 0; i < 64; ++i) q[i] = (uint8_t)std::min(255, std::max(1, (base[i] * scale + 50) / 100));
+}
+
+// A Huffman code from symbol counts (T.81 K.2): code sizes by repeatedly
+// merging the two least frequent nodes, a reserved symbol (count 1) keeping
+// the all-ones code out, then lengths limited to 16 bits (Adjust_BITS) and the
+// reserved code dropped from the longest length.
+struct HuffCode {
+  uint8_t bits[16] = {};   // codes per length 1..16
+  uint8_t vals[256] = {};  // symbols in code order
+  int nvals = 0;
+  uint16_t code[256] = {};
+  uint8_t size[256] = {};
+  void build(const uint64_t* freq_in) {
+    uint64_t freq[257];
+    for (int i = 0; i < 256; ++i) freq[i] = freq_in[i];
+    freq[256] = 1;
+    int codesize[257] = {}, others[257];
+    for (int i = 0; i < 257; ++i) others[i] = -1;
+    for (;;) {
+      int c1 = -1, c2 = -1;  // least, then next least nonzero count (ties: the larger symbol first)
+      for (int i = 0; i < 257; ++i) {
+        if (freq[i] == 0) continue;
+        if (c1 < 0 || freq[i] <= freq[c1]) {
+          c2 = c1;
+          c1 = i;
+        } else if (c2 < 0 || freq[i] <= freq[c2]) {
+          c2 = i;
+        }
+      }
+      if (c2 < 0) break;
+      freq[c1] += freq[c2];
+      freq[c2] = 0;
+      ++codesize[c1];
+      while (others[c1] >= 0) {
+        c1 = others[c1];
+        ++codesize[c1];
+      }
+      others[c1] = c2;
+      ++codesize[c2];
+      while (others[c2] >= 0) {
+        c2 = others[c2];
+        ++codesize[c2];
+      }
+    }
+    int count[258] = {};  // a code size is at most 256 (257 symbols)
+    int maxsize = 0;
+    for (int i = 0; i < 257; ++i)
+      if (codesize[i]) {
+        ++count[codesize[i]];
+        maxsize = std::max(maxsize, codesize[i]);
+      }
+    for (int i = maxsize; i > 16; --i)
+      while (count[i] > 0) {
+        int j = i - 2;
+        while (count[j] == 0) --j;
+        count[i] -= 2;
+        count[i - 1] += 1;
+        count[j + 1] += 2;
+        count[j] -= 1;
+      }
+    int longest = 16;
+    while (longest > 0 && count[longest] == 0) --longest;
+    if (longest > 0) --count[longest];  // the reserved symbol's code
+    for (int i = 0; i < 16; ++i) bits[i] = (uint8_t)count[i + 1];
+    nvals = 0;
+    for (int len = 1; len <= maxsize; ++len)
+      for (int sym = 0; sym < 256; ++sym)
+        if (codesize[sym] == len) vals[nvals++] = (uint8_t)sym;
+    int k = 0, c = 0;
+    for (int len = 1; len <= 16; ++len) {
+      for (int i = 0; i < bits[len - 1]; ++i, ++k, ++c) {
+        code[vals[k]] = (uint16_t)c;
+        size[vals[k]] = (uint8_t)len;
+      }
+      c <<= 1;
+    }
+  }
+};
+
+struct BitSink {
+  std::vector<uint8_t> out;
+  uint32_t acc = 0;
+  int n = 0;
+  void put(uint32_t v, int bits) {  // bits <= 16
+    acc = (acc << bits) | (v & ((1u << bits) - 1u));
+    n += bits;
+    while (n >= 8) {
+      const uint8_t b = (uint8_t)(acc >> (n - 8));
+      out.push_back(b);
+      if (b == 0xFF) out.push_back(0x00);
+      n -= 8;
+    }
+    acc &= (1u << n) - 1u;
+  }
+  void pad() {
+    if (n) put((1u << (8 - n)) - 1u, 8 - n);
+  }
+};
+
+inline int category(int v) {
+  int a = v < 0 ? -v : v, s = 0;
+  while (a) {
+    ++s;
+    a >>= 1;
+  }
+  return s;
+}
+
+struct Encoder {
+  int w, h, mcux, mcuy;
+  uint8_t qt[2][64];  // natural order
+  // quantised coefficients, natural order: Y blocks (2 mcux x 2 mcuy), Cb, Cr (mcux x mcuy)
+  std::vector<int16_t> coef[3];
+  int bw[3], bh[3];
+
+  // One MCU row: pixel rows 16 my .. 16 my + 15 (edges replicated) to YCbCr,
+  // chroma averaged over 2x2, forward DCT, quantisation.
+  void transform_row(const uint8_t* rgb, int64_t stride, int my, const float (&ct)[8][8]) {
+    const int pw = mcux * 16;
+    std::vector<float> Y((size_t)16 * pw), cb((size_t)16 * pw), cr((size_t)16 * pw);
+    for (int y = 0; y < 16; ++y) {
+      const int sy = std::min(h - 1, my * 16 + y);
+      const uint8_t* row = rgb + (int64_t)sy * stride;
+      for (int x = 0; x < pw; ++x) {
+        const uint8_t* px = row + 3 * std::min(w - 1, x);
+        const float r = px[0], g = px[1], b = px[2];
+        Y[(size_t)y * pw + x] = 0.299f * r + 0.587f * g + 0.114f * b - 128.0f;
+        cb[(size_t)y * pw + x] = -0.168736f * r - 0.331264f * g + 0.5f * b;
+        cr[(size_t)y * pw + x] = 0.5f * r - 0.418688f * g - 0.081312f * b;
+      }
+    }
+    float blk[64];
+    for (int bx = 0; bx < 2 * mcux; ++bx)
+      for (int by = 0; by < 2; ++by) {
+        for (int y = 0; y < 8; ++y)
+          for (int x = 0; x < 8; ++x) blk[y * 8 + x] = Y[(size_t)(by * 8 + y) * pw + bx * 8 + x];
+        fdct_quant(blk, qt[0], coef[0].data() + ((size_t)(2 * my + by) * bw[0] + bx) * 64, ct);
+      }
+    for (int c = 1; c < 3; ++c) {
+      const std::vector<float>& p = c == 1 ? cb : cr;
+      for (int bx = 0; bx < mcux; ++bx) {
+        for (int y = 0; y < 8; ++y)
+          for (int x = 0; x < 8; ++x) {
+            const size_t o = (size_t)(2 * y) * pw + 2 * (bx * 8 + x);
+            blk[y * 8 + x] = 0.25f * (p[o] + p[o + 1] + p[o + pw] + p[o + pw + 1]);
+          }
+        fdct_quant(blk, qt[1], coef[c].data() + ((size_t)my * bw[c] + bx) * 64, ct);
+      }
+    }
+  }
+  // F(u, v) = sum_y ct[v][y] sum_x ct[u][x] f(x, y), then F / Q rounded half away from zero.
+  static void fdct_quant(const float* f, const uint8_t* q, int16_t* out, const float (&ct)[8][8]) {
+    float r[64];
+    for (int y = 0; y < 8; ++y) {
+      float s[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+      for (int x = 0; x < 8; ++x) {
+        const float fx = f[y * 8 + x];
+        for (int u = 0; u < 8; ++u) s[u] += ct[u][x] * fx;
+      }
+      for (int u = 0; u < 8; ++u) r[y * 8 + u] = s[u];
+    }
+    for (int v = 0; v < 8; ++v) {
+      float s[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+      for (int y = 0; y < 8; ++y) {
+        const float c = ct[v][y];
+        for (int u = 0; u < 8; ++u) s[u] += c * r[y * 8 + u];
+      }
+      for (int u = 0; u < 8; ++u) {
+        const float t = s[u] / (float)q[v * 8 + u];
+        const int r = t >= 0.0f ? (int)(t + 0.5f) : -(int)(0.5f - t);
+        const int lim = u + v ? 1023 : 2047;  // baseline: AC categories up to 10, DC up to 11
+        out[v * 8 + u] = (int16_t)std::max(-lim, std::min(lim, r));
+      }
+    }
+  }
+  // The blocks of MCU row my in scan order (Y 2x2, Cb, Cr per MCU), calling
+  // f(component, block coefficients).
+  template <class F>
+  void walk_row(int my, F&& f) const {
+    for (int mx = 0; mx < mcux; ++mx) {
+      for (int by = 0; by < 2; ++by)
+        for (int bx = 0; bx < 2; ++bx) f(0, coef[0].data() + ((size_t)(2 * my + by) * bw[0] + 2 * mx + bx) * 64);
+      for (int c = 1; c < 3; ++c) f(c, coef[c].data() + ((size_t)my * bw[c] + mx) * 64);
+    }
+  }
+  // Symbol counts of MCU row my (DC prediction restarts with the row): [table][symbol]
+  void count_row(int my, uint64_t (*freq)[256]) const {
+    int pred[3] = {0, 0, 0};
+    walk_row(my, [&](int c, const int16_t* b) {
+      const int t = c ? 1 : 0;
+      ++freq[2 * t][category(b[0] - pred[c])];
+      pred[c] = b[0];
+      int run = 0;
+      for (int k = 1; k < 64; ++k) {
+        const int v = b[kZigzag[k]];
+        if (v == 0) {
+          ++run;
+          continue;
+        }
+        while (run > 15) {
+          ++freq[2 * t + 1][0xF0];
+          run -= 16;
+        }
+        ++freq[2 * t + 1][(run << 4) | category(v)];
+        run = 0;
+      }
+      if (run) ++freq[2 * t + 1][0x00];
+    });
+  }
+  void code_row(int my, const HuffCode* hc, BitSink& bs) const {
+    int pred[3] = {0, 0, 0};
+    walk_row(my, [&](int c, const int16_t* b) {
+      const HuffCode& dc = hc[c ? 2 : 0];
+      const HuffCode& ac = hc[c ? 3 : 1];
+      const int diff = b[0] - pred[c];
+      pred[c] = b[0];
+      int s = category(diff);
+      bs.put(dc.code[s], dc.size[s]);
+      if (s) bs.put((uint32_t)(diff < 0 ? diff + (1 << s) - 1 : diff), s);
+      int run = 0;
+      for (int k = 1; k < 64; ++k) {
+        const int v = b[kZigzag[k]];
+        if (v == 0) {
+          ++run;
+          continue;
+        }
+        while (run > 15) {
+          bs.put(ac.code[0xF0], ac.size[0xF0]);
+          run -= 16;
+        }
+        s = category(v);
+        const int sym = (run << 4) | s;
+        bs.put(ac.code[sym], ac.size[sym]);
+        bs.put((uint32_t)(v < 0 ? v + (1 << s) - 1 : v), s);
+        run = 0;
+      }
+      if (run) bs.put(ac.code[0x00], ac.size[0x00]);
+    });
+    bs.pad();
+  }
+};
+
+template <class F>
+void run_threads(int threads, int items, F&& f) {
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (int i; (i = next.fetch_add(1)) < items;) f(i);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < threads; ++t) {
+    try {
+      pool.emplace_back(work);
+    } catch (const std::exception&) {
+      break;  // the threads running (and this one) take the rest
+    }
+  }
+  work();
+  for (auto& t : pool) t.join();
+}
+
+void put_segment(std::vector<uint8_t>& o, int marker, const std::vector<uint8_t>& body) {
+  o.push_back(0xFF);
+  o.push_back((uint8_t)marker);
+  o.push_back((uint8_t)((body.size() + 2) >> 8));
+  o.push_back((uint8_t)(body.size() + 2));
+  o.insert(o.end(), body.begin(), body.end());
+}
+
+// The whole file into `file` (MG_OK) or an error code.
+int jpeg_encode(const uint8_t* rgb, int w, int h, int64_t stride, int quality, int threads, std::vector<uint8_t>& file) {
+  Encoder E;
+  E.w = w;
+  E.h = h;
+  E.mcux = (w + 15) / 16;
+  E.mcuy = (h + 15) / 16;
+  scaled_quant(kQLuma, quality, E.qt[0]);
+  scaled_quant(kQChroma, quality, E.qt[1]);
+  E.bw[0] = 2 * E.mcux;
+  E.bh[0] = 2 * E.mcuy;
+  E.bw[1] = E.bw[2] = E.mcux;
+  E.bh[1] = E.bh[2] = E.mcuy;
+  for (int c = 0; c < 3; ++c) E.coef[c].assign((size_t)E.bw[c] * E.bh[c] * 64, 0);
+  float ct[8][8];  // ct[u][x] = C(u)/2 cos((2x+1) u pi / 16), as the decoder's
+  for (int x = 0; x < 8; ++x)
+    for (int u = 0; u < 8; ++u)
+      ct[u][x] = (float)((u == 0 ? std::sqrt(0.5) : 1.0) * 0.5 * std::cos((2 * x + 1) * u * M_PI / 16.0));
+  if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  threads = std::max(1, std::min(threads, E.mcuy));
+  run_threads(threads, E.mcuy, [&](int my) { E.transform_row(rgb, stride, my, ct); });
+  std::vector<std::array<std::array<uint64_t, 256>, 4>> counts((size_t)E.mcuy);
+  run_threads(threads, E.mcuy, [&](int my) {
+    uint64_t f[4][256] = {};
+    E.count_row(my, f);
+    for (int t = 0; t < 4; ++t)
+      for (int s = 0; s < 256; ++s) counts[my][t][s] = f[t][s];
+  });
+  uint64_t total[4][256] = {};
+  for (const auto& c : counts)
+    for (int t = 0; t < 4; ++t)
+      for (int s = 0; s < 256; ++s) total[t][s] += c[t][s];
+  HuffCode hc[4];  // DC luma, AC luma, DC chroma, AC chroma
+  for (int t = 0; t < 4; ++t) hc[t].build(total[t]);
+  std::vector<BitSink> rows((size_t)E.mcuy);
+  run_threads(threads, E.mcuy, [&](int my) { E.code_row(my, hc, rows[my]); });
+  // headers
+  file.clear();
+  file.insert(file.end(), {0xFF, 0xD8});
+  put_segment(file, 0xE0, {'J', 'F', 'I', 'F', 0, 1, 2, 0, 0, 1, 0, 1, 0, 0});
+  std::vector<uint8_t> dqt;
+  for (int t = 0; t < 2; ++t) {
+    dqt.push_back((uint8_t)t);
+    for (int k = 0; k < 64; ++k) dqt.push_back(E.qt[t][kZigzag[k]]);
+  }
+  put_segment(file, 0xDB, dqt);
+  put_segment(file, 0xC0,
+              {8, (uint8_t)(h >> 8), (uint8_t)h, (uint8_t)(w >> 8), (uint8_t)w, 3, 1, 0x22, 0, 2, 0x11, 1, 3, 0x11, 1});
+  std::vector<uint8_t> dht;
+  for (int t = 0; t < 4; ++t) {
+    dht.push_back((uint8_t)(((t & 1) << 4) | (t >> 1)));
+    dht.insert(dht.end(), hc[t].bits, hc[t].bits + 16);
+    dht.insert(dht.end(), hc[t].vals, hc[t].vals + hc[t].nvals);
+  }
+  put_segment(file, 0xC4, dht);
+  put_segment(file, 0xDD, {(uint8_t)(E.mcux >> 8), (uint8_t)E.mcux});
+  put_segment(file, 0xDA, {3, 1, 0x00, 2, 0x11, 3, 0x11, 0, 63, 0});
+  for (int my = 0; my < E.mcuy; ++my) {
+    if (my) file.insert(file.end(), {0xFF, (uint8_t)(0xD0 + ((my - 1) & 7))});
+    file.insert(file.end(), rows[my].out.begin(), rows[my].out.end());
+  }
+  file.insert(file.end(), {0xFF, 0xD9});
+  return MG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -753,6 +1111,45 @@ int mg_image_decode_batch(const uint8_t* const* data, const size_t* n, int count
     }
   }
   return first;
+}
+
+size_t mg_jpeg_encode_bound(int w, int h) {
+  if (w <= 0 || h <= 0 || w > 65535 || h > 65535) return 0;
+  const size_t mcus = (size_t)((w + 15) / 16) * ((h + 15) / 16);
+  // per block at most 16 + 11 bits of DC and 63 x (16 + 10) bits of AC, doubled for 0xFF stuffing
+  return 4096 + mcus * 6 * 2 * ((27 + 63 * 26 + 7) / 8) + 2 * (size_t)((h + 15) / 16);
+}
+
+int mg_jpeg_encode(const uint8_t* rgb, int w, int h, int64_t stride, int quality, int threads, uint8_t* out,
+                   size_t cap, size_t* len) {
+  const size_t bound = mg_jpeg_encode_bound(w, h);
+  if (!rgb || !out || !len || bound == 0 || stride < 3ll * w || quality < 1 || quality > 100) {
+    mg::set_error("invalid arguments (sizes 1..65535, quality 1..100)");
+    return MG_ERR_ARG;
+  }
+  if (cap < bound) {
+    *len = bound;
+    mg::set_error("output buffer smaller than mg_jpeg_encode_bound");
+    return MG_ERR_ARG;
+  }
+  try {
+    std::vector<uint8_t> file;
+    const int st = jpeg_encode(rgb, w, h, stride, quality, threads, file);
+    if (st != MG_OK) return st;
+    if (file.size() > cap) {  // cannot happen within the bound; kept as a guard
+      mg::set_error("JPEG larger than its bound");
+      return MG_ERR_ARG;
+    }
+    std::memcpy(out, file.data(), file.size());
+    *len = file.size();
+    return MG_OK;
+  } catch (const std::bad_alloc&) {
+    mg::set_error("out of host memory");
+    return MG_ERR_OOM;
+  } catch (const std::exception& e) {
+    mg::set_error(e.what());
+    return MG_ERR_ARG;
+  }
 }
 
 }  // extern "C"

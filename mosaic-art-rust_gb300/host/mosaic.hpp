@@ -14,8 +14,8 @@
 //   ColorAdjustment /
 //   calculate_optimal_adjustment            color_adjustment.rs:6-154
 //   generate_mosaic                         main.rs:105-164 + 477-685
-//   open_image / open_png / save_png        main.rs:492, 548, 672 (image::open
-//                                           + to_rgb8, DynamicImage::save)
+//   open_image / open_png / save_png /      main.rs:492, 548, 672 (image::open
+//   save_jpeg / save_image                  + to_rgb8, DynamicImage::save)
 //   read_material_files                     main.rs:166-206 (load_tiles' files)
 //   generate_mosaic_files                   main.rs:105-164 + 477-685 from paths
 // plus RAII handles for the resident palette, batches and the request loop.
@@ -257,6 +257,32 @@ inline void save_png(const RgbImageView& img, const Path& path, int level = 1, i
   std::ofstream f(path, std::ios::binary | std::ios::trunc);
   if (!f || !f.write(reinterpret_cast<const char*>(data.data()), (std::streamsize)data.size()))
     throw Error(MG_ERR_ARG, "cannot write " + path.string());
+}
+
+// main.rs:672 for a .jpg / .jpeg path: image's JPEG encoder (quality 75 by
+// default); this library's baseline encoder (mg_jpeg_encode).
+inline std::vector<uint8_t> encode_jpeg(const RgbImageView& img, int quality = 75, int threads = 0) {
+  std::vector<uint8_t> out(mg_jpeg_encode_bound(img.width, img.height));
+  size_t len = 0;
+  detail::check(mg_jpeg_encode(img.data, img.width, img.height, img.row_bytes(), quality, threads, out.data(),
+                               out.size(), &len));
+  out.resize(len);
+  return out;
+}
+inline void save_jpeg(const RgbImageView& img, const Path& path, int quality = 75, int threads = 0) {
+  const std::vector<uint8_t> data = encode_jpeg(img, quality, threads);
+  std::ofstream f(path, std::ios::binary | std::ios::trunc);
+  if (!f || !f.write(reinterpret_cast<const char*>(data.data()), (std::streamsize)data.size()))
+    throw Error(MG_ERR_ARG, "cannot write " + path.string());
+}
+// main.rs:672 output_img.save(path): the format from the extension (any
+// case): .png (level 1) or .jpg / .jpeg (quality 75); other formats throw.
+inline void save_image(const RgbImageView& img, const Path& path, int threads = 0) {
+  std::string ext = path.extension().string();
+  for (char& c : ext) c = (char)std::tolower((unsigned char)c);
+  if (ext == ".png") save_png(img, path, 1, threads);
+  else if (ext == ".jpg" || ext == ".jpeg") save_jpeg(img, path, 75, threads);
+  else throw Error(MG_ERR_ARG, "only PNG and JPEG output is written: " + path.string());
 }
 
 // similarity.rs:141-146
@@ -1055,10 +1081,11 @@ inline MosaicOutput generate_mosaic(const RgbImageView& target, const std::vecto
 
 // main.rs:105-164 + 477-685 from files: the target (PNG or JPEG), the
 // material folder (read_material_files on up to `threads` host threads) and,
-// when output_path is not empty, the mosaic saved there as PNG after creating
-// its parent folders (main.rs:667-672; the crate picks the format by
-// extension, and only .png is written here: any other fails with MG_ERR_ARG
-// before any work).  Files skipped while reading are listed in *skipped.
+// when output_path is not empty, the mosaic saved there after creating its
+// parent folders (main.rs:667-672; the format by extension as the crate picks
+// it: save_image writes .png and .jpg / .jpeg, any other fails with
+// MG_ERR_ARG before any work).  Files skipped while reading are listed in
+// *skipped.
 inline MosaicOutput generate_mosaic_files(const Path& target_path, const Path& material_dir, const Path& output_path,
                                           const MosaicOptions& o, int threads = 0,
                                           std::vector<std::pair<Path, std::string>>* skipped = nullptr,
@@ -1066,7 +1093,8 @@ inline MosaicOutput generate_mosaic_files(const Path& target_path, const Path& m
   if (!output_path.empty()) {
     std::string ext = output_path.extension().string();
     for (char& c : ext) c = (char)std::tolower((unsigned char)c);
-    if (ext != ".png") throw Error(MG_ERR_ARG, "only PNG output is written: " + output_path.string());
+    if (ext != ".png" && ext != ".jpg" && ext != ".jpeg")
+      throw Error(MG_ERR_ARG, "only PNG and JPEG output is written: " + output_path.string());
   }
   const RgbImage target = open_image(target_path);
   const MaterialFiles m = read_material_files(material_dir, threads);
@@ -1074,7 +1102,7 @@ inline MosaicOutput generate_mosaic_files(const Path& target_path, const Path& m
   MosaicOutput out = generate_mosaic(target.view(), m.views(), m.paths, o, nullptr, ctx);
   if (!output_path.empty()) {
     if (output_path.has_parent_path()) std::filesystem::create_directories(output_path.parent_path());
-    save_png(out.image.view(), output_path, 1, threads);
+    save_image(out.image.view(), output_path, threads);
   }
   return out;
 }

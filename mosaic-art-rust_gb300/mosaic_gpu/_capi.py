@@ -158,6 +158,9 @@ SIGNATURES = [
     ("mg_png_decode_batch", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(C.c_size_t), C.c_int, C.POINTER(_u8p),
                                       _i64p, C.c_int, C.POINTER(C.c_int)]),
     ("mg_png_encode_bound", C.c_size_t, [C.c_int, C.c_int]),
+    ("mg_jpeg_encode_bound", C.c_size_t, [C.c_int, C.c_int]),
+    ("mg_jpeg_encode", C.c_int, [_u8p, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_int, _u8p, C.c_size_t,
+                                 C.POINTER(C.c_size_t)]),
     ("mg_png_encode", C.c_int, [_u8p, C.c_int, C.c_int, C.c_int64, C.c_int, C.c_int, _u8p, C.c_size_t,
                                 C.POINTER(C.c_size_t)]),
     ("mg_similarity_build", C.c_int, [C.c_void_p, _f32p, C.c_int, C.c_int, _f32p]),
@@ -485,6 +488,18 @@ def png_decode_batch(files: list[bytes], threads: int = 0) -> tuple[list[np.ndar
     load().mg_png_decode_batch(data, sizes, n, out_p, strides, threads, status)
     codes = [status[i] for i in range(n)]
     return [o if c == MG_OK else None for o, c in zip(outs, codes)], codes
+
+
+def jpeg_encode(img: np.ndarray, quality: int = 75, threads: int = 0) -> bytes:
+    img = np.ascontiguousarray(img, np.uint8)
+    h, w = img.shape[:2]
+    lib = load()
+    cap = lib.mg_jpeg_encode_bound(w, h)
+    out = np.empty(max(cap, 1), np.uint8)
+    n = C.c_size_t()
+    check(lib.mg_jpeg_encode(ptr(img, C.c_uint8), w, h, img.strides[0], quality, threads, ptr(out, C.c_uint8), cap,
+                             C.byref(n)))
+    return out[: n.value].tobytes()
 
 
 def png_encode(img: np.ndarray, level: int = 1, threads: int = 0) -> bytes:

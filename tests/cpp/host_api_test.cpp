@@ -620,6 +620,39 @@ static RgbImage solid_image(int w, int h, uint8_t r, uint8_t g, uint8_t b) {
   return img;
 }
 
+// main.rs:672 DynamicImage::save: the format from the extension.
+static void save_image_tests() {
+  const Path dir = tmp_file("_save");
+  std::filesystem::remove_all(dir);
+  std::filesystem::create_directories(dir);
+  RgbImage img = solid_image(37, 21, 0, 0, 0);
+  for (int y = 0; y < 21; ++y)
+    for (int x = 0; x < 37; ++x) {
+      const uint8_t g = (uint8_t)(60 + 3 * x + 2 * y);
+      uint8_t* p = img.pixels.data() + 3 * (y * 37 + x);
+      p[0] = p[1] = p[2] = g;
+    }
+  save_image(img.view(), dir / "a.png");
+  save_image(img.view(), dir / "b.jpeg");
+  save_image(img.view(), dir / "c.JpG");
+  CHECK(open_png(dir / "a.png").pixels == img.pixels);
+  for (const char* n : {"b.jpeg", "c.JpG"}) {
+    const RgbImage back = open_image(dir / n);
+    int worst = 0;
+    for (size_t i = 0; i < img.pixels.size(); ++i) worst = std::max(worst, std::abs((int)back.pixels[i] - img.pixels[i]));
+    CHECK(back.width == 37 && back.height == 21 && worst <= 8);  // grey ramp at quality 75
+  }
+  CHECK(detail::read_file(dir / "b.jpeg") == encode_jpeg(img.view(), 75));
+  bool threw = false;
+  try {
+    save_image(img.view(), dir / "d.bmp");
+  } catch (const Error& e) {
+    threw = e.code() == MG_ERR_ARG;
+  }
+  CHECK(threw && !std::filesystem::exists(dir / "d.bmp"));
+  std::filesystem::remove_all(dir);
+}
+
 static void material_file_tests() {  // main.rs:166-206 load_tiles' files (extensions, skipped files)
   const Path dir = tmp_file("_materials");
   std::filesystem::remove_all(dir);
@@ -697,9 +730,16 @@ static void generate_files_tests() {  // main.rs:105-164 + 477-685 from files
   CHECK(a.image.pixels == b.image.pixels);
   const RgbImage saved = open_png(out_path);
   CHECK(saved.width == 96 && saved.height == 72 && saved.pixels == a.image.pixels);
+  // main.rs:672 picks the format by extension: a .jpg path is a JPEG file
+  const MosaicOutput j = generate_mosaic_files(dir / "target.png", dir / "materials", dir / "mosaic.JPG", o);
+  CHECK(j.image.pixels == a.image.pixels);
+  const std::vector<uint8_t> jf = detail::read_file(dir / "mosaic.JPG");
+  CHECK(jf.size() > 3 && jf[0] == 0xFF && jf[1] == 0xD8 && jf[2] == 0xFF);
+  const RgbImage back = open_image(dir / "mosaic.JPG");
+  CHECK(back.width == 96 && back.height == 72);
   bool threw = false;
   try {
-    generate_mosaic_files(dir / "target.png", dir / "materials", dir / "mosaic.jpg", o);
+    generate_mosaic_files(dir / "target.png", dir / "materials", dir / "mosaic.bmp", o);
   } catch (const Error& e) {
     threw = e.code() == MG_ERR_ARG;
   }
@@ -718,6 +758,7 @@ int main(int argc, char** argv) {
   color_host_tests();
   result_tests();
   png_tests();
+  save_image_tests();
   material_file_tests();
   if (gpu) {
     average_lab_tests();

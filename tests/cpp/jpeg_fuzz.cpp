@@ -6,7 +6,8 @@
 // before the first scan: frame, tables, restart interval) so that broken
 // tables and sampling factors reach the entropy decoder.  Every result must
 // be a status code; the sanitizers turn any out-of-bounds access or undefined
-// operation into a failed run.
+// operation into a failed run.  Then the encoder writes random images of
+// random small sizes and qualities, each decoded back.
 //
 //   jpeg_fuzz ITERATIONS SEED.jpg...
 #include <cstdio>
@@ -77,6 +78,21 @@ int main(int argc, char** argv) {
       if (muts == 0 && rc != MG_OK) return 1;  // an unmutated seed must decode
     }
   }
-  std::printf("decoded %ld rejected %ld\n", decoded, rejected);
+  // the encoder on random images of every small size (edges, partial MCUs),
+  // each file decoded back
+  long encoded = 0;
+  for (int it = 0; it < 300; ++it) {
+    const int w = 1 + (int)(rng() % 70), h = 1 + (int)(rng() % 70), q = 1 + (int)(rng() % 100);
+    std::vector<uint8_t> img((size_t)w * h * 3);
+    for (auto& v : img) v = (uint8_t)rng();
+    std::vector<uint8_t> file(mg_jpeg_encode_bound(w, h));
+    size_t len = 0;
+    if (mg_jpeg_encode(img.data(), w, h, 3ll * w, q, 1 + (int)(rng() % 4), file.data(), file.size(), &len) != MG_OK)
+      return 1;
+    std::vector<uint8_t> back((size_t)w * h * 3);
+    if (mg_image_decode(file.data(), len, back.data(), 3ll * w) != MG_OK) return 1;
+    ++encoded;
+  }
+  std::printf("decoded %ld rejected %ld encoded %ld\n", decoded, rejected, encoded);
   return 0;
 }

@@ -551,6 +551,106 @@ def test_defects_fail_cleanly(capi):
     assert code(b"GIF89a") == _capi.MG_ERR_ARG and b"neither" in lib.mg_last_error()
 
 
+# ---- the encoder (main.rs:672 save of a .jpg path) ------------------------------------
+def _grey_wave(rng, w, h):
+    y, x = np.mgrid[0:h, 0:w]
+    g = np.clip(128 + 100 * np.sin(x / 17.0) * np.cos(y / 11.0) + rng.integers(-2, 3, (h, w)), 0, 255)
+    return np.repeat(g.astype(np.uint8)[..., None], 3, axis=2)
+
+
+def _segments(data):
+    """(marker, body) of every segment before the scan data, and the scan's bytes."""
+    pos, out = 2, []
+    while True:
+        m = data[pos + 1]
+        n = struct.unpack(">H", data[pos + 2:pos + 4])[0]
+        out.append((m, data[pos + 4:pos + 2 + n]))
+        pos += 2 + n
+        if m == 0xDA:
+            return out, data[pos:]
+
+
+@pytest.mark.parametrize("size", [(1, 1), (7, 5), (17, 16), (64, 48), (250, 3), (333, 211)])
+def test_encode_round_trips_through_the_decoder(capi, size):
+    """Grey images (so the 4:2:0 chroma loses nothing): at quality 100 (every
+    quantiser 1) the forward and inverse DCT and the rounding leave at most one
+    level; lower qualities stay within their quantisation."""
+    rng = np.random.default_rng(size[0] + 31 * size[1])
+    img = _grey_wave(rng, *size)
+    for q, worst, psnr_min in ((100, 1, 55.0), (95, 6, 42.0), (75, 10, 38.0), (50, 14, 35.0)):
+        data = capi.jpeg_encode(img, q)
+        assert capi.image_info(data) == size
+        got = capi.image_decode(data)
+        err = got.astype(np.int32) - img.astype(np.int32)
+        assert np.abs(err).max() <= worst, (q, np.abs(err).max())
+        mse = float(np.mean(err.astype(np.float64) ** 2))
+        assert mse == 0 or 10 * math.log10(255 ** 2 / mse) >= psnr_min, (q, mse)
+
+
+def test_encode_colour_subsampled(capi):
+    """Colour: chroma averaged over 2x2 boxes (4:2:0), so a smooth colour image
+    comes back close and solid colours almost exactly."""
+    rng = np.random.default_rng(8)
+    y, x = np.mgrid[0:90, 0:120]
+    img = np.stack([120 + 80 * np.sin(x / 23.0), 128 + 90 * np.cos(y / 19.0), 60 + x // 3], -1)
+    img = np.clip(img + rng.integers(-2, 3, img.shape), 0, 255).astype(np.uint8)
+    got = capi.image_decode(capi.jpeg_encode(img, 95))
+    err = got.astype(np.float64) - img.astype(np.float64)
+    assert 10 * math.log10(255 ** 2 / np.mean(err ** 2)) >= 36.0
+    for rgb in ((255, 0, 0), (0, 255, 0), (0, 0, 255), (12, 200, 77)):
+        solid = np.zeros((24, 40, 3), np.uint8) + np.array(rgb, np.uint8)
+        got = capi.image_decode(capi.jpeg_encode(solid, 90))
+        assert np.abs(got.astype(np.int16) - solid.astype(np.int16)).max() <= 3, rgb
+
+
+def test_encode_layout(capi):
+    """Baseline JFIF: the Annex K tables scaled by quality (the IJG rule), 4:2:0
+    sampling, one restart interval per MCU row (RSTn in order between rows),
+    the same bytes on one thread as on many."""
+    rng = np.random.default_rng(4)
+    img = _grey_wave(rng, 100, 70)
+    luma = [16, 11, 10, 16, 24, 40, 51, 61, 12, 12, 14, 19, 26, 58, 60, 55, 14, 13, 16, 24, 40, 57, 69, 56, 14, 17,
+            22, 29, 51, 87, 80, 62, 18, 22, 37, 56, 68, 109, 103, 77, 24, 35, 55, 64, 81, 104, 113, 92, 49, 64, 78,
+            87, 103, 121, 120, 101, 72, 92, 95, 98, 112, 100, 103, 99]
+    for q in (1, 50, 75, 100):
+        data = capi.jpeg_encode(img, q)
+        segs, scan = _segments(data)
+        kinds = [m for m, _ in segs]
+        assert kinds == [0xE0, 0xDB, 0xC0, 0xC4, 0xDD, 0xDA]
+        dqt = dict(segs)[0xDB]
+        zz_luma = np.frombuffer(dqt[1:65], np.uint8).astype(int)
+        nat = np.zeros(64, int)
+        nat[ZIGZAG] = zz_luma
+        scale = 5000 // q if q < 50 else 200 - 2 * q
+        assert list(nat) == [min(255, max(1, (v * scale + 50) // 100)) for v in luma], q
+        sof = dict(segs)[0xC0]
+        assert sof[5] == 3 and sof[7] == 0x22 and sof[10] == 0x11 and sof[13] == 0x11
+        assert struct.unpack(">H", dict(segs)[0xDD])[0] == -(-100 // 16)  # MCUs per row
+        rst = [scan[i + 1] for i in range(len(scan) - 1) if scan[i] == 0xFF and 0xD0 <= scan[i + 1] <= 0xD7]
+        assert rst == [0xD0 + (i & 7) for i in range(-(-70 // 16) - 1)]
+    assert capi.jpeg_encode(img, 80, threads=1) == capi.jpeg_encode(img, 80, threads=7)
+
+
+def test_encode_arguments(capi):
+    from mosaic_gpu import _capi
+
+    lib = _capi.load()
+    img = np.zeros((8, 8, 3), np.uint8)
+    out = np.zeros(1 << 16, np.uint8)
+    n = np.ctypeslib.ctypes.c_size_t()
+    u8 = np.ctypeslib.ctypes.c_uint8
+
+    def enc(w, h, stride, q, cap):
+        return lib.mg_jpeg_encode(_capi.ptr(img, u8), w, h, stride, q, 1, _capi.ptr(out, u8), cap,
+                                  np.ctypeslib.ctypes.byref(n))
+
+    assert enc(8, 8, 24, 75, out.size) == _capi.MG_OK and n.value > 0
+    for args in ((8, 8, 24, 0, out.size), (8, 8, 24, 101, out.size), (0, 8, 24, 75, out.size), (8, 8, 23, 75, out.size),
+                 (70000, 1, 210000, 75, out.size)):
+        assert enc(*args) == _capi.MG_ERR_ARG, args
+    assert enc(8, 8, 24, 75, 10) == _capi.MG_ERR_ARG and n.value == lib.mg_jpeg_encode_bound(8, 8)
+
+
 def test_batch_decodes_png_and_jpeg(capi):
     rng = np.random.default_rng(11)
     imgs = [_image(rng, 33, 21, "smooth"), _image(rng, 16, 16, "noise")]
