@@ -230,19 +230,30 @@ for _ in range(3):
     t0 = time.perf_counter()
     capi.png_decode(data, out)
     dec_ms = min(dec_ms, 1000 * (time.perf_counter() - t0))
+t0 = time.perf_counter()
+jdata = capi.jpeg_encode(target, quality=75, threads=0)
+jenc_ms = 1000 * (time.perf_counter() - t0)
+jdec_ms = float("inf")
+for _ in range(3):
+    t0 = time.perf_counter()
+    back = capi.image_decode(jdata)
+    jdec_ms = min(jdec_ms, 1000 * (time.perf_counter() - t0))
 print(json.dumps({"png_bytes": len(data), "encode_ms": round(enc_ms, 2), "decode_ms": round(dec_ms, 2),
-                  "round_trip_exact": bool(np.array_equal(out, target))}))
+                  "round_trip_exact": bool(np.array_equal(out, target)),
+                  "jpeg": {"bytes": len(jdata), "quality": 75, "encode_ms": round(jenc_ms, 2),
+                           "decode_ms": round(jdec_ms, 2), "decoded_shape_ok": back.shape == target.shape}}))
 """
 
 
 def file_ends(target):
     """The path's file ends on this machine's host cores, beside the step (not
     part of `value` or `e2e`): the workload's target encoded as PNG (level 1,
-    all threads) and decoded back (best of three), with the round trip checked.
-    Run in a child process so that nothing in it can cost the bench line."""
+    all threads) and decoded back (best of three), with the round trip checked;
+    and as JPEG (quality 75, the crate's default for a .jpg output) and decoded
+    back.  Run in a child process so that nothing in it can cost the bench line."""
     import numpy as np
 
-    info = {"what": "PNG encode (level 1, all host threads) and decode of the target",
+    info = {"what": "PNG encode (level 1, all host threads) and decode of the target; JPEG (quality 75) the same",
             "pixels_bytes": int(target.nbytes), "host_threads": os.cpu_count()}
     try:
         with tempfile.TemporaryDirectory() as d:
