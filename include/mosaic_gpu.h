@@ -148,8 +148,9 @@ int mg_png_encode(const uint8_t* rgb, int w, int h, int64_t stride, int level, i
 /* main.rs:172-185, 492, 548: load_tiles also takes jpg/jpeg materials, opened
  * by image::open (zune-jpeg 0.4.18).  This library's own decoder (ITU-T T.81,
  * JFIF): Huffman JPEG with 8-bit samples, sequential (baseline and extended)
- * and progressive (spectral selection, successive approximation), grey or
- * YCbCr with sampling factors 1 or 2, restart intervals; lossless,
+ * and progressive (spectral selection, successive approximation), grey,
+ * YCbCr or RGB-coded (Adobe transform 0, or 'R' 'G' 'B' components without
+ * JFIF) with sampling factors 1 or 2, restart intervals; lossless,
  * hierarchical and arithmetic-coded files fail with MG_ERR_ARG.  The inverse DCT
  * is the FP32 separable form of T.81 A.3.3, chroma is upsampled by
  * replication and converted with the JFIF equations, so pixels may differ

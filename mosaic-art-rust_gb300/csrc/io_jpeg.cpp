@@ -11,7 +11,9 @@
 //     scans with end-of-band runs, AC refinement scans with correction bits);
 //     lossless, hierarchical and arithmetic-coded files are refused with
 //     MG_ERR_ARG;
-//   * one component (grey, replicated to RGB) or three (YCbCr per JFIF);
+//   * one component (grey, replicated to RGB) or three (YCbCr per JFIF, or
+//     R, G, B when an Adobe segment says "no transform" or, without JFIF or
+//     Adobe segments, the components are named 'R', 'G', 'B');
 //     sampling factors 1 or 2 in each direction; interleaved and
 //     one-component scans; 8- and 16-bit quantisation tables; restart
 //     intervals;
@@ -202,6 +204,8 @@ struct Decoder {
   int width = 0, height = 0, ncomp = 0, hmax = 1, vmax = 1, mcux = 0, mcuy = 0;
   bool have_frame = false;
   bool progressive = false;
+  bool jfif = false;         // an APP0 "JFIF" segment (YCbCr by definition)
+  int adobe_transform = -1;  // the APP14 "Adobe" segment's colour transform, -1 without one
   // the current progressive scan: spectral band ss..se, successive approximation ah / al
   int ss = 0, se = 63, ah = 0, al = 0;
   int eobrun = 0;  // blocks left in the current end-of-band run
@@ -573,8 +577,12 @@ struct Decoder {
         scanned = true;
       } else if (m == 0xDC) {
         return err.bad("DNL (height defined later) is not supported");
+      } else if (m == 0xE0 && sl >= 5 && std::memcmp(s, "JFIF", 5) == 0) {
+        jfif = true;
+      } else if (m == 0xEE && sl >= 12 && std::memcmp(s, "Adobe", 5) == 0) {
+        adobe_transform = s[11];  // 0: no colour transform, 1: YCbCr, 2: YCCK
       }
-      // APPn, COM and the rest: skipped
+      // other APPn, COM and the rest: skipped
     }
     if (!have_frame) return err.bad("no frame header");
     if (!scanned) return err.bad("no scan");
@@ -610,6 +618,15 @@ struct Decoder {
     }
   }
 
+  // Three components stored as R, G, B rather than YCbCr: an Adobe segment
+  // saying "no transform", or no JFIF or Adobe segment and components named
+  // 'R', 'G', 'B' (the conventions of T.872 and libjpeg-era writers).
+  bool rgb_samples() const {
+    if (ncomp != 3) return false;
+    if (adobe_transform >= 0) return adobe_transform == 0;
+    return !jfif && comp[0].id == 'R' && comp[1].id == 'G' && comp[2].id == 'B';
+  }
+
   bool output(uint8_t* out, int64_t stride) {
     float ct[8][8];  // ct[u][x] = C(u)/2 cos((2x+1) u pi / 16)
     for (int x = 0; x < 8; ++x)
@@ -630,6 +647,18 @@ struct Decoder {
       if (ncomp == 1) {
         const uint8_t* p = plane[0].data() + (size_t)y * comp[0].bw * 8;
         for (int x = 0; x < width; ++x) o[3 * x] = o[3 * x + 1] = o[3 * x + 2] = p[x];
+        continue;
+      }
+      if (rgb_samples()) {  // three components that are R, G and B themselves
+        const uint8_t* row[3];
+        int sh[3];
+        for (int i = 0; i < 3; ++i) {
+          const Component& c = comp[i];
+          row[i] = plane[i].data() + (size_t)(y * c.v / vmax) * c.bw * 8;
+          sh[i] = hmax / c.h == 2 ? 1 : 0;
+        }
+        for (int x = 0; x < width; ++x)
+          for (int i = 0; i < 3; ++i) o[3 * x + i] = row[i][x >> sh[i]];
         continue;
       }
       const uint8_t* row[3];

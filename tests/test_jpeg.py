@@ -119,12 +119,16 @@ def _segment(marker, payload):
     return bytes([0xFF, marker]) + struct.pack(">H", len(payload) + 2) + payload
 
 
-def _coefficients(img, sampling, quant, grey):
+def _coefficients(img, sampling, quant, grey, rgb_ids=None):
     """The quantised DCT coefficients of each component: ({cid: (bh, bw, 64) natural
-    order}, [(cid, h, v)], {cid: the component's own block grid (bx, by)}, mcux, mcuy)."""
+    order}, [(cid, h, v)], {cid: the component's own block grid (bx, by)}, mcux, mcuy).
+    rgb_ids: the three component ids of an image stored as R, G, B (no YCbCr)."""
     if grey:
         planes = [img.astype(np.float64)]
         comps = [(1, 1, 1)]
+    elif rgb_ids:
+        planes = [img[..., i].astype(np.float64) for i in range(3)]
+        comps = [(rgb_ids[0], sampling[0], sampling[1]), (rgb_ids[1], 1, 1), (rgb_ids[2], 1, 1)]
     else:
         r, g, b = (img[..., i].astype(np.float64) for i in range(3))
         y = np.clip(np.floor(0.299 * r + 0.587 * g + 0.114 * b + 0.5), 0, 255)
@@ -168,21 +172,27 @@ def _unit_order(cid_list, comps, scan_blocks, mcux, mcuy):
     return units
 
 
-def _headers(comps, quant, grey, H, W, sof_marker):
-    out = b"\xff\xd8" + _segment(0xE0, b"JFIF\x00\x01\x02\x00\x00\x01\x00\x01\x00\x00")
+def _headers(comps, quant, grey, H, W, sof_marker, app="jfif"):
+    """app: "jfif" (an APP0 JFIF segment), "adobe0" / "adobe1" (an APP14 Adobe
+    segment, colour transform 0 or 1, no JFIF) or "none"."""
+    out = b"\xff\xd8"
+    if app == "jfif":
+        out += _segment(0xE0, b"JFIF\x00\x01\x02\x00\x00\x01\x00\x01\x00\x00")
+    elif app.startswith("adobe"):
+        out += _segment(0xEE, b"Adobe" + struct.pack(">HHHB", 100, 0, 0, int(app[-1])))
     out += _segment(0xDB, bytes([0]) + bytes([quant] * 64) + (bytes([1]) + bytes([quant] * 64) if not grey else b""))
     sof = struct.pack(">BHHB", 8, H, W, len(comps))
     for cid, hs, vs in comps:
-        sof += bytes([cid, (hs << 4) | vs, 0 if cid == 1 else 1])
+        sof += bytes([cid, (hs << 4) | vs, 0 if cid == comps[0][0] else 1])
     return out + _segment(sof_marker, sof)
 
 
-def encode_jpeg(img, sampling=(1, 1), quant=1, restart=0, interleaved=True, grey=False):
+def encode_jpeg(img, sampling=(1, 1), quant=1, restart=0, interleaved=True, grey=False, rgb_ids=None, app="jfif"):
     """img: (h, w, 3) uint8 (or (h, w) for grey).  sampling: the luma factors (h, v)
     with chroma at 1x1.  quant: one quantiser for every coefficient.  Returns
     (file bytes, {component: quantised coefficients (bh, bw, 64) natural order}, planes)."""
     H, W = img.shape[:2]
-    coefs, comps, scan_blocks, mcux, mcuy = _coefficients(img, sampling, quant, grey)
+    coefs, comps, scan_blocks, mcux, mcuy = _coefficients(img, sampling, quant, grey, rgb_ids)
 
     # entropy-code the scans, collecting symbols first for the Huffman codes
     def mcu_order(cid_list):
@@ -202,7 +212,7 @@ def encode_jpeg(img, sampling=(1, 1), quant=1, restart=0, interleaved=True, grey
         return units, mcux * mcuy
 
     scans = [[c[0] for c in comps]] if interleaved or grey else [[c[0]] for c in comps]
-    tables = {cid: (0 if cid == 1 else 1) for cid, _, _ in comps}
+    tables = {cid: (0 if cid == comps[0][0] else 1) for cid, _, _ in comps}
     symbols = {("dc", 0): {}, ("dc", 1): {}, ("ac", 0): {}, ("ac", 1): {}}
     streams = []
     for sc in scans:
@@ -249,7 +259,7 @@ def encode_jpeg(img, sampling=(1, 1), quant=1, restart=0, interleaved=True, grey
         counts, order, code = _canonical(_huffman_lengths(freq))
         codes[(kind, t)] = code
         dht += bytes([(0 if kind == "dc" else 16) | t]) + bytes(counts) + bytes(order)
-    out = _headers(comps, quant, grey, H, W, 0xC0) + _segment(0xC4, dht)
+    out = _headers(comps, quant, grey, H, W, 0xC0, app) + _segment(0xC4, dht)
     if restart:
         out += _segment(0xDD, struct.pack(">H", restart))
     for sc, events in streams:
@@ -404,7 +414,7 @@ def encode_jpeg_progressive(img, sampling=(1, 1), quant=1, restart=0, grey=False
     return out + b"\xff\xd9", coefs, comps
 
 
-def decode_restated(coefs, comps, quant, W, H):
+def decode_restated(coefs, comps, quant, W, H, rgb=False):
     """The decoder's output steps in float32, in its order: dequantise, rows then
     columns of the T.81 A.3.3 inverse DCT, + 128, round, clamp; replicate chroma;
     JFIF colour equations; round, clamp."""
@@ -442,6 +452,8 @@ def decode_restated(coefs, comps, quant, W, H):
     for cid, hs, vs in comps:
         p = planes[cid]
         chan.append(p[(ys * vs // vmax)[:, None], (xs // (hmax // hs))[None, :]].astype(np.float32))
+    if rgb:  # stored as R, G, B: the samples themselves
+        return np.stack(chan, -1).astype(np.uint8)
     Y, cb, cr = chan[0], chan[1] - np.float32(128), chan[2] - np.float32(128)
     rgb = [Y + np.float32(1.402) * cr, Y - np.float32(0.344136) * cb - np.float32(0.714136) * cr,
            Y + np.float32(1.772) * cb]
@@ -501,6 +513,22 @@ def test_progressive_decodes_like_the_sequential_file(capi, sampling, quant, res
         got = capi.image_decode(data)
         assert np.array_equal(got, capi.image_decode(seq)), (kind, sampling, restart, script is None)
         assert np.array_equal(got, decode_restated(coefs, comps, quant, *size)), kind
+
+
+@pytest.mark.parametrize("ids,app,is_rgb", [((82, 71, 66), "none", True), ((1, 2, 3), "adobe0", True),
+                                             ((82, 71, 66), "adobe0", True), ((82, 71, 66), "jfif", False),
+                                             ((1, 2, 3), "adobe1", False), ((1, 2, 3), "none", False)])
+def test_rgb_coded_files(capi, ids, app, is_rgb):
+    """Three components stored as R, G, B (no YCbCr): an Adobe segment with
+    colour transform 0, or no JFIF / Adobe segment and components named 'R',
+    'G', 'B'; a JFIF segment or an Adobe transform of 1 means YCbCr whatever the
+    names."""
+    rng = np.random.default_rng(sum(ids) + len(app))
+    img = _image(rng, 45, 31, "smooth")
+    for sampling in ((1, 1), (2, 2)):
+        data, coefs, comps = encode_jpeg(img, sampling, 2, 0, True, rgb_ids=ids, app=app)
+        got = capi.image_decode(data)
+        assert np.array_equal(got, decode_restated(coefs, comps, 2, 45, 31, rgb=is_rgb)), sampling
 
 
 def test_grey_blocks_decode_exactly(capi):
